@@ -1,0 +1,152 @@
+/*
+ * jues_gpu.h -- C ABI of libjuesgpu.so, the GB300 (sm_103a) implementation of the
+ * JuES correlated-method hot path: AO->MO four-index transformation, closed-shell
+ * MP2 energy and closed-shell CCD / CCSD amplitude iterations.
+ *
+ * Conventions (shared by every entry point):
+ *  - All arrays are column-major (Julia layout): element X[i,j,a,b] of a d1 x d2 x d3 x d4
+ *    array sits at offset i + d1*(j + d2*(a + d3*b)).  Julia arrays can be passed as is.
+ *  - Pointers are host pointers unless the name ends in _dev; inputs are borrowed for the
+ *    duration of the call and never modified; outputs are caller-allocated.
+ *  - Every function returns 0 (JUES_OK) or a positive JUES_E* code; jues_last_error()
+ *    gives the message of the last failure on the calling thread.
+ *  - A jues_ctx owns one CUDA stream and every device buffer it allocates.  A context is
+ *    single-threaded; different contexts may be used concurrently.  Calls are synchronous
+ *    at return.
+ *
+ * Reference interfaces replaced (paths within mdav2/JuES.jl):
+ *  jues_tei_transform  <- JuES.Transformation.tei_transform        src/Backend/Transformation.jl:15-20,39-93
+ *  jues_get_eri        <- JuES.IntegralTransformation.get_eri      src/Backend/IntegralTransformation.jl:38-101
+ *  jues_rmp2           <- JuES.MollerPlesset.do_rmp2               src/MollerPlesset/RMP2.jl:11-45
+ *  jues_rccd           <- JuES.CoupledCluster.{mRCCD,RCCD}.do_rccd src/CoupledCluster/mRCCD.jl:38-118, RCCD.jl:33-83
+ *  jues_rccsd          <- JuES.CoupledCluster.{RCCSD,mRCCSD}.do_rccsd  src/CoupledCluster/RCCSD.jl:33-116, mRCCSD.jl:35-101
+ */
+#ifndef JUES_GPU_H
+#define JUES_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define JUES_API __attribute__((visibility("default")))
+#else
+#define JUES_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JUES_OK 0
+#define JUES_EINVAL 1      /* bad argument (dimension, pointer, spec string, option) */
+#define JUES_ENOMEM 2      /* device allocation failed or over the context's memory cap */
+#define JUES_ECUDA 3       /* CUDA runtime / driver error */
+#define JUES_ENOTCONV 4    /* CC iterations hit maxit before the requested convergence */
+#define JUES_ENONFINITE 5  /* a NaN or Inf was found in inputs or iterates */
+#define JUES_ETIMEOUT 6    /* a bounded device-side wait expired (kernel returned early) */
+#define JUES_ENODEV 7      /* no usable sm_103 device */
+
+/* arithmetic used for the bulk of the contractions */
+#define JUES_PREC_FP64 0       /* plain FP64 (the drop-in form)                          */
+#define JUES_PREC_SPLIT_BF16 1 /* tcgen05 BF16 hi+lo, three products, FP32 accumulation  */
+
+/* CC initial amplitudes */
+#define JUES_GUESS_ZERO 0  /* T2 = 0 (mRCCD.jl:239-256); first sweep gives MP2 amplitudes   */
+#define JUES_GUESS_MP2 1   /* T2 = <ij|ab>/D (mRCCSD.jl:66)                                  */
+#define JUES_GUESS_OVOV 2  /* T2 = (ij|ab)/D (RCCD.jl:145-160)                               */
+
+typedef struct jues_ctx jues_ctx;
+typedef struct jues_cc jues_cc;
+
+typedef struct {
+    int maxit;        /* maximum sweeps (reference default 40)                            */
+    double e_conv;    /* |E_k - E_{k-1}| threshold; <= 0 disables                          */
+    double r_conv;    /* ||T_new - T_old||_2 threshold (mRCCD.jl:106); <= 0 disables        */
+    int diis;         /* 0 = plain Jacobi sweeps, 1 = DIIS (mRCCD.jl:138-208, FP64)         */
+    int diis_size;    /* number of stored amplitude vectors (reference max_diis = 6)        */
+    int precision;    /* JUES_PREC_*                                                       */
+    int guess;        /* JUES_GUESS_*                                                      */
+    int refine;       /* split precision only: number of closing FP64 sweeps               */
+} jues_cc_opts;
+
+typedef struct {
+    int iter;         /* 1-based sweep number                                            */
+    int precision;    /* precision that sweep ran in                                     */
+    double energy;    /* correlation energy of the amplitudes carried to the next sweep  */
+    double rnorm;     /* ||T_new - T_old||_2 of the un-extrapolated update               */
+    double ms;        /* device time of the sweep (CUDA events on the context stream)    */
+} jues_iter_log;
+
+/* ---- context ---------------------------------------------------------------------- */
+JUES_API int jues_version(void);
+JUES_API int jues_last_error(char *buf, size_t len);
+JUES_API int jues_ctx_create(int device, jues_ctx **out);
+JUES_API int jues_ctx_destroy(jues_ctx *ctx);
+/* Cap the device memory the context may hold (bytes, 0 = no cap); used to exercise the
+ * out-of-memory path without exhausting the GPU. */
+JUES_API int jues_ctx_set_mem_limit(jues_ctx *ctx, size_t bytes);
+/* Per-kernel CUDA-event timing of the named hot kernels (0 = off). */
+JUES_API int jues_ctx_set_profiling(jues_ctx *ctx, int on);
+/* Total time and launch count recorded for kernels whose name starts with `prefix`. */
+JUES_API int jues_ctx_profile(jues_ctx *ctx, const char *prefix, double *total_ms, long long *launches);
+JUES_API int jues_ctx_profile_reset(jues_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+JUES_API long long jues_ctx_launch_count(jues_ctx *ctx);
+
+/* ---- four-index transformation -------------------------------------------------------
+ * out[i,a,j,b] = sum C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b] gao[mu,nu,lam,sig]
+ * (chemists' (C1 C2|C3 C4)); gao is n^4, Ck is n x dk, out is d1 x d2 x d3 x d4.
+ * Replaces Transformation.jl:39-93 (the 2-argument form :15-20 is C1=C2=C3=C4). */
+JUES_API int jues_tei_transform(jues_ctx *ctx, const double *gao, int n,
+                       const double *C1, int d1, const double *C2, int d2,
+                       const double *C3, int d3, const double *C4, int d4,
+                       int precision, double *out);
+
+/* get_eri(wfn, spec; notation, fcn) for a closed-shell Wfn: spec is 4 chars of o/O/v/V
+ * (lower = beta = alpha blocks for a restricted Wfn); phys != 0 selects physicists'
+ * notation (IntegralTransformation.jl:46-48,96-98); fcn drops the first fcn occupied
+ * columns (:54-59).  out has the block's shape in the requested notation. */
+JUES_API int jues_get_eri(jues_ctx *ctx, const double *gao, int n,
+                 const double *Cocc, int o, const double *Cvir, int v,
+                 const char *spec, int phys, int fcn, int precision, double *out);
+
+/* ---- MP2 -------------------------------------------------------------------------------
+ * E = sum <ij|ab>(2<ij|ab> - <ij|ba>)/(e_i+e_j-e_a-e_b) (RMP2.jl:27-41). eps has n entries,
+ * occupied first.  Optional k_out (o*o*v*v, may be NULL) receives <ij|ab>. */
+JUES_API int jues_rmp2(jues_ctx *ctx, const double *gao, int n,
+              const double *Cocc, int o, const double *Cvir, int v,
+              const double *eps, int precision, double *e_out, double *k_out);
+
+/* ---- coupled cluster ------------------------------------------------------------------
+ * Whole solves.  t2_out (o*o*v*v, [i,j,a,b]) and t1_out (o*v, [i,a]) may be NULL; log may
+ * be NULL, else it receives up to log_cap records.  Returns JUES_ENOTCONV (with e_out,
+ * amplitudes and niter filled) when a convergence threshold was requested and not met. */
+JUES_API int jues_cc_default_opts(jues_cc_opts *opts);
+JUES_API int jues_rccd(jues_ctx *ctx, const double *gao, int n,
+              const double *Cocc, int o, const double *Cvir, int v, const double *eps,
+              const jues_cc_opts *opts, double *e_out, double *t2_out,
+              jues_iter_log *log, int log_cap, int *niter);
+JUES_API int jues_rccsd(jues_ctx *ctx, const double *gao, int n,
+               const double *Cocc, int o, const double *Cvir, int v, const double *eps,
+               const jues_cc_opts *opts, double *e_out, double *t1_out, double *t2_out,
+               jues_iter_log *log, int log_cap, int *niter);
+
+/* Resident CC sessions: integrals and amplitudes stay in device memory between calls, so
+ * a caller can time single sweeps.  method: 0 = CCD, 1 = CCSD.  gao_is_device != 0 means
+ * gao is a device pointer on the context's device. */
+JUES_API int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_device, int n,
+                   const double *Cocc, int o, const double *Cvir, int v, const double *eps,
+                   const jues_cc_opts *opts, jues_cc **out);
+/* Run up to nsweeps sweeps (stopping early on convergence); *done = sweeps run,
+ * *converged = 1 if the thresholds were met. */
+JUES_API int jues_cc_iterate(jues_cc *cc, int nsweeps, int *done, int *converged);
+JUES_API int jues_cc_set_precision(jues_cc *cc, int precision);
+JUES_API int jues_cc_energy(jues_cc *cc, double *e_out);
+JUES_API int jues_cc_amplitudes(jues_cc *cc, double *t1_out, double *t2_out);
+JUES_API int jues_cc_log(jues_cc *cc, jues_iter_log *log, int log_cap, int *count);
+JUES_API int jues_cc_destroy(jues_cc *cc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JUES_GPU_H */

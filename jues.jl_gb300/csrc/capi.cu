@@ -1,0 +1,375 @@
+// extern "C" entry points of libjuesgpu.so (declared in include/jues_gpu.h).
+#include <cstring>
+#include <string>
+
+#include "cc.cuh"
+#include "common.cuh"
+#include "transform.cuh"
+
+using namespace jues;
+
+namespace jues {
+const std::string &last_error();
+}
+
+namespace {
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        f();
+        return JUES_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return JUES_ENOMEM;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return JUES_EINVAL;
+    }
+}
+
+Ctx &C(jues_ctx *c) {
+    if (!c) throw Error(JUES_EINVAL, "null context");
+    return c->impl;
+}
+
+void need(const void *p, const char *what) {
+    if (!p) throw Error(JUES_EINVAL, std::string("null pointer: ") + what);
+}
+
+// copy a host array to a new context buffer
+DBuf<double> h2d(Ctx &ctx, const double *h, size_t n) {
+    DBuf<double> d(&ctx, n);
+    if (n) JUES_CHECK_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+    return d;
+}
+
+void d2h(Ctx &ctx, double *h, const double *d, size_t n) {
+    if (n) JUES_CHECK_CUDA(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+}
+
+void check_dims(int n, int o, int v) {
+    if (n <= 0) throw Error(JUES_EINVAL, "nbf must be positive");
+    if (o <= 0 || v <= 0) throw Error(JUES_EINVAL, "nocc and nvir must be positive");
+    if (o + v > n) throw Error(JUES_EINVAL, "nocc + nvir exceeds nbf");
+}
+
+void check_opts(const jues_cc_opts &o) {
+    if (o.maxit < 0) throw Error(JUES_EINVAL, "maxit must be >= 0");
+    if (o.diis && (o.diis_size < 2 || o.diis_size > 16)) throw Error(JUES_EINVAL, "diis_size must be in 2..16");
+    if (o.precision != JUES_PREC_FP64 && o.precision != JUES_PREC_SPLIT_BF16)
+        throw Error(JUES_EINVAL, "unknown precision");
+    if (o.guess < 0 || o.guess > 2) throw Error(JUES_EINVAL, "unknown guess");
+    if (o.refine < 0) throw Error(JUES_EINVAL, "refine must be >= 0");
+}
+
+}  // namespace
+
+struct jues_cc {
+    CCState *s = nullptr;
+    ~jues_cc() { delete s; }
+};
+
+extern "C" {
+
+int jues_version(void) { return 10000; }
+
+int jues_last_error(char *buf, size_t len) {
+    if (!buf || !len) return JUES_EINVAL;
+    const std::string &m = last_error();
+    size_t k = m.size() < len - 1 ? m.size() : len - 1;
+    std::memcpy(buf, m.data(), k);
+    buf[k] = 0;
+    return JUES_OK;
+}
+
+int jues_ctx_create(int device, jues_ctx **out) {
+    return guarded([&] {
+        need(out, "out");
+        *out = nullptr;
+        int ndev = 0;
+        cudaError_t e = cudaGetDeviceCount(&ndev);
+        if (e != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw Error(JUES_ENODEV, "no CUDA device available");
+        }
+        if (device < 0 || device >= ndev) throw Error(JUES_EINVAL, "device index out of range");
+        cudaDeviceProp prop;
+        JUES_CHECK_CUDA(cudaGetDeviceProperties(&prop, device));
+        if (prop.major != 10 || prop.minor != 3)
+            throw Error(JUES_ENODEV, std::string("libjuesgpu is built for sm_103 (GB300); device is ") +
+                                         prop.name + " sm_" + std::to_string(prop.major) +
+                                         std::to_string(prop.minor));
+        JUES_CHECK_CUDA(cudaSetDevice(device));
+        std::unique_ptr<jues_ctx> c(new jues_ctx());
+        Ctx &x = c->impl;
+        x.device = device;
+        JUES_CHECK_CUDA(cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking));
+        JUES_CHECK_CUDA(cudaMalloc(&x.d_flags, 4 * sizeof(unsigned)));
+        JUES_CHECK_CUDA(cudaMemset(x.d_flags, 0, 4 * sizeof(unsigned)));
+        JUES_CHECK_CUDA(cudaMalloc(&x.d_red, 65536 * sizeof(double)));
+        *out = c.release();
+    });
+}
+
+int jues_ctx_destroy(jues_ctx *ctx) {
+    return guarded([&] {
+        need(ctx, "ctx");
+        cudaSetDevice(ctx->impl.device);
+        delete ctx;
+    });
+}
+
+int jues_ctx_set_mem_limit(jues_ctx *ctx, size_t bytes) {
+    return guarded([&] { C(ctx).mem_limit = bytes; });
+}
+
+int jues_ctx_set_profiling(jues_ctx *ctx, int on) {
+    return guarded([&] { C(ctx).profiling = on != 0; });
+}
+
+int jues_ctx_profile(jues_ctx *ctx, const char *prefix, double *total_ms, long long *launches) {
+    return guarded([&] {
+        Ctx &c = C(ctx);
+        need(prefix, "prefix");
+        c.flush_profile();
+        double t = 0.0;
+        long long n = 0;
+        size_t lp = std::strlen(prefix);
+        for (auto &kv : c.prof) {
+            if (kv.first.compare(0, lp, prefix) == 0) {
+                t += kv.second.total_ms;
+                n += kv.second.launches;
+            }
+        }
+        if (total_ms) *total_ms = t;
+        if (launches) *launches = n;
+    });
+}
+
+int jues_ctx_profile_reset(jues_ctx *ctx) {
+    return guarded([&] {
+        Ctx &c = C(ctx);
+        c.flush_profile();
+        for (auto &kv : c.prof) {
+            kv.second.total_ms = 0.0;
+            kv.second.launches = 0;
+        }
+    });
+}
+
+long long jues_ctx_launch_count(jues_ctx *ctx) { return ctx ? ctx->impl.launches : -1; }
+
+int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1, int d1, const double *C2,
+                       int d2, const double *C3, int d3, const double *C4, int d4, int precision,
+                       double *out) {
+    return guarded([&] {
+        Ctx &c = C(ctx);
+        need(gao, "gao");
+        need(C1, "C1"); need(C2, "C2"); need(C3, "C3"); need(C4, "C4");
+        need(out, "out");
+        if (n <= 0) throw Error(JUES_EINVAL, "nbf must be positive");
+        if (d1 < 0 || d2 < 0 || d3 < 0 || d4 < 0) throw Error(JUES_EINVAL, "negative MO dimension");
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cudaSetDevice(c.device);
+        const size_t n4 = (size_t)n * n * n * n;
+        DBuf<double> g = h2d(c, gao, n4);
+        DBuf<double> c1 = h2d(c, C1, (size_t)n * d1), c2 = h2d(c, C2, (size_t)n * d2),
+                     c3 = h2d(c, C3, (size_t)n * d3), c4 = h2d(c, C4, (size_t)n * d4);
+        const size_t no = (size_t)d1 * d2 * d3 * d4;
+        DBuf<double> dout(&c, no);
+        const double *Cs[4] = {c1.p, c2.p, c3.p, c4.p};
+        int d[4] = {d1, d2, d3, d4};
+        long long ostr[4] = {1, d1, (long long)d1 * d2, (long long)d1 * d2 * d3};
+        transform4(&c, precision, g.p, n, Cs, d, dout.p, ostr, false);
+        d2h(c, out, dout.p, no);
+        c.check_flags();
+    });
+}
+
+int jues_get_eri(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,
+                 const char *spec, int phys, int fcn, int precision, double *out) {
+    return guarded([&] {
+        Ctx &c = C(ctx);
+        need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(spec, "spec"); need(out, "out");
+        if (std::strlen(spec) != 4)
+            throw Error(JUES_EINVAL, std::string("Invalid string given to get_eri: ") + spec);
+        check_dims(n, o, v);
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        size_t no = 1;
+        for (int q = 0; q < 4; ++q) {
+            char ch = spec[q];
+            if (ch == 'o' || ch == 'O') {
+                if (fcn < 0 || fcn > o) throw Error(JUES_EINVAL, "fcn out of range");
+                no *= (size_t)(o - fcn);
+            } else if (ch == 'v' || ch == 'V') {
+                no *= (size_t)v;
+            } else {
+                throw Error(JUES_EINVAL, std::string("Invalid string given to get_eri: ") + spec);
+            }
+        }
+        cudaSetDevice(c.device);
+        DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
+        DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
+        DBuf<double> dout(&c, no);
+        get_eri_block(&c, precision, g.p, n, co.p, o, cv.p, v, spec, phys != 0, fcn, dout.p, false);
+        d2h(c, out, dout.p, no);
+        c.check_flags();
+    });
+}
+
+int jues_rmp2(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,
+              const double *eps, int precision, double *e_out, double *k_out) {
+    return guarded([&] {
+        Ctx &c = C(ctx);
+        need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(e_out, "e_out");
+        check_dims(n, o, v);
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cudaSetDevice(c.device);
+        DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
+        DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
+        DBuf<double> de = h2d(c, eps, (size_t)n);
+        const size_t nk = (size_t)o * o * v * v;
+        DBuf<double> K(&c, nk);
+        get_eri_block(&c, precision, g.p, n, co.p, o, cv.p, v, "OOVV", true, 0, K.p, false);
+        g.reset();
+        *e_out = mp2_energy(&c, K.p, de.p, o, v);
+        if (k_out) d2h(c, k_out, K.p, nk);
+        c.check_flags();
+    });
+}
+
+int jues_cc_default_opts(jues_cc_opts *opts) {
+    return guarded([&] {
+        need(opts, "opts");
+        opts->maxit = 40;        // mRCCD.jl:38
+        opts->e_conv = 0.0;
+        opts->r_conv = 1e-7;     // mRCCD.jl:106
+        opts->diis = 1;          // mRCCD.jl:39
+        opts->diis_size = 6;     // mRCCD.jl:67
+        opts->precision = JUES_PREC_FP64;
+        opts->guess = JUES_GUESS_ZERO;   // mRCCD.jl:245
+        opts->refine = 2;
+    });
+}
+
+int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_device, int n, const double *Cocc,
+                   int o, const double *Cvir, int v, const double *eps, const jues_cc_opts *opts,
+                   jues_cc **out) {
+    return guarded([&] {
+        Ctx &c = C(ctx);
+        need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(out, "out");
+        *out = nullptr;
+        check_dims(n, o, v);
+        jues_cc_opts op;
+        if (opts) op = *opts; else jues_cc_default_opts(&op);
+        check_opts(op);
+        cudaSetDevice(c.device);
+        DBuf<double> g;
+        const double *gp = gao;
+        if (!gao_is_device) {
+            g = h2d(c, gao, (size_t)n * n * n * n);
+            gp = g.p;
+        }
+        DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
+        DBuf<double> de = h2d(c, eps, (size_t)n);
+        std::unique_ptr<jues_cc> cc(new jues_cc());
+        cc->s = cc_create(&c, method, gp, n, co.p, o, cv.p, v, de.p, op);
+        *out = cc.release();
+    });
+}
+
+int jues_cc_iterate(jues_cc *cc, int nsweeps, int *done, int *converged) {
+    return guarded([&] {
+        need(cc, "cc");
+        if (nsweeps < 0) throw Error(JUES_EINVAL, "nsweeps must be >= 0");
+        cudaSetDevice(cc->s->ctx->device);
+        cc_iterate(cc->s, nsweeps, done, converged);
+    });
+}
+
+int jues_cc_set_precision(jues_cc *cc, int precision) {
+    return guarded([&] {
+        need(cc, "cc");
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cc->s->precision = precision;
+        cc->s->refine_left = -1;
+    });
+}
+
+int jues_cc_energy(jues_cc *cc, double *e_out) {
+    return guarded([&] {
+        need(cc, "cc"); need(e_out, "e_out");
+        *e_out = cc->s->energy;
+    });
+}
+
+int jues_cc_amplitudes(jues_cc *cc, double *t1_out, double *t2_out) {
+    return guarded([&] {
+        need(cc, "cc");
+        cudaSetDevice(cc->s->ctx->device);
+        cc_amplitudes(cc->s, t1_out, t2_out);
+    });
+}
+
+int jues_cc_log(jues_cc *cc, jues_iter_log *log, int log_cap, int *count) {
+    return guarded([&] {
+        need(cc, "cc");
+        int m = (int)cc->s->log.size();
+        if (count) *count = m;
+        if (log)
+            for (int k = 0; k < m && k < log_cap; ++k) log[k] = cc->s->log[k];
+    });
+}
+
+int jues_cc_destroy(jues_cc *cc) {
+    return guarded([&] {
+        need(cc, "cc");
+        cudaSetDevice(cc->s->ctx->device);
+        delete cc;
+    });
+}
+
+static int cc_solve(jues_ctx *ctx, int method, const double *gao, int n, const double *Cocc, int o,
+                    const double *Cvir, int v, const double *eps, const jues_cc_opts *opts, double *e_out,
+                    double *t1_out, double *t2_out, jues_iter_log *log, int log_cap, int *niter) {
+    jues_cc *cc = nullptr;
+    int st = jues_cc_create(ctx, method, gao, 0, n, Cocc, o, Cvir, v, eps, opts, &cc);
+    if (st) return st;
+    jues_cc_opts op;
+    if (opts) op = *opts; else jues_cc_default_opts(&op);
+    int done = 0, conv = 0;
+    st = jues_cc_iterate(cc, op.maxit, &done, &conv);
+    if (!st && e_out) st = jues_cc_energy(cc, e_out);
+    if (!st && (t1_out || t2_out)) st = jues_cc_amplitudes(cc, t1_out, t2_out);
+    if (!st && log) st = jues_cc_log(cc, log, log_cap, nullptr);
+    if (niter) *niter = cc ? (int)cc->s->iters : 0;
+    jues_cc_destroy(cc);
+    if (!st && !conv && (op.r_conv > 0 || op.e_conv > 0) && op.maxit > 0) {
+        set_last_error("CC iterations did not converge within maxit");
+        st = JUES_ENOTCONV;
+    }
+    return st;
+}
+
+int jues_rccd(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,
+              const double *eps, const jues_cc_opts *opts, double *e_out, double *t2_out, jues_iter_log *log,
+              int log_cap, int *niter) {
+    return cc_solve(ctx, 0, gao, n, Cocc, o, Cvir, v, eps, opts, e_out, nullptr, t2_out, log, log_cap, niter);
+}
+
+int jues_rccsd(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,
+               const double *eps, const jues_cc_opts *opts, double *e_out, double *t1_out, double *t2_out,
+               jues_iter_log *log, int log_cap, int *niter) {
+    return cc_solve(ctx, 1, gao, n, Cocc, o, Cvir, v, eps, opts, e_out, t1_out, t2_out, log, log_cap, niter);
+}
+
+}  // extern "C"

@@ -1,0 +1,568 @@
+// Closed-shell CCD / CCSD on the device: integrals, sweeps, DIIS, convergence.
+//
+// The equations are those of src/CoupledCluster/RCCD.jl:234-303 (== mRCCD.jl:301-394) and
+// RCCSD.jl:187-289; intermediates as in RCCD.jl:169-467.  Every contraction is one GETT over
+// composite tensor modes, so no permuted copies of T2 are made.  Two exact rewrites reduce the
+// work without changing the result beyond rounding:
+//   * Wabef is never formed: sum_ef T[ij,ef] Wabef[ab,ef] = T.vvvv^T + 1/2 X^T.T with
+//     X[mn,ij] = sum_ef oovv[mn,ef] T[ij,ef]; X also gives Wmnij (= oooo + X/2), so the two
+//     ladders become T.vvvv^T + (oooo + X)^T.T  (2o^2v^4 + 4o^4v^2 instead of 4o^2v^4 + 2o^4v^2);
+//   * the terms of RCCD.jl:243-254 that are images of each other under (i,a)<->(j,b) are
+//     computed once into Z and added as Z[i,j,a,b] + Z[j,i,b,a] by the finalisation kernel.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "cc.cuh"
+#include "transform.cuh"
+
+namespace jues {
+
+double ccd_sweep_flops(int o_, int v_) {
+    double o = o_, v = v_;
+    return 2 * o * o * v * v * v * v + 12 * o * o * o * v * v * v + 4 * o * o * o * o * v * v +
+           4 * o * o * v * v * v + 4 * o * o * o * v * v;
+}
+
+double ccd_reference_flops(int o_, int v_) {
+    double o = o_, v = v_;
+    return 4 * o * o * v * v * v * v + 16 * o * o * o * v * v * v + 4 * o * o * o * o * v * v +
+           6 * o * o * v * v * v + 6 * o * o * o * v * v;
+}
+
+namespace {
+
+// C = alpha * A.B + beta * Cin over the given modes
+void G(CCState *s, int prec, const char *name, long long M, long long N, long long K, double alpha,
+       const double *A, Mode mA, Mode kA, const double *B, Mode kB, Mode nB, double beta, double *C,
+       Mode mC, Mode nC, const double *Cin = nullptr, bool a_const = false, bool b_const = false) {
+    GettArgs g;
+    g.M = M; g.N = N; g.K = K;
+    g.alpha = alpha; g.beta = beta;
+    g.A = A; g.mA = mA; g.kA = kA;
+    g.B = B; g.kB = kB; g.nB = nB;
+    g.C = C; g.mC = mC; g.nC = nC;
+    g.Cin = Cin;
+    g.a_const = a_const; g.b_const = b_const;
+    gett(s->ctx, prec, g, name);
+}
+
+void d2d(Ctx *ctx, double *dst, const double *src, size_t n) {
+    JUES_CHECK_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// CCD sweep (FP64 or split precision for the contractions; everything else FP64)
+// ---------------------------------------------------------------------------------------
+double ccd_sweep(CCState *s, int prec) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v, vv = v * v;
+    const double *T = s->T.p;
+    // T~[i,j,a,b] = 2T[i,j,a,b] - T[j,i,a,b]
+    t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
+    const double *Tt = s->Tt.p;
+    const double *W = s->oovv.p;
+
+    // Fae[a,e] = -sum_{mnf} T~[m,n,a,f] oovv[m,n,e,f]                    (RCCD.jl:179)
+    G(s, prec, "ccd_fae", v, v, oov, -1.0, Tt, plain(oo), mode2(oo, 1, oov), W, mode2(oo, 1, oov),
+      plain(oo), 0.0, s->Fae.p, plain(1), plain(v));
+    // Fmi[m,i] = sum_{nef} oovv[m,n,e,f] T~[i,n,e,f]                      (RCCD.jl:216)
+    G(s, prec, "ccd_fmi", o, o, o * vv, 1.0, W, plain(1), plain(o), Tt, plain(o), plain(1), 0.0,
+      s->Fmi.p, plain(1), plain(o));
+    // W'[mn,ij] = oooo[mn,ij] + sum_ef oovv[mn,ef] T[ij,ef]        (Wmnij + the Wabef T-part)
+    G(s, prec, "ccd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), T, plain(oo), plain(1), 1.0, s->Wp.p,
+      plain(1), plain(oo), s->oooo.p);
+    // L = oovv + (W')^T.T + T.vvvv^T                                     (RCCD.jl:243,245,246)
+    G(s, prec, "ccd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), T, plain(1), plain(oo),
+      1.0, s->L.p, plain(1), plain(oo), W);
+    G(s, prec, "ccd_pp_ladder", oo, vv, vv, 1.0, T, plain(1), plain(oo), s->vvvv.p, plain(vv), plain(1),
+      1.0, s->L.p, plain(1), plain(oo), nullptr, false, true);
+
+    // ring intermediates in (me),(bj) layout
+    // WJ = WmBeJ = ovvo + 1/2 oovv[m,n,e,f] T~[n,j,f,b] - 1/2 oovv[n,m,e,f] T[n,j,f,b]  (RCCD.jl:400)
+    G(s, prec, "ccd_wj", ov, ov, ov, 0.5, W, mode2(o, 1, oo), mode2(o, o, oov), Tt, mode2(o, 1, oo),
+      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p);
+    G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
+      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
+    // WK = WmBEj = -ovov[m,b,j,e] + 1/2 T[j,n,f,b] oovv[n,m,e,f]                  (RCCD.jl:445)
+    G(s, prec, "ccd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
+      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p);
+    // W12 = 2 WJ + WK
+    axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
+
+    // Z: the terms of RCCD.jl:243-254 whose (i,a)<->(j,b) images are added by t2_finalize
+    double *Z = s->Z.p;
+    // + T[i,j,a,e] Fae[b,e]
+    G(s, prec, "ccd_z_fae", oov, v, v, 1.0, T, plain(1), plain(oov), s->Fae.p, plain(v), plain(1), 0.0,
+      Z, plain(1), plain(oov));
+    // - T[i,m,a,b] Fmi[m,j]
+    G(s, prec, "ccd_z_fmi", o * vv, o, o, -1.0, T, mode2(o, 1, oo), plain(o), s->Fmi.p, plain(1),
+      plain(o), 1.0, Z, mode2(o, 1, oo), plain(o));
+    // + T[i,m,a,e] (2WmBeJ + WmBEj)[m,b,e,j]
+    G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
+      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
+    // - T[m,i,a,e] WmBeJ[m,b,e,j]
+    G(s, prec, "ccd_ring", ov, ov, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WJ.p, plain(1),
+      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
+    // + T[m,i,b,e] WmBEj[m,a,e,j]
+    G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
+      plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
+
+    return t2_finalize(ctx, s->L.p, Z, s->eps.p, (int)o, (int)v, T, s->Tn.p);
+}
+
+// ---------------------------------------------------------------------------------------
+// DIIS (mRCCD.jl:138-208) in FP64: keep the last diis_size-1 (amplitude, error) pairs, B[k,l] =
+// e_k.e_l scaled by max|B|, bordered by -1/0, c = B^-1 [0..0,-1], T = sum c_k v_k.
+// ---------------------------------------------------------------------------------------
+static bool solve_small(std::vector<double> A, std::vector<double> b, int n, std::vector<double> &x) {
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(A[r * n + c]) > std::fabs(A[p * n + c])) p = r;
+        if (A[p * n + c] == 0.0) return false;
+        if (p != c) {
+            for (int k = 0; k < n; ++k) std::swap(A[c * n + k], A[p * n + k]);
+            std::swap(b[c], b[p]);
+        }
+        for (int r = c + 1; r < n; ++r) {
+            double f = A[r * n + c] / A[c * n + c];
+            for (int k = c; k < n; ++k) A[r * n + k] -= f * A[c * n + k];
+            b[r] -= f * b[c];
+        }
+    }
+    x.assign(n, 0.0);
+    for (int r = n - 1; r >= 0; --r) {
+        double t = b[r];
+        for (int k = r + 1; k < n; ++k) t -= A[r * n + k] * x[k];
+        x[r] = t / A[r * n + r];
+    }
+    return true;
+}
+
+static void diis_reset(CCState *s) {
+    s->dcount = 0;
+    s->dhead = 0;
+    s->dorder.clear();
+    s->gram.clear();
+}
+
+// x = vector fed into the sweep, xn = sweep output (both length len, device); on return x holds
+// the extrapolated vector.
+static void diis_step(CCState *s, double *x, const double *xn, size_t len) {
+    Ctx *ctx = s->ctx;
+    const int cap = std::max(1, s->opts.diis_size - 1);
+    if ((int)s->dv.size() < cap) {
+        s->dv.resize(cap);
+        s->de.resize(cap);
+    }
+    int slot;
+    if (s->dcount < cap) {
+        slot = s->dcount++;
+    } else {
+        slot = s->dorder.front();
+        s->dorder.erase(s->dorder.begin());
+        s->gram.erase(s->gram.begin());
+        for (auto &row : s->gram) row.erase(row.begin());
+    }
+    if (s->dv[slot].n < len) {
+        s->dv[slot] = DBuf<double>(ctx, len);
+        s->de[slot] = DBuf<double>(ctx, len);
+    }
+    d2d(ctx, s->dv[slot].p, xn, len);
+    axpby(ctx, len, 1.0, xn, -1.0, x, s->de[slot].p);
+    s->dorder.push_back(slot);
+    const int m = (int)s->dorder.size();
+    std::vector<double> row(m);
+    for (int k = 0; k < m; ++k) row[k] = dot(ctx, len, s->de[s->dorder[k]].p, s->de[slot].p);
+    for (int k = 0; k < m - 1; ++k) s->gram[k].push_back(row[k]);
+    s->gram.push_back(row);
+    double mx = 0.0;
+    for (int k = 0; k < m; ++k)
+        for (int l = 0; l < m; ++l) mx = std::max(mx, std::fabs(s->gram[k][l]));
+    const int nb = m + 1;
+    std::vector<double> B(nb * nb, -1.0), rhs(nb, 0.0), c;
+    B[m * nb + m] = 0.0;
+    for (int k = 0; k < m; ++k)
+        for (int l = 0; l < m; ++l) B[k * nb + l] = mx > 0 ? s->gram[k][l] / mx : 0.0;
+    rhs[m] = -1.0;
+    if (mx == 0.0 || !solve_small(B, rhs, nb, c)) {
+        d2d(ctx, x, xn, len);   // degenerate subspace: plain update
+        return;
+    }
+    std::vector<const double *> vecs(m);
+    for (int k = 0; k < m; ++k) vecs[k] = s->dv[s->dorder[k]].p;
+    lincomb(ctx, len, m, vecs.data(), c.data(), x);
+}
+
+// ---------------------------------------------------------------------------------------
+// set-up
+// ---------------------------------------------------------------------------------------
+CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *Cocc, int o,
+                   const double *Cvir, int v, const double *eps_dev, const jues_cc_opts &opts) {
+    JUES_REQUIRE(method == 0 || method == 1, "method must be 0 (CCD) or 1 (CCSD)");
+    JUES_REQUIRE(n > 0 && o > 0 && v > 0 && o + v <= n, "need 0 < nocc, 0 < nvir, nocc + nvir <= nbf");
+    JUES_REQUIRE(opts.maxit >= 0, "maxit must be >= 0");
+    JUES_REQUIRE(opts.diis_size >= 2 && opts.diis_size <= 16 || !opts.diis, "diis_size must be in 2..16");
+    JUES_REQUIRE(opts.precision == JUES_PREC_FP64 || opts.precision == JUES_PREC_SPLIT_BF16,
+                 "unknown precision");
+    JUES_REQUIRE(opts.guess >= 0 && opts.guess <= 2, "unknown guess");
+    std::unique_ptr<CCState> s(new CCState());
+    s->ctx = ctx;
+    s->method = method;
+    s->n = n; s->o = o; s->v = v;
+    s->opts = opts;
+    s->precision = opts.precision;
+    const long long oo = (long long)o * o, vv = (long long)v * v, ov = (long long)o * v;
+    const size_t t2n = (size_t)(oo * vv);
+    s->eps = DBuf<double>(ctx, n);
+    d2d(ctx, s->eps.p, eps_dev, n);
+    // integral blocks (mRCCD.jl:120-127, mRCCSD.jl:102-110), physicists' notation
+    const int iprec = opts.precision;   // transform in the same precision form
+    s->oovv = DBuf<double>(ctx, t2n);
+    s->ovov = DBuf<double>(ctx, t2n);
+    s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));
+    s->vvvv = DBuf<double>(ctx, (size_t)(vv * vv));
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOVV", true, 0, s->oovv.p, true);
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVOV", true, 0, s->ovov.p, true);
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOOO", true, 0, s->oooo.p, true);
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "VVVV", true, 0, s->vvvv.p, true);
+    if (method == 0) {
+        s->ovvo = DBuf<double>(ctx, t2n);
+        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVVO", true, 0, s->ovvo.p, true);
+    } else {
+        s->ooov = DBuf<double>(ctx, (size_t)(oo * ov));
+        s->ovvv = DBuf<double>(ctx, (size_t)(ov * vv));
+        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ooov", true, 0, s->ooov.p, true);
+        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ovvv", true, 0, s->ovvv.p, true);
+    }
+    pack_cache_drop(ctx, g);
+    // ring seeds in (me),(bj) layout: ovvoJ[(me),(bj)] = ovvo[m,b,e,j] (CCD) or, for CCSD,
+    // the same value read from oovv[m,j,e,b] (= <mj|eb> = (me|jb), as mRCCSD.jl:187 does);
+    // ovovK[(me),(bj)] = -ovov[m,b,j,e]
+    s->ovvoJ = DBuf<double>(ctx, (size_t)(ov * ov));
+    s->ovovK = DBuf<double>(ctx, (size_t)(ov * ov));
+    {
+        if (method == 0) {
+            // box (m, e, b, j); ovvo[m,b,e,j] offset m + o b + ov e + ovv j
+            Perm4 p{{o, v, v, o}, {1, ov, o, ov * v}, {1, o, ov, ov * v}};
+            permute4(ctx, p, 1.0, s->ovvo.p, 0.0, s->ovvoJ.p);
+        } else {
+            // box (m, e, b, j); oovv[m,j,e,b] offset m + o j + oo e + oov b
+            Perm4 p{{o, v, v, o}, {1, oo, oo * v, o}, {1, o, ov, ov * v}};
+            permute4(ctx, p, 1.0, s->oovv.p, 0.0, s->ovvoJ.p);
+        }
+        // ovov[m,b,j,e] offset m + o b + ov j + ovo e
+        Perm4 q{{o, v, v, o}, {1, ov * o, o, ov}, {1, o, ov, ov * v}};
+        permute4(ctx, q, -1.0, s->ovov.p, 0.0, s->ovovK.p);
+    }
+    s->T = DBuf<double>(ctx, t2n);
+    s->Tn = DBuf<double>(ctx, t2n);
+    s->Tt = DBuf<double>(ctx, t2n);
+    s->Z = DBuf<double>(ctx, t2n);
+    s->L = DBuf<double>(ctx, t2n);
+    s->Wp = DBuf<double>(ctx, (size_t)(oo * oo));
+    s->WJ = DBuf<double>(ctx, (size_t)(ov * ov));
+    s->WK = DBuf<double>(ctx, (size_t)(ov * ov));
+    s->W12 = DBuf<double>(ctx, (size_t)(ov * ov));
+    s->Fae = DBuf<double>(ctx, (size_t)vv);
+    s->Fmi = DBuf<double>(ctx, (size_t)oo);
+    if (method == 1) {
+        s->t1 = DBuf<double>(ctx, (size_t)ov);
+        s->t1n = DBuf<double>(ctx, (size_t)ov);
+        s->Fme = DBuf<double>(ctx, (size_t)ov);
+        s->Wabef = DBuf<double>(ctx, (size_t)(vv * vv));
+        fill(ctx, s->t1.p, (size_t)ov, 0.0);
+    }
+    // initial amplitudes
+    if (method == 1 || opts.guess == JUES_GUESS_MP2) {
+        divide_by_d(ctx, s->oovv.p, s->eps.p, o, v, s->T.p);   // mRCCSD.jl:66
+    } else if (opts.guess == JUES_GUESS_ZERO) {
+        fill(ctx, s->T.p, t2n, 0.0);                          // mRCCD.jl:245
+    } else {
+        // RCCD.jl:145-160: T[i,j,a,b] = ovov[i,a,j,b] / D
+        Perm4 p{{o, o, v, v}, {1, ov, o, ov * o}, {1, o, oo, oo * v}};
+        permute4(ctx, p, 1.0, s->ovov.p, 0.0, s->Tn.p);
+        divide_by_d(ctx, s->Tn.p, s->eps.p, o, v, s->T.p);
+    }
+    s->energy = cc_energy(ctx, s->oovv.p, s->T.p, method == 1 ? s->t1.p : nullptr, o, v);
+    s->e_prev = s->energy;
+    diis_reset(s.get());
+    ctx->check_flags();
+    return s.release();
+}
+
+// amplitude vector for DIIS: CCD = T2; CCSD = [t1; T2] packed in aux1
+static void cc_one(CCState *s, int prec) {
+    Ctx *ctx = s->ctx;
+    const size_t t2n = (size_t)s->o * s->o * s->v * s->v;
+    const size_t t1n = (size_t)s->o * s->v;
+    cudaEvent_t e0, e1;
+    JUES_CHECK_CUDA(cudaEventCreate(&e0));
+    JUES_CHECK_CUDA(cudaEventCreate(&e1));
+    JUES_CHECK_CUDA(cudaEventRecord(e0, ctx->stream));
+    double r2;
+    if (s->method == 0) {
+        r2 = ccd_sweep(s, prec);
+    } else {
+        r2 = ccsd_sweep(s, prec);
+    }
+    double rn = std::sqrt(r2);
+    if (s->opts.diis) {
+        if (s->method == 0) {
+            diis_step(s, s->T.p, s->Tn.p, t2n);
+        } else {
+            // pack [t1; T2] contiguously for the DIIS vectors
+            if (s->aux1.n < t1n + t2n) s->aux1 = DBuf<double>(ctx, t1n + t2n);
+            if (s->aux2.n < t1n + t2n) s->aux2 = DBuf<double>(ctx, t1n + t2n);
+            d2d(ctx, s->aux1.p, s->t1.p, t1n);
+            d2d(ctx, s->aux1.p + t1n, s->T.p, t2n);
+            d2d(ctx, s->aux2.p, s->t1n.p, t1n);
+            d2d(ctx, s->aux2.p + t1n, s->Tn.p, t2n);
+            diis_step(s, s->aux1.p, s->aux2.p, t1n + t2n);
+            d2d(ctx, s->t1.p, s->aux1.p, t1n);
+            d2d(ctx, s->T.p, s->aux1.p + t1n, t2n);
+        }
+    } else {
+        std::swap(s->T, s->Tn);
+        if (s->method == 1) std::swap(s->t1, s->t1n);
+    }
+    s->e_prev = s->energy;
+    s->energy = cc_energy(ctx, s->oovv.p, s->T.p, s->method == 1 ? s->t1.p : nullptr, s->o, s->v);
+    JUES_CHECK_CUDA(cudaEventRecord(e1, ctx->stream));
+    JUES_CHECK_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->check_flags();
+    if (!std::isfinite(s->energy) || !std::isfinite(rn))
+        throw Error(JUES_ENONFINITE, "CC iterations produced a non-finite energy or step (diverged)");
+    s->iters += 1;
+    jues_iter_log rec;
+    rec.iter = s->iters;
+    rec.precision = prec;
+    rec.energy = s->energy;
+    rec.rnorm = rn;
+    rec.ms = ms;
+    s->log.push_back(rec);
+}
+
+static bool cc_converged(const CCState *s) {
+    if (s->log.empty()) return false;
+    const jues_iter_log &r = s->log.back();
+    bool any = false, ok = true;
+    if (s->opts.r_conv > 0) { any = true; ok = ok && r.rnorm < s->opts.r_conv; }
+    if (s->opts.e_conv > 0) { any = true; ok = ok && std::fabs(s->energy - s->e_prev) < s->opts.e_conv; }
+    return any && ok;
+}
+
+// Split precision stops improving once the step reaches the BF16-split noise floor; detect
+// that (no decrease over two sweeps after it fell below 1e-5) and hand over to FP64 sweeps.
+static bool at_noise_floor(const CCState *s) {
+    const auto &L = s->log;
+    if (L.size() < 3) return false;
+    const double a = L[L.size() - 3].rnorm, b = L[L.size() - 2].rnorm, c = L.back().rnorm;
+    return c < 1e-5 && c > 0.5 * b && b > 0.5 * a;
+}
+
+void cc_iterate(CCState *s, int nsweeps, int *done, int *converged) {
+    int k = 0;
+    bool conv = false;
+    const bool split = s->precision == JUES_PREC_SPLIT_BF16;
+    while (k < nsweeps) {
+        const int prec = (split && s->refine_left >= 0) ? JUES_PREC_FP64 : s->precision;
+        cc_one(s, prec);
+        ++k;
+        conv = cc_converged(s);
+        if (split && s->opts.refine > 0) {
+            if (s->refine_left < 0) {
+                if (conv || at_noise_floor(s)) {
+                    // hand over to the closing FP64 sweeps; restart DIIS with exact residuals
+                    s->refine_left = s->opts.refine;
+                    diis_reset(s);
+                    conv = false;
+                }
+                continue;
+            }
+            if (--s->refine_left == 0) break;
+        }
+        if (conv) break;
+    }
+    s->converged = conv;
+    if (done) *done = k;
+    if (converged) *converged = conv ? 1 : 0;
+}
+
+void cc_amplitudes(CCState *s, double *t1_host, double *t2_host) {
+    Ctx *ctx = s->ctx;
+    const size_t t2n = (size_t)s->o * s->o * s->v * s->v;
+    if (t2_host)
+        JUES_CHECK_CUDA(cudaMemcpyAsync(t2_host, s->T.p, t2n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (t1_host) {
+        if (s->method == 1)
+            JUES_CHECK_CUDA(cudaMemcpyAsync(t1_host, s->t1.p, (size_t)s->o * s->v * sizeof(double),
+                                            cudaMemcpyDeviceToHost, ctx->stream));
+        else
+            std::memset(t1_host, 0, (size_t)s->o * s->v * sizeof(double));
+    }
+    ctx->sync();
+}
+
+double CCState::sweep_flops(int prec) const {
+    (void)prec;
+    return ccd_sweep_flops(o, v);
+}
+
+}  // namespace jues
+
+namespace jues {
+
+// ---------------------------------------------------------------------------------------
+// CCSD sweep (RCCSD.jl:150-289 on the six blocks of mRCCSD.jl:102-110).
+// Work buffers: Tt = t~(T2 + tau/2) for Fae/Fmi, then t~(T2); aux1 = T2 + tau; tau; Wabef.
+// ---------------------------------------------------------------------------------------
+double ccsd_sweep(CCState *s, int prec) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v, ooo = oo * o,
+                    vv = v * v, ovv = ov * v;
+    const size_t t2n = (size_t)(oo * vv);
+    const double *T = s->T.p, *t1 = s->t1.p, *W = s->oovv.p, *ooov = s->ooov.p, *ovvv = s->ovvv.p,
+                 *ovov = s->ovov.p;
+    if (s->tau.n < t2n) s->tau = DBuf<double>(ctx, t2n);
+    if (s->aux1.n < t2n) s->aux1 = DBuf<double>(ctx, t2n);
+    double *tau = s->tau.p, *Ttau = s->aux1.p;
+    // tau[m,n,a,f] = t1[m,a] t1[n,f]: outer product as a K=1 GEMM over (m,a) x (n,f)
+    G(s, JUES_PREC_FP64, "ccsd_tau", ov, ov, 1, 1.0, t1, plain(1), plain(0), t1, plain(0), plain(1), 0.0,
+      tau, mode2(o, 1, oo), mode2(o, o, oov));
+    axpby(ctx, t2n, 1.0, T, 0.5, tau, Ttau);                 // T2 + tau/2
+    t_tilde(ctx, Ttau, (int)o, (int)v, s->Tt.p);             // 2Ts - Ts[n,m,..]
+    axpby(ctx, t2n, 1.0, T, 1.0, tau, Ttau);                 // T2 + tau (ladders)
+
+    // Fae (RCCSD.jl:187-194)
+    G(s, prec, "ccsd_fae", v, v, oov, -1.0, s->Tt.p, plain(oo), mode2(oo, 1, oov), W, mode2(oo, 1, oov),
+      plain(oo), 0.0, s->Fae.p, plain(1), plain(v));
+    G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, 2.0, ovvv, mode2(v, o, ovv), mode2(o, 1, ov), t1,
+      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0));
+    G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, -1.0, ovvv, mode2(v, o, ov), mode2(o, 1, ovv), t1,
+      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0));
+    // Fmi (RCCSD.jl:195-203)
+    G(s, prec, "ccsd_fmi", o, o, o * vv, 1.0, W, plain(1), plain(o), s->Tt.p, plain(o), plain(1), 0.0,
+      s->Fmi.p, plain(1), plain(o));
+    G(s, JUES_PREC_FP64, "ccsd_fmi_t1", oo, 1, ov, 2.0, ooov, mode2(o, 1, oo), mode2(o, o, ooo), t1,
+      plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0));
+    G(s, JUES_PREC_FP64, "ccsd_fmi_t1", oo, 1, ov, -1.0, ooov, mode2(o, o, oo), mode2(o, 1, ooo), t1,
+      plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0));
+    // Fme (RCCSD.jl:204-210)
+    G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
+      plain(0), 0.0, s->Fme.p, plain(1), plain(0));
+    G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, -1.0, W, mode2(o, o, oo), mode2(o, 1, oov), t1, plain(1),
+      plain(0), 1.0, s->Fme.p, plain(1), plain(0));
+
+    // W' = oooo + t1[j,e] ooov[m,n,i,e] + t1[i,e] ooov[n,m,j,e] + sum_ef oovv[mn,ef] (T2+tau)[ij,ef]
+    G(s, JUES_PREC_FP64, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
+      plain(1), 1.0, s->Wp.p, plain(1), plain(ooo), s->oooo.p);
+    G(s, JUES_PREC_FP64, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
+      plain(1), 1.0, s->Wp.p, mode3(o, o, o, 1, ooo), plain(oo));
+    G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
+      plain(1), plain(oo));
+    // Wabef without its T2 part: vvvv - t1[m,b] <am|ef> - t1[m,a] <mb|ef>  (<am|ef> = ovvv[m,a,f,e])
+    G(s, prec, "ccsd_wabef_t1", v * vv, v, o, -1.0, ovvv, mode3(v, v, o, ovv, ov), plain(1), t1, plain(1),
+      plain(o), 1.0, s->Wabef.p, mode3(v, v, 1, vv, v * vv), plain(v), s->vvvv.p);
+    G(s, prec, "ccsd_wabef_t1", v * vv, v, o, -1.0, ovvv, mode3(v, v, o, ov, ovv), plain(1), t1, plain(1),
+      plain(o), 1.0, s->Wabef.p, mode3(v, v, v, vv, v * vv), plain(1));
+    // L = oovv + W'^T (T2+tau) + (T2+tau) Wabef^T
+    G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
+      1.0, s->L.p, plain(1), plain(oo), W);
+    G(s, prec, "ccsd_pp_ladder", oo, vv, vv, 1.0, Ttau, plain(1), plain(oo), s->Wabef.p, plain(vv),
+      plain(1), 1.0, s->L.p, plain(1), plain(oo));
+
+    // ring intermediates; T~ of T2 alone from here on
+    t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
+    const double *Tt = s->Tt.p;
+    // WJ = WmBeJ (RCCSD.jl:229-238 with <mb|ej> = oovv[m,j,e,b], <mn|ej> = ooov[n,m,j,e])
+    G(s, prec, "ccsd_wj", ov, ov, ov, 0.5, W, mode2(o, 1, oo), mode2(o, o, oov), Tt, mode2(o, 1, oo),
+      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p);
+    G(s, prec, "ccsd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
+      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
+    G(s, prec, "ccsd_wj", ov, ov, ov, -1.0, W, mode2(o, 1, oo), mode2(o, o, oov), tau, mode2(o, o, oo),
+      mode2(v, oov, 1), 1.0, s->WJ.p, plain(1), plain(ov));
+    G(s, JUES_PREC_FP64, "ccsd_wj_t1", ovv, o, v, 1.0, ovvv, mode3(o, v, 1, ov, o), plain(ovv), t1,
+      plain(o), plain(1), 1.0, s->WJ.p, mode3(o, v, 1, o, ov), plain(ovv));
+    G(s, JUES_PREC_FP64, "ccsd_wj_t1", ov * o, v, o, -1.0, ooov, mode3(o, v, o, ooo, oo), plain(1), t1,
+      plain(1), plain(o), 1.0, s->WJ.p, mode3(o, v, 1, o, ovv), plain(ov));
+    // WK = WmBEj (RCCSD.jl:239-247 with <bm|ej> = ovov[m,b,j,e], <nm|ej> = ooov[m,n,j,e])
+    G(s, prec, "ccsd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
+      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p);
+    G(s, prec, "ccsd_wk", ov, ov, ov, 1.0, W, mode2(o, o, oo), mode2(o, 1, oov), tau, mode2(o, o, oo),
+      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov));
+    G(s, JUES_PREC_FP64, "ccsd_wk_t1", ovv, o, v, -1.0, ovvv, mode3(o, v, 1, ovv, o), plain(ov), t1,
+      plain(o), plain(1), 1.0, s->WK.p, mode3(o, v, 1, o, ov), plain(ovv));
+    G(s, JUES_PREC_FP64, "ccsd_wk_t1", ov * o, v, o, 1.0, ooov, mode3(o, v, 1, ooo, oo), plain(o), t1,
+      plain(1), plain(o), 1.0, s->WK.p, mode3(o, v, 1, o, ovv), plain(ov));
+    axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
+
+    // T1 (RCCSD.jl:248-259) into t1n, before the amplitudes change
+    double *R1 = s->t1n.p;
+    G(s, JUES_PREC_FP64, "ccsd_t1", o, v, v, 1.0, t1, plain(1), plain(o), s->Fae.p, plain(v), plain(1),
+      0.0, R1, plain(1), plain(o));
+    G(s, JUES_PREC_FP64, "ccsd_t1", o, v, o, -1.0, s->Fmi.p, plain(o), plain(1), t1, plain(1), plain(o),
+      1.0, R1, plain(1), plain(o));
+    G(s, JUES_PREC_FP64, "ccsd_t1", ov, 1, ov, 1.0, Tt, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
+      plain(1), plain(0), 1.0, R1, plain(1), plain(0));
+    G(s, JUES_PREC_FP64, "ccsd_t1", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
+      plain(0), 1.0, R1, plain(1), plain(0));
+    G(s, JUES_PREC_FP64, "ccsd_t1", ov, 1, ov, -1.0, ovov, mode2(o, ov, o), mode2(o, 1, oov), t1,
+      plain(1), plain(0), 1.0, R1, plain(1), plain(0));
+    G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, ooov, plain(oo), mode2(oo, 1, ooo), Tt,
+      mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o));
+    G(s, prec, "ccsd_t1_ovvv", o, v, ovv, 1.0, Tt, plain(1), mode3(o, v, o, oo, oov), ovvv,
+      mode3(o, v, 1, ovv, ov), plain(o), 1.0, R1, plain(1), plain(o));
+
+    // F~ae[b,e] = Fae - 1/2 t1[m,b] Fme[m,e];  F~mi[m,j] = Fmi + 1/2 Fme[m,e] t1[j,e]
+    G(s, JUES_PREC_FP64, "ccsd_ftilde", v, v, o, -0.5, t1, plain(o), plain(1), s->Fme.p, plain(1),
+      plain(o), 1.0, s->Fae.p, plain(1), plain(v));
+    G(s, JUES_PREC_FP64, "ccsd_ftilde", o, o, v, 0.5, s->Fme.p, plain(1), plain(o), t1, plain(o),
+      plain(1), 1.0, s->Fmi.p, plain(1), plain(o));
+
+    // Z (RCCSD.jl:264-284, one member of each (i,a)<->(j,b) pair)
+    double *Z = s->Z.p;
+    G(s, prec, "ccsd_z_fae", oov, v, v, 1.0, T, plain(1), plain(oov), s->Fae.p, plain(v), plain(1), 0.0,
+      Z, plain(1), plain(oov));
+    G(s, prec, "ccsd_z_fmi", o * vv, o, o, -1.0, T, mode2(o, 1, oo), plain(o), s->Fmi.p, plain(1),
+      plain(o), 1.0, Z, mode2(o, 1, oo), plain(o));
+    G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
+      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
+    G(s, prec, "ccsd_ring", ov, ov, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WJ.p, plain(1),
+      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
+    G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
+      plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
+    // - tau[i,m,e,a] <mb|ej>: Y1[i,m,j,b] = sum_e t1[i,e] oovv[m,j,e,b]; Z -= sum_m t1[m,a] Y1[i,m,j,b]
+    if (s->aux2.n < (size_t)(ooo * v)) s->aux2 = DBuf<double>(ctx, (size_t)(ooo * v));
+    double *Y = s->aux2.p;
+    G(s, JUES_PREC_FP64, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo),
+      mode3(o, o, 1, o, oov), 0.0, Y, plain(1), plain(o));
+    G(s, JUES_PREC_FP64, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, o, 1, oo, ooo), plain(o), t1,
+      plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
+    // - tau[i,m,e,b] <am|ej>: Y2[i,m,a,j] = sum_e t1[i,e] ovov[m,a,j,e]; Z -= sum_m Y2 t1[m,b]
+    G(s, JUES_PREC_FP64, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov),
+      plain(1), 0.0, Y, plain(1), plain(o));
+    G(s, JUES_PREC_FP64, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, v, 1, oo, oov), plain(o), t1,
+      plain(1), plain(o), 1.0, Z, mode3(o, v, 1, oo, o), plain(oov));
+    // + t1[i,e] <ab|ej> = t1[i,e] ovvv[j,a,b,e]
+    G(s, prec, "ccsd_z_ovvv", o, ovv, v, 1.0, t1, plain(1), plain(o), ovvv, plain(ovv), plain(1), 1.0, Z,
+      plain(1), plain(o));
+    // - t1[m,a] <mb|ij> = t1[m,a] ooov[m,j,i,b]
+    G(s, JUES_PREC_FP64, "ccsd_z_ooov", oov, v, o, -1.0, ooov, mode3(o, o, oo, o, ooo), plain(1), t1,
+      plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
+
+    double r2 = t2_finalize(ctx, s->L.p, Z, s->eps.p, (int)o, (int)v, T, s->Tn.p);
+    // t1n = R1 / D_ia and its step norm
+    r2 += t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, t1);
+    return r2;
+}
+
+}  // namespace jues

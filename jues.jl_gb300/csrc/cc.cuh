@@ -1,0 +1,48 @@
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+
+namespace jues {
+
+// Device-resident closed-shell CC problem (CCD or CCSD).
+struct CCState {
+    Ctx *ctx = nullptr;
+    int method = 0;   // 0 CCD, 1 CCSD
+    int n = 0, o = 0, v = 0;
+    jues_cc_opts opts{};
+    int precision = JUES_PREC_FP64;
+    // integrals, physicists' notation, column-major as the reference's get_eri blocks
+    DBuf<double> eps, oovv, ovov, ovvo, oooo, vvvv, ooov, ovvv;
+    DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
+    // amplitudes and work arrays
+    DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;
+    DBuf<double> t1, t1n, Fme, tau;         // CCSD
+    DBuf<double> Wabef;                     // CCSD: vvvv + t1 terms
+    DBuf<double> aux1, aux2;                // CCSD scratch
+    // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
+    std::vector<DBuf<double>> dv, de;
+    std::vector<std::vector<double>> gram;   // gram[k][l] = e_k . e_l, k,l in insertion order
+    int dcount = 0;     // pairs stored
+    int dhead = 0;      // next slot
+    std::vector<int> dorder;   // slots in insertion order
+    double energy = 0.0, e_prev = 0.0;
+    int iters = 0;
+    int refine_left = -1;   // split precision: closing FP64 sweeps left (-1 = not started)
+    bool converged = false;
+    std::vector<jues_iter_log> log;
+    double sweep_flops(int prec) const;
+};
+
+CCState *cc_create(Ctx *ctx, int method, const double *gao_dev, int n, const double *Cocc_dev, int o,
+                   const double *Cvir_dev, int v, const double *eps_dev, const jues_cc_opts &opts);
+void cc_iterate(CCState *s, int nsweeps, int *done, int *converged);
+void cc_amplitudes(CCState *s, double *t1_host, double *t2_host);
+// one CCD / CCSD sweep: Tn from T (and t1n from t1), returns the squared step norm
+double ccd_sweep(CCState *s, int prec);
+double ccsd_sweep(CCState *s, int prec);
+// flop counts
+double ccd_sweep_flops(int o, int v);
+double ccd_reference_flops(int o, int v);   // mRCCD.jl GEMM set (Wabef formed)
+
+}  // namespace jues

@@ -1,0 +1,197 @@
+// Shared definitions of libjuesgpu: context, errors, device buffers, tensor modes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/jues_gpu.h"
+
+namespace jues {
+
+// ---------------------------------------------------------------------------------------
+// errors: internal code throws jues::Error; the C ABI layer converts to a status code and
+// stores the message for jues_last_error().
+// ---------------------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define JUES_CHECK_CUDA(expr)                                                             \
+    do {                                                                                  \
+        cudaError_t _e = (expr);                                                          \
+        if (_e != cudaSuccess)                                                            \
+            throw ::jues::Error(JUES_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e) + \
+                                " (" __FILE__ ":" + std::to_string(__LINE__) + ")");       \
+    } while (0)
+
+#define JUES_REQUIRE(cond, msg)                                                           \
+    do {                                                                                  \
+        if (!(cond)) throw ::jues::Error(JUES_EINVAL, (msg));                              \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------
+// A tensor "mode": one GEMM dimension that is really up to three tensor indices.
+// Index r maps to the element offset
+//     (r % d0) * s0 + ((r / d0) % d1) * s1 + (r / (d0 * d1)) * s2.
+// A plain dimension with stride s is {BIG, 1, s, 0, 0}.
+// ---------------------------------------------------------------------------------------
+struct Mode {
+    long long d0, d1;
+    long long s0, s1, s2;
+};
+constexpr long long MODE_BIG = (1LL << 60);
+inline Mode plain(long long stride) { return Mode{MODE_BIG, 1, stride, 0, 0}; }
+inline Mode mode2(long long d0, long long s0, long long s1) { return Mode{d0, MODE_BIG, s0, s1, 0}; }
+inline Mode mode3(long long d0, long long d1, long long s0, long long s1, long long s2) {
+    return Mode{d0, d1, s0, s1, s2};
+}
+__host__ __device__ inline long long mode_off(const Mode &m, long long r) {
+    long long q = r / m.d0;
+    return (r - q * m.d0) * m.s0 + (q % m.d1) * m.s1 + (q / m.d1) * m.s2;
+}
+
+// ---------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------
+struct ProfRec {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    double total_ms = 0.0;
+    long long launches = 0;
+};
+
+struct PackCache;  // split-precision operand cache (gett_tc.cu)
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t mem_limit = 0;   // 0 = unlimited
+    size_t mem_used = 0;
+    bool profiling = false;
+    long long launches = 0;
+    std::map<std::string, ProfRec> prof;
+    unsigned int *d_flags = nullptr;   // device error flags (timeouts, non-finite)
+    double *d_red = nullptr;           // reduction scratch (1 << 16 doubles)
+    PackCache *pack = nullptr;         // owned; destroyed by pack_cache_destroy
+    Ctx();
+    ~Ctx();
+
+    void *alloc(size_t bytes);
+    void free(void *p, size_t bytes);
+    void sync() { JUES_CHECK_CUDA(cudaStreamSynchronize(stream)); }
+    // bracket a launch with profiling events when profiling is on
+    struct Scope {
+        Ctx *c;
+        ProfRec *r = nullptr;
+        std::pair<cudaEvent_t, cudaEvent_t> ev{};
+        Scope(Ctx *c, const char *name);
+        ~Scope();
+    };
+    void flush_profile();
+    void count_launch() { ++launches; }
+    void check_flags();   // reads d_flags after a sync; throws on a set flag
+};
+
+// device buffer owned by a context
+template <class T>
+struct DBuf {
+    Ctx *ctx = nullptr;
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(Ctx *c, size_t count) : ctx(c), p(nullptr), n(count) {
+        if (count) p = static_cast<T *>(c->alloc(count * sizeof(T)));
+    }
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    DBuf(DBuf &&o) noexcept : ctx(o.ctx), p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf &operator=(DBuf &&o) noexcept {
+        reset();
+        ctx = o.ctx; p = o.p; n = o.n;
+        o.p = nullptr; o.n = 0;
+        return *this;
+    }
+    ~DBuf() { reset(); }
+    void reset() {
+        if (p && ctx) ctx->free(p, n * sizeof(T));
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// flag bits in Ctx::d_flags[0]
+constexpr unsigned FLAG_TIMEOUT = 1u;
+constexpr unsigned FLAG_NONFINITE = 2u;
+
+// ---------------------------------------------------------------------------------------
+// GEMM over tensor modes ("GETT"):
+//   C[mC(m) + nC(n)] = alpha * sum_k A[mA(m) + kA(k)] * B[kB(k) + nB(n)] + beta * C[...]
+// for m < M, n < N, k < K; beta == 0 never reads C.
+// ---------------------------------------------------------------------------------------
+struct GettArgs {
+    long long M, N, K;
+    double alpha, beta;
+    const double *A; Mode mA, kA;
+    const double *B; Mode kB, nB;
+    double *C; Mode mC, nC;
+    const double *Cin = nullptr;   // beta term reads Cin (same modes as C) when set, else C
+    // split precision: operands whose values do not change between calls may be cached
+    bool a_const = false, b_const = false;
+};
+
+void gett_f64(Ctx *ctx, const GettArgs &g, const char *name);
+void gett_tc(Ctx *ctx, const GettArgs &g, const char *name);   // split BF16 on tcgen05
+void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
+void pack_cache_clear(Ctx *ctx);
+void pack_cache_destroy(PackCache *p);
+void pack_cache_drop(Ctx *ctx, const void *ptr);
+
+// ---------------------------------------------------------------------------------------
+// bandwidth kernels (kernels.cu)
+// ---------------------------------------------------------------------------------------
+// out[mode_out(x)] = alpha * in[mode_in(x)] + beta * out[...], x over a d0*d1*d2*d3 box
+// described by per-dimension strides.
+struct Perm4 {
+    long long d[4];
+    long long si[4];
+    long long so[4];
+};
+void permute4(Ctx *ctx, const Perm4 &p, double alpha, const double *in, double beta, double *out);
+void fill(Ctx *ctx, double *p, size_t n, double v);
+void axpby(Ctx *ctx, size_t n, double a, const double *x, double b, const double *y, double *out);
+// sum_i x_i*y_i in FP64 (deterministic two-pass block reduction)
+double dot(Ctx *ctx, size_t n, const double *x, const double *y);
+// MP2: sum K[i,j,a,b](2K[i,j,a,b]-K[i,j,b,a]) / D (K column-major [i,j,a,b])
+double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v);
+// CC energy: sum oovv[i,j,a,b] (2 X[i,j,a,b] - X[j,i,a,b]) with X = T2 (+ t1 t1 when t1)
+double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t1, int o, int v);
+// T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a]) / D ; returns ||Tn - Told||^2
+// if Told != nullptr.  Writes Tn.
+double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *eps, int o, int v,
+                   const double *Told, double *Tn);
+// t1n[i,a] /= (e_i - e_a) in place; returns ||t1n - t1old||^2
+double t1_finalize(Ctx *ctx, double *t1n, const double *eps, int o, int v, const double *t1old);
+// X[i,j,a,b] = (L[...]) / D in place variants used for guesses
+void divide_by_d(Ctx *ctx, const double *in, const double *eps, int o, int v, double *out);
+// T~ = 2 T[i,j,a,b] - T[j,i,a,b]
+void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out);
+// sum_k c_k * vecs[k] -> out (length n)
+void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out);
+// 1 if any element of x is NaN/Inf
+bool any_nonfinite(Ctx *ctx, const double *x, size_t n);
+
+}  // namespace jues
+
+struct jues_ctx {
+    jues::Ctx impl;
+};

@@ -1,0 +1,98 @@
+// Context: stream, memory accounting, per-kernel event timing, error flags.
+#include <cstring>
+
+#include "common.cuh"
+
+namespace jues {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+const std::string &last_error() { return g_last_error; }
+
+Ctx::Ctx() {}
+
+Ctx::~Ctx() {
+    if (stream) cudaStreamSynchronize(stream);
+    pack_cache_destroy(pack);
+    pack = nullptr;
+    for (auto &kv : prof) {
+        for (auto &e : kv.second.pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        for (auto &e : kv.second.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+    }
+    if (d_flags) cudaFree(d_flags);
+    if (d_red) cudaFree(d_red);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void *Ctx::alloc(size_t bytes) {
+    if (bytes == 0) return nullptr;
+    if (mem_limit && mem_used + bytes > mem_limit)
+        throw Error(JUES_ENOMEM, "device allocation of " + std::to_string(bytes) +
+                                     " bytes exceeds the context memory limit (" +
+                                     std::to_string(mem_limit) + " bytes, " +
+                                     std::to_string(mem_used) + " in use)");
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(JUES_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                     cudaGetErrorString(e));
+    }
+    mem_used += bytes;
+    return p;
+}
+
+void Ctx::free(void *p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    mem_used -= bytes;
+}
+
+Ctx::Scope::Scope(Ctx *c_, const char *name) : c(c_) {
+    c->count_launch();
+    if (!c->profiling) return;
+    r = &c->prof[name];
+    if (!r->pool.empty()) {
+        ev = r->pool.back();
+        r->pool.pop_back();
+    } else {
+        JUES_CHECK_CUDA(cudaEventCreate(&ev.first));
+        JUES_CHECK_CUDA(cudaEventCreate(&ev.second));
+    }
+    JUES_CHECK_CUDA(cudaEventRecord(ev.first, c->stream));
+}
+
+Ctx::Scope::~Scope() {
+    if (!r) return;
+    cudaEventRecord(ev.second, c->stream);
+    r->pending.push_back(ev);
+    r->launches += 1;
+}
+
+void Ctx::flush_profile() {
+    for (auto &kv : prof) {
+        ProfRec &r = kv.second;
+        for (auto &e : r.pending) {
+            cudaEventSynchronize(e.second);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e.first, e.second);
+            r.total_ms += ms;
+            r.pool.push_back(e);
+        }
+        r.pending.clear();
+    }
+}
+
+void Ctx::check_flags() {
+    unsigned h = 0;
+    JUES_CHECK_CUDA(cudaMemcpyAsync(&h, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    JUES_CHECK_CUDA(cudaStreamSynchronize(stream));
+    if (h) {
+        JUES_CHECK_CUDA(cudaMemsetAsync(d_flags, 0, 4 * sizeof(unsigned), stream));
+        if (h & FLAG_TIMEOUT)
+            throw Error(JUES_ETIMEOUT, "a bounded device-side wait expired; the kernel returned early");
+        if (h & FLAG_NONFINITE) throw Error(JUES_ENONFINITE, "non-finite value detected on the device");
+    }
+}
+
+}  // namespace jues

@@ -1,0 +1,358 @@
+// Bandwidth-bound kernels: permutations, energies, amplitude finalisation, DIIS vectors.
+//
+// Every reduction is deterministic: a fixed-size grid writes one FP64 partial per block,
+// and a single block sums the partials in a fixed order.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace jues {
+
+namespace {
+
+constexpr int RED_BLOCKS = 1184;   // 8 blocks per SM on 148-152 SM parts; fixed for determinism
+constexpr int RED_THREADS = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-wide sum; result valid in thread 0
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double s[32];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) s[w] = v;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? s[threadIdx.x] : 0.0;
+    if (w == 0) v = warp_sum(v);
+    return v;
+}
+
+__global__ void reduce_partials(const double *part, int n, double *out) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[i];
+    v = block_sum(v);
+    if (threadIdx.x == 0) *out = v;
+}
+
+__global__ void permute4_kernel(Perm4 p, double alpha, const double *__restrict__ in, double beta,
+                                double *__restrict__ out, long long total) {
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long r = x;
+        long long i0 = r % p.d[0]; r /= p.d[0];
+        long long i1 = r % p.d[1]; r /= p.d[1];
+        long long i2 = r % p.d[2]; long long i3 = r / p.d[2];
+        long long oi = i0 * p.si[0] + i1 * p.si[1] + i2 * p.si[2] + i3 * p.si[3];
+        long long oo = i0 * p.so[0] + i1 * p.so[1] + i2 * p.so[2] + i3 * p.so[3];
+        double v = alpha * in[oi];
+        if (beta != 0.0) v += beta * out[oo];
+        out[oo] = v;
+    }
+}
+
+__global__ void fill_kernel(double *p, size_t n, double v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void axpby_kernel(size_t n, double a, const double *__restrict__ x, double b,
+                             const double *__restrict__ y, double *__restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = a * x[i] + (y ? b * y[i] : 0.0);
+}
+
+__global__ void dot_kernel(size_t n, const double *__restrict__ x, const double *__restrict__ y,
+                           double *part) {
+    double v = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        v = fma(x[i], y[i], v);
+    v = block_sum(v);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+}
+
+__global__ void nonfinite_kernel(size_t n, const double *__restrict__ x, unsigned *flag) {
+    bool bad = false;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        bad |= !isfinite(x[i]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1u);
+}
+
+// pair index p (a <= b) -> (a, b)
+__device__ __forceinline__ void pair_ab(long long p, int &a, int &b) {
+    long long bb = (long long)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+    while (bb * (bb + 1) / 2 > p) --bb;
+    while ((bb + 1) * (bb + 2) / 2 <= p) ++bb;
+    b = (int)bb;
+    a = (int)(p - bb * (bb + 1) / 2);
+}
+
+// MP2: each (a<=b) pair block reads K[:,:,a,b] and K[:,:,b,a] once.
+__global__ void mp2_kernel(const double *__restrict__ K, const double *__restrict__ eps, int o, int v,
+                           double *part) {
+    const long long oo = (long long)o * o;
+    const long long npair = (long long)v * (v + 1) / 2;
+    double acc = 0.0;
+    for (long long p = blockIdx.x; p < npair; p += gridDim.x) {
+        int a, b;
+        pair_ab(p, a, b);
+        const double ea = eps[o + a], eb = eps[o + b];
+        const double *Kab = K + oo * (a + (long long)v * b);
+        const double *Kba = K + oo * (b + (long long)v * a);
+        for (long long ij = threadIdx.x; ij < oo; ij += blockDim.x) {
+            int i = (int)(ij % o), j = (int)(ij / o);
+            double inv = 1.0 / (eps[i] + eps[j] - ea - eb);
+            double x = Kab[ij];
+            if (a == b) {
+                acc = fma(x * x, inv, acc);
+            } else {
+                double y = Kba[ij];
+                acc = fma(x * (2.0 * x - y) + y * (2.0 * y - x), inv, acc);
+            }
+        }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// CC energy: sum oovv[i,j,a,b] (2X[i,j,a,b] - X[j,i,a,b]), X = T2 + t1(x)t1
+__global__ void ccenergy_kernel(const double *__restrict__ W, const double *__restrict__ T,
+                                const double *__restrict__ t1, int o, int v, double *part) {
+    const long long oo = (long long)o * o, vv = (long long)v * v;
+    double acc = 0.0;
+    for (long long ab = blockIdx.x; ab < vv; ab += gridDim.x) {
+        const int a = (int)(ab % v), b = (int)(ab / v);
+        const double *Wb = W + oo * ab;
+        const double *Tb = T + oo * ab;
+        for (long long ij = threadIdx.x; ij < oo; ij += blockDim.x) {
+            int i = (int)(ij % o), j = (int)(ij / o);
+            double x = Tb[ij], y = Tb[j + (long long)o * i];
+            if (t1) {
+                x += t1[i + (long long)o * a] * t1[j + (long long)o * b];
+                y += t1[j + (long long)o * a] * t1[i + (long long)o * b];
+            }
+            acc = fma(Wb[ij], 2.0 * x - y, acc);
+        }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// Tn[i,j,a,b] = (L[i,j,a,b] + Z[i,j,a,b] + Z[j,i,b,a]) / D, and the squared step norm.
+__global__ void t2_finalize_kernel(const double *__restrict__ L, const double *__restrict__ Z,
+                                   const double *__restrict__ eps, int o, int v,
+                                   const double *__restrict__ Told, double *__restrict__ Tn,
+                                   double *part) {
+    const long long oo = (long long)o * o;
+    const long long npair = (long long)v * (v + 1) / 2;
+    double acc = 0.0;
+    for (long long p = blockIdx.x; p < npair; p += gridDim.x) {
+        int a, b;
+        pair_ab(p, a, b);
+        const double ea = eps[o + a], eb = eps[o + b];
+        const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
+        for (long long ij = threadIdx.x; ij < oo; ij += blockDim.x) {
+            int i = (int)(ij % o), j = (int)(ij / o);
+            long long ji = j + (long long)o * i;
+            double inv = 1.0 / (eps[i] + eps[j] - ea - eb);
+            double x = (L[ab + ij] + Z[ab + ij] + Z[ba + ji]) * inv;
+            Tn[ab + ij] = x;
+            if (Told) { double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
+            if (a != b) {
+                double y = (L[ba + ij] + Z[ba + ij] + Z[ab + ji]) * inv;
+                Tn[ba + ij] = y;
+                if (Told) { double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
+            }
+        }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void divide_by_d_kernel(const double *__restrict__ in, const double *__restrict__ eps, int o,
+                                   int v, double *__restrict__ out) {
+    const long long oo = (long long)o * o, n = oo * v * v;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long ij = x % oo, ab = x / oo;
+        int i = (int)(ij % o), j = (int)(ij / o), a = (int)(ab % v), b = (int)(ab / v);
+        out[x] = in[x] / (eps[i] + eps[j] - eps[o + a] - eps[o + b]);
+    }
+}
+
+__global__ void t_tilde_kernel(const double *__restrict__ T, int o, int v, double *__restrict__ out) {
+    const long long oo = (long long)o * o, n = oo * v * v;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long ij = x % oo, ab = x - ij;
+        int i = (int)(ij % o), j = (int)(ij / o);
+        out[x] = 2.0 * T[x] - T[ab + j + (long long)o * i];
+    }
+}
+
+struct VecList {
+    const double *p[16];
+    double c[16];
+};
+
+__global__ void lincomb_kernel(size_t n, int m, VecList vl, double *__restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < m; ++k) s = fma(vl.c[k], vl.p[k][i], s);
+        out[i] = s;
+    }
+}
+
+__global__ void t1_finalize_kernel(double *__restrict__ t1n, const double *__restrict__ eps, int o, int v,
+                                   const double *__restrict__ t1old, double *part) {
+    double acc = 0.0;
+    const long long n = (long long)o * v;
+    for (long long x = threadIdx.x; x < n; x += blockDim.x) {
+        int i = (int)(x % o), a = (int)(x / o);
+        double val = t1n[x] / (eps[i] - eps[o + a]);
+        t1n[x] = val;
+        if (t1old) { double d = val - t1old[x]; acc = fma(d, d, acc); }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[0] = acc;
+}
+
+unsigned grid_for(long long n, int threads = 256) {
+    long long b = (n + threads - 1) / threads;
+    if (b > 152LL * 32) b = 152LL * 32;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+double finish_reduce(Ctx *ctx, int nblocks) {
+    reduce_partials<<<1, 1024, 0, ctx->stream>>>(ctx->d_red, nblocks, ctx->d_red + 65536 - 8);
+    ctx->count_launch();
+    JUES_CHECK_CUDA(cudaGetLastError());
+    double h = 0.0;
+    JUES_CHECK_CUDA(cudaMemcpyAsync(&h, ctx->d_red + 65536 - 8, sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    JUES_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return h;
+}
+
+}  // namespace
+
+void permute4(Ctx *ctx, const Perm4 &p, double alpha, const double *in, double beta, double *out) {
+    long long total = p.d[0] * p.d[1] * p.d[2] * p.d[3];
+    if (total == 0) return;
+    Ctx::Scope s(ctx, "permute4");
+    permute4_kernel<<<grid_for(total), 256, 0, ctx->stream>>>(p, alpha, in, beta, out, total);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void fill(Ctx *ctx, double *p, size_t n, double v) {
+    if (!n) return;
+    Ctx::Scope s(ctx, "fill");
+    fill_kernel<<<grid_for((long long)n), 256, 0, ctx->stream>>>(p, n, v);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void axpby(Ctx *ctx, size_t n, double a, const double *x, double b, const double *y, double *out) {
+    if (!n) return;
+    Ctx::Scope s(ctx, "axpby");
+    axpby_kernel<<<grid_for((long long)n), 256, 0, ctx->stream>>>(n, a, x, b, y, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+double dot(Ctx *ctx, size_t n, const double *x, const double *y) {
+    {
+        Ctx::Scope s(ctx, "dot");
+        dot_kernel<<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, x, y, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    return finish_reduce(ctx, RED_BLOCKS);
+}
+
+bool any_nonfinite(Ctx *ctx, const double *x, size_t n) {
+    if (!n) return false;
+    JUES_CHECK_CUDA(cudaMemsetAsync(ctx->d_flags + 1, 0, sizeof(unsigned), ctx->stream));
+    {
+        Ctx::Scope s(ctx, "nonfinite");
+        nonfinite_kernel<<<grid_for((long long)n), 256, 0, ctx->stream>>>(n, x, ctx->d_flags + 1);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    unsigned h = 0;
+    JUES_CHECK_CUDA(cudaMemcpyAsync(&h, ctx->d_flags + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    JUES_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return h != 0;
+}
+
+double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v) {
+    long long npair = (long long)v * (v + 1) / 2;
+    int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
+    if (nb < 1) return 0.0;
+    {
+        Ctx::Scope s(ctx, "mp2_energy");
+        mp2_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(K, eps, o, v, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    return finish_reduce(ctx, nb);
+}
+
+double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t1, int o, int v) {
+    long long vv = (long long)v * v;
+    int nb = (int)(vv < RED_BLOCKS ? vv : RED_BLOCKS);
+    if (nb < 1) return 0.0;
+    {
+        Ctx::Scope s(ctx, "cc_energy");
+        ccenergy_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(oovv, T2, t1, o, v, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    return finish_reduce(ctx, nb);
+}
+
+double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *eps, int o, int v,
+                   const double *Told, double *Tn) {
+    long long npair = (long long)v * (v + 1) / 2;
+    int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
+    {
+        Ctx::Scope s(ctx, "t2_finalize");
+        t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, eps, o, v, Told, Tn, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    return Told ? finish_reduce(ctx, nb) : 0.0;
+}
+
+double t1_finalize(Ctx *ctx, double *t1n, const double *eps, int o, int v, const double *t1old) {
+    {
+        Ctx::Scope s(ctx, "t1_finalize");
+        t1_finalize_kernel<<<1, 1024, 0, ctx->stream>>>(t1n, eps, o, v, t1old, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    return t1old ? finish_reduce(ctx, 1) : 0.0;
+}
+
+void divide_by_d(Ctx *ctx, const double *in, const double *eps, int o, int v, double *out) {
+    long long n = (long long)o * o * v * v;
+    Ctx::Scope s(ctx, "divide_by_d");
+    divide_by_d_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(in, eps, o, v, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out) {
+    long long n = (long long)o * o * v * v;
+    Ctx::Scope s(ctx, "t_tilde");
+    t_tilde_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(T, o, v, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out) {
+    JUES_REQUIRE(m >= 1 && m <= 16, "lincomb supports 1..16 vectors");
+    VecList vl;
+    for (int k = 0; k < m; ++k) { vl.p[k] = vecs[k]; vl.c[k] = c[k]; }
+    Ctx::Scope s(ctx, "lincomb");
+    lincomb_kernel<<<grid_for((long long)n), 256, 0, ctx->stream>>>(n, m, vl, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace jues

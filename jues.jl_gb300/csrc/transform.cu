@@ -1,0 +1,125 @@
+// AO->MO four-index transformation (Transformation.jl:39-93, IntegralTransformation.jl:38-101).
+//
+// out[i,a,j,b] = sum C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b] g[mu,nu,lam,sig] is evaluated as four
+// quarter transforms, each one GEMM over composite tensor modes (no explicit permutes).  The
+// reference always contracts sigma first (C4); the result does not depend on the order, so the
+// quarter with the smallest MO dimension goes first, which minimises the flops
+// (F = sum_k 2 n^(5-k) prod_{m<=k} d_(m)).  The last quarter writes straight into the caller's
+// layout: chemists' [i,a,j,b] or, for get_eri's physicists' notation, [i,j,a,b].
+#include <algorithm>
+
+#include "common.cuh"
+#include "transform.cuh"
+
+namespace jues {
+
+double transform4_flops(int n, const int d[4]) {
+    int s[4] = {d[0], d[1], d[2], d[3]};
+    std::sort(s, s + 4);
+    double f = 0.0, prod = 1.0, np = (double)n * n * n * n;
+    for (int k = 0; k < 4; ++k) {
+        prod *= s[k];
+        np /= n;
+        f += 2.0 * np * n * prod;   // 2 n^(5-k) prod d
+    }
+    return f;
+}
+
+void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const C[4], const int d[4],
+                double *out, const long long ostr[4], bool g_const) {
+    for (int p = 0; p < 4; ++p) JUES_REQUIRE(d[p] >= 0, "negative MO dimension");
+    if (d[0] == 0 || d[1] == 0 || d[2] == 0 || d[3] == 0) return;
+    long long dims[4] = {n, n, n, n};
+    bool done[4] = {false, false, false, false};
+    const double *cur = g;
+    DBuf<double> bufs[2];
+    int which = 0;
+    for (int step = 0; step < 4; ++step) {
+        int p = -1;
+        for (int q = 0; q < 4; ++q)
+            if (!done[q] && (p < 0 || d[q] < d[p])) p = q;
+        long long sX[4], nd[4], sY[4];
+        sX[0] = 1;
+        for (int q = 1; q < 4; ++q) sX[q] = sX[q - 1] * dims[q - 1];
+        for (int q = 0; q < 4; ++q) nd[q] = dims[q];
+        nd[p] = d[p];
+        double *dst;
+        if (step == 3) {
+            for (int q = 0; q < 4; ++q) sY[q] = ostr[q];
+            dst = out;
+        } else {
+            sY[0] = 1;
+            for (int q = 1; q < 4; ++q) sY[q] = sY[q - 1] * nd[q - 1];
+            size_t cnt = (size_t)(nd[0] * nd[1] * nd[2] * nd[3]);
+            if (bufs[which].n < cnt) bufs[which] = DBuf<double>(ctx, cnt);
+            dst = bufs[which].p;
+        }
+        int q1 = -1, q2 = -1, q3 = -1;
+        for (int q = 0; q < 4; ++q) {
+            if (q == p) continue;
+            if (q1 < 0) q1 = q; else if (q2 < 0) q2 = q; else q3 = q;
+        }
+        GettArgs a;
+        a.M = dims[q1] * dims[q2] * dims[q3];
+        a.N = d[p];
+        a.K = n;
+        a.alpha = 1.0;
+        a.beta = 0.0;
+        a.A = cur;
+        a.mA = mode3(dims[q1], dims[q2], sX[q1], sX[q2], sX[q3]);
+        a.kA = plain(sX[p]);
+        a.B = C[p];
+        a.kB = plain(1);
+        a.nB = plain(n);
+        a.C = dst;
+        a.mC = mode3(nd[q1], nd[q2], sY[q1], sY[q2], sY[q3]);
+        a.nC = plain(sY[p]);
+        a.a_const = (step == 0) && g_const;
+        a.b_const = false;
+        gett(ctx, prec, a, step == 0 ? "transform_q1" : "transform_q234");
+        for (int q = 0; q < 4; ++q) dims[q] = nd[q];
+        done[p] = true;
+        cur = dst;
+        which ^= 1;
+        // the buffer two steps back is now free for reuse
+    }
+}
+
+void get_eri_block(Ctx *ctx, int prec, const double *g, int n, const double *Cocc, int o,
+                   const double *Cvir, int v, const char spec_in[4], bool phys, int fcn, double *out,
+                   bool g_const) {
+    char s[4] = {spec_in[0], spec_in[1], spec_in[2], spec_in[3]};
+    if (phys) { char t = s[1]; s[1] = s[2]; s[2] = t; }   // IntegralTransformation.jl:46-48
+    const double *C[4];
+    int d[4];
+    for (int q = 0; q < 4; ++q) {
+        char ch = s[q];
+        if (ch == 'o' || ch == 'O') {
+            JUES_REQUIRE(fcn >= 0 && fcn <= o, "fcn out of range");
+            C[q] = Cocc + (size_t)fcn * n;   // drop the first fcn occupied columns (:54,58)
+            d[q] = o - fcn;
+        } else if (ch == 'v' || ch == 'V') {
+            C[q] = Cvir;
+            d[q] = v;
+        } else {
+            throw Error(JUES_EINVAL, std::string("Invalid string given to get_eri: ") +
+                                         std::string(spec_in, 4));
+        }
+    }
+    long long ostr[4];
+    if (phys) {
+        // chem positions (1,2,3,4) = (i,a,j,b) land in phys [i,j,a,b] with dims (d1,d3,d2,d4)
+        ostr[0] = 1;
+        ostr[2] = d[0];
+        ostr[1] = (long long)d[0] * d[2];
+        ostr[3] = (long long)d[0] * d[2] * d[1];
+    } else {
+        ostr[0] = 1;
+        ostr[1] = d[0];
+        ostr[2] = (long long)d[0] * d[1];
+        ostr[3] = (long long)d[0] * d[1] * d[2];
+    }
+    transform4(ctx, prec, g, n, C, d, out, ostr, g_const);
+}
+
+}  // namespace jues

@@ -1,0 +1,181 @@
+"""ctypes binding of libjuesgpu.so (the C ABI declared in include/jues_gpu.h).
+
+There is no CPU fallback: if the shared library is missing or no GB300 is visible,
+every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libjuesgpu.so")
+
+OK, EINVAL, ENOMEM, ECUDA, ENOTCONV, ENONFINITE, ETIMEOUT, ENODEV = range(8)
+PREC = {"fp64": 0, "split_bf16": 1}
+GUESS = {"zero": 0, "mp2": 1, "ovov": 2}
+
+
+class JuESError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class NotConverged(JuESError):
+    pass
+
+
+class CCOpts(C.Structure):
+    _fields_ = [("maxit", C.c_int), ("e_conv", C.c_double), ("r_conv", C.c_double),
+                ("diis", C.c_int), ("diis_size", C.c_int), ("precision", C.c_int),
+                ("guess", C.c_int), ("refine", C.c_int)]
+
+
+class IterLog(C.Structure):
+    _fields_ = [("iter", C.c_int), ("precision", C.c_int), ("energy", C.c_double),
+                ("rnorm", C.c_double), ("ms", C.c_double)]
+
+
+DP = C.POINTER(C.c_double)
+VP = C.c_void_p
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "jues_version": (C.c_int, []),
+    "jues_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "jues_ctx_create": (C.c_int, [C.c_int, C.POINTER(VP)]),
+    "jues_ctx_destroy": (C.c_int, [VP]),
+    "jues_ctx_set_mem_limit": (C.c_int, [VP, C.c_size_t]),
+    "jues_ctx_set_profiling": (C.c_int, [VP, C.c_int]),
+    "jues_ctx_profile": (C.c_int, [VP, C.c_char_p, DP, C.POINTER(C.c_longlong)]),
+    "jues_ctx_profile_reset": (C.c_int, [VP]),
+    "jues_ctx_launch_count": (C.c_longlong, [VP]),
+    "jues_tei_transform": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP,
+                                     C.c_int, C.c_int, DP]),
+    "jues_get_eri": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_char_p, C.c_int,
+                               C.c_int, C.c_int, DP]),
+    "jues_rmp2": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, DP]),
+    "jues_cc_default_opts": (C.c_int, [C.POINTER(CCOpts)]),
+    "jues_rccd": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts), DP,
+                            DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
+    "jues_rccsd": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts), DP,
+                             DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
+    "jues_cc_create": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, DP, C.c_int, DP, C.c_int, DP,
+                                 C.POINTER(CCOpts), C.POINTER(VP)]),
+    "jues_cc_iterate": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "jues_cc_set_precision": (C.c_int, [VP, C.c_int]),
+    "jues_cc_energy": (C.c_int, [VP, DP]),
+    "jues_cc_amplitudes": (C.c_int, [VP, DP, DP]),
+    "jues_cc_log": (C.c_int, [VP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
+    "jues_cc_destroy": (C.c_int, [VP]),
+}
+
+_lib = None
+_lock = threading.Lock()
+_ctxs = {}
+
+
+def load(path: Optional[str] = None):
+    """Load libjuesgpu.so and bind every C ABI symbol (no GPU needed)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise JuESError(ENODEV, f"{p} is not built; run __graft_entry__.build() or "
+                                    "python jues.jl_gb300/build.py")
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(4096)
+    load().jues_last_error(buf, 4096)
+    return buf.value.decode(errors="replace")
+
+
+def check(code: int):
+    if code == OK:
+        return
+    msg = last_error()
+    if code == ENOTCONV:
+        raise NotConverged(code, msg)
+    raise JuESError(code, msg)
+
+
+class Context:
+    """A device context (stream + memory) of the library."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = VP()
+        check(lib.jues_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+        self.lib = lib
+
+    def close(self):
+        if self.h:
+            self.lib.jues_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_mem_limit(self, nbytes: int):
+        check(self.lib.jues_ctx_set_mem_limit(self.h, nbytes))
+
+    def set_profiling(self, on: bool):
+        check(self.lib.jues_ctx_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self, prefix: str):
+        t = C.c_double()
+        n = C.c_longlong()
+        check(self.lib.jues_ctx_profile(self.h, prefix.encode(), C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def profile_reset(self):
+        check(self.lib.jues_ctx_profile_reset(self.h))
+
+    def launches(self) -> int:
+        return int(self.lib.jues_ctx_launch_count(self.h))
+
+
+def context(device: int = 0) -> Context:
+    c = _ctxs.get(device)
+    if c is None or c.h is None:
+        c = Context(device)
+        _ctxs[device] = c
+    return c
+
+
+def f64(x) -> np.ndarray:
+    """Column-major float64 view/copy (Julia layout); Float32 inputs are promoted."""
+    return np.asfortranarray(np.asarray(x, dtype=np.float64))
+
+
+def ptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data_as(DP)
+
+
+def default_opts() -> CCOpts:
+    o = CCOpts()
+    check(load().jues_cc_default_opts(C.byref(o)))
+    return o

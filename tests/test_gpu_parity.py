@@ -1,0 +1,254 @@
+"""GPU parity of the FP64 (drop-in) form against the oracle and the reference's known answers.
+
+Every call goes through the C ABI (juesgpu -> libjuesgpu.so).  Tolerances: 1e-10 Eh on
+energies and 1e-9 on amplitudes (the drop-in bar); 1e-12 relative on integrals.
+"""
+import json
+import os
+import warnings
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import oracle
+from oracle import ccd as occd, ccsd as occsd
+from oracle.mp2 import rmp2_energy
+from juesgpu.Wavefunction import wfn_from_rhf
+from juesgpu.synthetic import make_named, make_system
+
+pytestmark = pytest.mark.gpu
+
+E_MP2_H2O = -0.04914964480386458      # test/TestMollerPlesset.jl:35
+E_CCD_H2O = -0.07015050066089029      # test/TestCoupledCluster.jl:41-42
+E_CCSD_H2O = -0.070680102078571       # test/TestCoupledCluster.jl:44-45
+
+
+@pytest.fixture(scope="module")
+def jg():
+    import juesgpu
+    from juesgpu import CoupledCluster, IntegralTransformation, MollerPlesset, Transformation  # noqa
+    juesgpu.context(0)
+    return juesgpu
+
+
+def h2o():
+    d = np.load(os.path.join(GOLDEN, "h2o_sto3g.npz"))
+    return wfn_from_rhf(d["C"], d["eps"], d["ao_eri"], int(d["nocc"]))
+
+
+def golden():
+    with open(os.path.join(GOLDEN, "synthetic_golden.json")) as f:
+        return json.load(f)
+
+
+# ------------------------------------------------------------------------------ transform
+@pytest.mark.parametrize("n,dims", [(7, (2, 5, 3, 4)), (1, (1, 1, 1, 1)), (13, (13, 1, 6, 13)),
+                                    (70, (9, 61, 9, 61))])
+def test_tei_transform_matches_oracle(jg, n, dims):
+    rng = np.random.default_rng(n)
+    g = rng.normal(size=(n, n, n, n))          # no symmetry assumed
+    Cs = [rng.normal(size=(n, d)) for d in dims]
+    got = jg.Transformation.tei_transform(g, *Cs)
+    want = oracle.tei_transform(g, *Cs)
+    assert got.shape == want.shape
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+
+
+def test_tei_transform_two_argument_form(jg):
+    s = make_system(11, 3, 33, seed=2)
+    g = s.ao_eri()
+    a = jg.Transformation.tei_transform(g, s.C)
+    b = jg.Transformation.tei_transform(g, s.C, s.C, s.C, s.C)
+    assert np.array_equal(a, b)
+    assert np.allclose(a, oracle.tei_transform(g, s.C), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("spec", ["OOVV", "VVVV", "OVVO", "OVOV", "OOOO", "ooov", "ovvv", "oovv"])
+@pytest.mark.parametrize("notation", ["phys", "chem"])
+def test_get_eri_blocks(jg, spec, notation):
+    w = make_system(12, 3, 36, seed=5).wfn()
+    got = jg.IntegralTransformation.get_eri(w, spec, notation)
+    want = oracle.get_eri(w, spec, notation)
+    assert got.shape == want.shape
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-14)
+
+
+def test_get_eri_frozen_core(jg):
+    w = make_system(12, 4, 36, seed=6).wfn()
+    got = jg.IntegralTransformation.get_eri(w, "OOVV", fcn=2)
+    assert np.allclose(got, oracle.get_eri(w, "OOVV", fcn=2), atol=1e-14)
+
+
+def test_get_eri_rejects_bad_spec(jg):
+    w = make_system(8, 2, 24).wfn()
+    with pytest.raises(ValueError):
+        jg.IntegralTransformation.get_eri(w, "OOVX")
+
+
+# ------------------------------------------------------------------------------ MP2
+def test_rmp2_h2o_known_answer(jg):
+    assert abs(jg.MollerPlesset.do_rmp2(h2o()) - E_MP2_H2O) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rmp2_synthetic(jg, name):
+    w = make_named(name).wfn()
+    want = golden()[name]["mp2"]
+    assert abs(jg.MollerPlesset.do_rmp2(w) - want) < 1e-10 * max(1.0, abs(want))
+
+
+def test_rmp2_odd_sizes(jg):
+    for n, o in ((5, 1), (9, 4), (17, 8)):
+        w = make_system(n, o, 3 * n, seed=n).wfn()
+        assert abs(jg.MollerPlesset.do_rmp2(w) - oracle.do_rmp2(w)) < 1e-12
+
+
+# ------------------------------------------------------------------------------ CCD
+def test_rccd_h2o_known_answer(jg):
+    from juesgpu.CoupledCluster import RCCD, mRCCD
+    w = h2o()
+    assert abs(mRCCD.do_rccd(w, maxit=100, r_conv=1e-12) - E_CCD_H2O) < 1e-10
+    assert abs(RCCD.do_rccd(w) - E_CCD_H2O) < 1e-10          # 40 sweeps from (ij|ab)/D
+
+
+def test_rccd_per_iteration_matches_oracle(jg):
+    from juesgpu.CoupledCluster import mRCCD
+    ref = golden()["S25"]["ccd_zero_diis_8"]
+    w = make_named("S25").wfn()
+    e, log = mRCCD.do_rccd(w, maxit=8, r_conv=0.0, return_log=True)
+    assert len(log) == 8
+    for (it, en, rn, ms, p), (rit, ren, rrn) in zip(log, ref):
+        assert it == rit
+        assert abs(en - ren) < 1e-12
+        assert abs(rn - rrn) < 1e-9 * max(1.0, rrn)
+
+
+def test_rccd_amplitudes_match_oracle(jg):
+    from juesgpu.CoupledCluster import mRCCD
+    w = make_named("S25").wfn()
+    e, T2 = mRCCD.do_rccd(w, maxit=60, r_conv=1e-11, return_T2=True, guess="mp2")
+    eo, To, _ = occd.do_rccd(w, maxit=60, r_conv=1e-11, guess="mp2", return_T2=True)
+    assert abs(e - eo) < 1e-10
+    assert np.abs(T2 - To).max() < 1e-9
+    # closed-shell pair symmetry T[i,j,a,b] = T[j,i,b,a]
+    assert np.abs(T2 - np.transpose(T2, (1, 0, 3, 2))).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rccd_converged_energy(jg, name):
+    from juesgpu.CoupledCluster import mRCCD
+    ref = golden()[name]["ccd_mp2guess_diis"]
+    w = make_named(name).wfn()
+    e = mRCCD.do_rccd(w, maxit=60, r_conv=1e-11, guess="mp2")
+    assert abs(e - ref["energy"]) < 1e-10
+
+
+def test_rccd_guesses_reach_same_energy(jg):
+    from juesgpu.CoupledCluster import mRCCD
+    w = make_named("S25").wfn()
+    es = [mRCCD.do_rccd(w, maxit=80, r_conv=1e-11, guess=g) for g in ("zero", "mp2", "ovov")]
+    assert max(es) - min(es) < 1e-11
+
+
+# ------------------------------------------------------------------------------ CCSD
+def test_rccsd_h2o_known_answer(jg):
+    from juesgpu.CoupledCluster import RCCSD
+    assert abs(RCCSD.do_rccsd(h2o()) - E_CCSD_H2O) < 1e-10
+
+
+def test_rccsd_per_iteration_matches_oracle(jg):
+    from juesgpu.CoupledCluster._solve import solve
+    ref = golden()["S25"]["ccsd_plain_6"]
+    w = make_named("S25").wfn()
+    e, t1, T2, nit, log = solve(1, w, maxit=6, r_conv=0.0, diis=False, guess="mp2")
+    for (it, en, rn, ms, p), (rit, ren, rrn) in zip(log, ref):
+        assert abs(en - ren) < 1e-12
+        assert abs(rn - rrn) < 1e-9 * max(1.0, rrn)
+
+
+def test_rccsd_amplitudes_match_oracle(jg):
+    from juesgpu.CoupledCluster import RCCSD
+    w = make_named("S25").wfn()
+    e, t1, T2 = RCCSD.do_rccsd(w, maxit=12, return_T1=True)
+    eo, t1o, T2o, _ = occsd.do_rccsd(w, form="jl", maxit=12, return_T=True)
+    assert abs(e - eo) < 1e-11
+    assert np.abs(t1 - t1o).max() < 1e-10
+    assert np.abs(T2 - T2o).max() < 1e-10
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rccsd_converged_energy(jg, name):
+    from juesgpu.CoupledCluster import RCCSD
+    ref = golden()[name]["ccsd_diis"]
+    w = make_named(name).wfn()
+    e = RCCSD.do_rccsd(w, maxit=60, diis=True, r_conv=1e-11)
+    assert abs(e - ref["energy"]) < 1e-10
+
+
+# ------------------------------------------------------------------------------ sessions
+def test_session_single_sweeps_equal_whole_solve(jg):
+    from juesgpu.CoupledCluster import CCSession, mRCCD
+    w = make_named("S25").wfn()
+    e_whole = mRCCD.do_rccd(w, maxit=6, r_conv=0.0, guess="mp2")
+    s = CCSession(0, w, guess="mp2", r_conv=0.0, maxit=6)
+    for _ in range(6):
+        s.iterate(1)
+    assert s.energy() == e_whole
+    assert len(s.log()) == 6
+    s.close()
+
+
+# ------------------------------------------------------------------------------ errors
+def test_dimension_errors(jg):
+    from juesgpu import _lib
+    import ctypes as C
+    ctx = _lib.context(0)
+    e = C.c_double()
+    g = np.zeros((4, 4, 4, 4), order="F")
+    c = np.zeros((4, 3), order="F")
+    eps = np.zeros(4)
+    st = ctx.lib.jues_rmp2(ctx.h, _lib.ptr(g), 4, _lib.ptr(c), 3, _lib.ptr(c), 3, _lib.ptr(eps), 0,
+                           C.byref(e), None)
+    assert st == _lib.EINVAL and "exceeds" in _lib.last_error()
+    st = ctx.lib.jues_rmp2(ctx.h, None, 4, _lib.ptr(c), 1, _lib.ptr(c), 3, _lib.ptr(eps), 0,
+                           C.byref(e), None)
+    assert st == _lib.EINVAL and "null" in _lib.last_error()
+
+
+def test_memory_cap_gives_enomem(jg):
+    from juesgpu import _lib
+    ctx = _lib.Context(0)
+    ctx.set_mem_limit(1 << 20)
+    w = make_named("S25").wfn()
+    import ctypes as C
+    g = _lib.f64(w.ao_eri)
+    e = C.c_double()
+    st = ctx.lib.jues_rmp2(ctx.h, _lib.ptr(g), 25, _lib.ptr(_lib.f64(w.Cao)), 5,
+                           _lib.ptr(_lib.f64(w.Cav)), 20, _lib.ptr(_lib.f64(w.epsa)), 0, C.byref(e), None)
+    assert st == _lib.ENOMEM
+    ctx.set_mem_limit(0)
+    st = ctx.lib.jues_rmp2(ctx.h, _lib.ptr(g), 25, _lib.ptr(_lib.f64(w.Cao)), 5,
+                           _lib.ptr(_lib.f64(w.Cav)), 20, _lib.ptr(_lib.f64(w.epsa)), 0, C.byref(e), None)
+    assert st == _lib.OK
+    ctx.close()
+
+
+def test_non_convergence_is_reported(jg):
+    from juesgpu.CoupledCluster import mRCCD
+    w = make_named("S25").wfn()
+    with warnings.catch_warnings(record=True) as rec:
+        warnings.simplefilter("always")
+        e = mRCCD.do_rccd(w, maxit=1, r_conv=1e-12)
+    assert any("converge" in str(r.message) for r in rec)
+    assert np.isfinite(e)
+
+
+def test_nonfinite_input_is_rejected(jg):
+    from juesgpu import JuESError
+    from juesgpu.CoupledCluster import mRCCD
+    w = make_system(8, 2, 24).wfn()
+    w.ao_eri[0, 0, 0, 0] = np.nan
+    with pytest.raises(JuESError) as ei:
+        mRCCD.do_rccd(w, maxit=3)
+    assert ei.value.code == 5
