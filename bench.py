@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""RCCD s/iter and TFLOP/s at nbf=200 on one GB300: split-BF16 vs FP64.
+
+Workload: the seeded synthetic closed-shell system nbf=200, nocc=40, nvir=160, naux=600
+(B-factored AO integrals, 12.8 GB).  A "step" is one RCCD sweep (all intermediates, the T2
+update, the energy and the DIIS extrapolation) with the integrals resident in HBM.
+
+Arms:
+  default            libjuesgpu.so: split-BF16 (tcgen05) sweeps timed with CUDA events on the
+                     library's stream; one FP64 sweep beside them; the split energy error against
+                     the FP64 result; e2e = the whole do_rccd C-ABI call with host buffers.
+  --impl reference   the CPU restatement of the reference's GEMM-form sweep (mRCCD.jl) on all
+                     host cores, on the same workload and metric.
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path has no
+data-parallel split of one system); rank 0 prints max-over-ranks timing.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "jues.jl_gb300")]
+
+import numpy as np  # noqa: E402
+
+METRIC = "RCCD s/iter at nbf=200 (split-BF16 tcgen05, FP64 beside)"
+SHAPES = {"S200": ("S200", 200, 40, 600), "S100": ("S100", 100, 20, 300)}
+SHAPE = SHAPES["S200"]
+
+
+def ccd_ref_flops(o, v):
+    """The reference's GEMM set per sweep (mRCCD.jl): 4o^2v^4+16o^3v^3+4o^4v^2+6o^2v^3+6o^3v^2."""
+    o, v = float(o), float(v)
+    return 4 * o**2 * v**4 + 16 * o**3 * v**3 + 4 * o**4 * v**2 + 6 * o**2 * v**3 + 6 * o**3 * v**2
+
+
+def ccd_exec_flops(o, v):
+    """Contractions this library executes per sweep (Wabef never formed)."""
+    o, v = float(o), float(v)
+    return 2 * o**2 * v**4 + 12 * o**3 * v**3 + 4 * o**4 * v**2 + 4 * o**2 * v**3 + 4 * o**3 * v**2
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic():
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def cpu_baseline(system, args):
+    """One sweep of the oracle's restatement of mRCCD.jl (FP64 numpy, all host cores)."""
+    from oracle import ccd
+    from oracle.df_blocks import rccd_blocks_from_B
+    from oracle.mp2 import denominators
+    o = system.nocc
+    blocks = rccd_blocks_from_B(system.B, system.C, o)
+    oovv, ovov, ovvo, oooo, vvvv = blocks
+    D = denominators(system.eps, o)
+    T = oovv / D
+    times = []
+    for _ in range(args.cpu_steps):
+        t0 = time.perf_counter()
+        T = ccd.m_residual_update(T, oovv, vvvv, oooo, ovov, ovvo, D)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args):
+    ws, rank, local, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    from juesgpu.synthetic import make_named
+    system = make_named(SHAPE[0])
+    args.cpu_steps = max(1, args.steps)
+    t_all = time.perf_counter()
+    times = cpu_baseline(system, args)
+    v = statistics.mean(times)
+    cores = os.cpu_count()
+    o, vir = SHAPE[2], SHAPE[1] - SHAPE[2]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/iter", "n_gpus": 1,
+            "steps": len(times), "warmup": 0, "ms_per_step": 1e3 * v, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "rccd_s200", "nbf": 200, "nocc": o, "nvir": vir, "naux": 600,
+                       "sweep": "mRCCD.jl GEMM form, FP64 numpy/OpenBLAS"},
+            "tflops_reference_flops": ccd_ref_flops(o, vir) / v / 1e12,
+            "cpu_baseline": {"value": v, "unit": "s/iter", "cores": cores, "kind": "port",
+                             "sample": "full mRCCD.jl-form sweeps at nbf=200 (oracle restatement; "
+                                       "MO blocks from the B factors)"},
+            "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t_all}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    ws, rank, local, pg = dist_setup(args.gpus)
+    import juesgpu
+    from juesgpu import _lib
+    from juesgpu.CoupledCluster import CCSession, mRCCD
+    from juesgpu.synthetic import make_named
+
+    name, n, o, naux = SHAPE
+    vir = n - o
+    system = make_named(name, seed=rank)
+    gao = system.ao_eri()
+    Cocc, Cvir, eps = system.C[:, :o], system.C[:, o:], system.eps
+    ctx = juesgpu.context(local)
+
+    # ---------------- resident sweeps (value) ----------------
+    t_setup = time.perf_counter()
+    sess = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
+                     guess="mp2", diis=True, r_conv=0.0, refine=0, maxit=10**6)
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        sess.iterate(1)
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    n0 = len(sess.log())
+    launches0 = ctx.launches()
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sess.iterate(1)
+    wall = time.perf_counter() - t0
+    barrier(pg)
+    clocks = clk.stop()
+    launches = ctx.launches() - launches0
+    log = sess.log()[n0:]
+    dev_s = sum(r[3] for r in log) / 1e3
+    pp_ms, pp_n = ctx.profile("ccd_pp_ladder")
+    ring_ms, ring_n = ctx.profile("ccd_ring")
+    pack_ms, pack_n = ctx.profile("pack_split")
+    ctx.set_profiling(False)
+    dev_s = max_over_ranks(pg, dev_s)
+    s_per_iter = dev_s / args.steps
+    # ---------------- FP64 sweeps on the same state ----------------
+    fp64 = None
+    if args.fp64_steps > 0:
+        sess.set_precision("fp64")
+        m0 = len(sess.log())
+        for _ in range(args.fp64_steps):
+            sess.iterate(1)
+        fp64 = sum(r[3] for r in sess.log()[m0:]) / 1e3 / args.fp64_steps
+        sess.set_precision("split_bf16")
+    sess.close()
+
+    # ---------------- energy error: converged split (+FP64 closing sweeps) vs FP64 ----------
+    err = None
+    golden = None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "synthetic_golden.json")) as f:
+            golden = json.load(f).get(name, {}).get("ccd_mp2guess_diis", {}).get("energy")
+    except OSError:
+        pass
+    e_split = None
+    if args.check:
+        s2 = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
+                       guess="mp2", diis=True, r_conv=1e-9, refine=2, maxit=60)
+        s2.iterate(60)
+        e_split = s2.energy()
+        nconv = len(s2.log())
+        s2.close()
+        if golden is not None and rank == 0:
+            err = e_split - golden
+
+    # ---------------- e2e through the C ABI with host buffers ----------------
+    e2e = None
+    if args.e2e_steps > 0:
+        w = system.wfn(ao_eri=gao)
+        barrier(pg)
+        t0 = time.perf_counter()
+        e, lg = mRCCD.do_rccd(w, maxit=args.e2e_steps, r_conv=0.0, guess="mp2", precision="split_bf16",
+                              refine=0, device=local, return_log=True)
+        t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+        h2d = gao.nbytes + system.C.nbytes + eps.nbytes
+        e2e = {"value": t_e2e / len(lg), "unit": "s/iter", "h2d_bytes_per_step": int(h2d / len(lg)),
+               "d2h_bytes_per_step": 8, "sweeps": len(lg), "includes": "H2D of AO ERIs, split transform "
+               "of the 5 RCCD blocks, sweeps, energy read-back"}
+
+    if rank != 0:
+        return
+    pk, pk_kind = peaks()
+    pp_flops_exec = 3 * 2.0 * o**2 * vir**4          # three BF16 products
+    pp_avg_s = (pp_ms / pp_n / 1e3) if pp_n else None
+    achieved = pp_flops_exec / pp_avg_s / 1e12 if pp_avg_s else None
+    peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+    traffic = load_traffic().get(f"ccd_pp_ladder_{name.lower()}")
+    cpu = None
+    if not args.skip_cpu and ws == 1:
+        args.cpu_steps = 1
+        ct = cpu_baseline(system, args)
+        cpu = {"value": statistics.mean(ct), "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full mRCCD.jl-form sweep at nbf=200 (FP64 numpy/OpenBLAS, oracle "
+                         "restatement; MO blocks from the B factors)"}
+    line = {
+        "metric": METRIC, "value": s_per_iter / ws, "unit": "s/iter", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * s_per_iter, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 (fp32 acc) + f64", "data": "synthetic",
+        "config": {"workload": f"rccd_{name.lower()}_split_bf16", "nbf": n, "nocc": o, "nvir": vir, "naux": naux,
+                   "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (packed vvvv 2.6 GB)",
+                   "guess": "mp2", "diis": 6},
+        "tflops_reference_flops": ccd_ref_flops(o, vir) / s_per_iter / 1e12,
+        "tflops_executed_bf16": 3 * ccd_exec_flops(o, vir) / s_per_iter / 1e12,
+        "fp64_s_per_iter": fp64,
+        "speedup_vs_fp64": (fp64 / s_per_iter) if fp64 else None,
+        "energy_split": e_split, "energy_fp64_golden": golden, "energy_error_eh": err,
+        "wall_s_timed": wall, "setup_s": setup_s,
+        "kernels_ms_per_step": {"pp_ladder": pp_ms / args.steps, "ring": ring_ms / args.steps,
+                                "pack_split": pack_ms / args.steps},
+        "roofline": {"bound": "tensor", "kernel": "ccd_pp_ladder (tcgen05 split-BF16 GEMM)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "peak_kind": f"{pk_kind} bf16 sustained",
+                     "flops_per_launch": pp_flops_exec, "launch_ms": 1e3 * pp_avg_s if pp_avg_s else None,
+                     "traffic": traffic},
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-check", dest="check", action="store_false")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--shape", default="S200", choices=sorted(SHAPES),
+                    help="S200 is the benchmark; S100 is the small case used for profiler captures")
+    args = ap.parse_args()
+    global SHAPE
+    SHAPE = SHAPES[args.shape]
+    if args.warmup < 3 and args.impl == "gb300":
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -93,6 +93,14 @@ JUES_API int jues_ctx_profile_reset(jues_ctx *ctx);
 /* Number of kernels this context has launched so far. */
 JUES_API long long jues_ctx_launch_count(jues_ctx *ctx);
 
+/* ---- dense contraction -----------------------------------------------------------------
+ * C = alpha * op(A) op(B) + beta * C, column-major, op = transpose when trans != 0: the
+ * BLAS.gemm! call the reference's explicit-GEMM CC (src/CoupledCluster/mRCCD.jl:274-485)
+ * is built from, run by the same engine as every contraction here (FP64 or split BF16). */
+JUES_API int jues_gemm(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double alpha,
+                       const double *A, int lda, const double *B, int ldb, double beta,
+                       double *C, int ldc, int precision);
+
 /* ---- four-index transformation -------------------------------------------------------
  * out[i,a,j,b] = sum C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b] gao[mu,nu,lam,sig]
  * (chemists' (C1 C2|C3 C4)); gao is n^4, Ck is n x dk, out is d1 x d2 x d3 x d4.

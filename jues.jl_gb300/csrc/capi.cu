@@ -1,4 +1,5 @@
 // extern "C" entry points of libjuesgpu.so (declared in include/jues_gpu.h).
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -31,7 +32,7 @@ int guarded(F &&f) {
     }
 }
 
-Ctx &C(jues_ctx *c) {
+Ctx &CX(jues_ctx *c) {
     if (!c) throw Error(JUES_EINVAL, "null context");
     return c->impl;
 }
@@ -125,16 +126,16 @@ int jues_ctx_destroy(jues_ctx *ctx) {
 }
 
 int jues_ctx_set_mem_limit(jues_ctx *ctx, size_t bytes) {
-    return guarded([&] { C(ctx).mem_limit = bytes; });
+    return guarded([&] { CX(ctx).mem_limit = bytes; });
 }
 
 int jues_ctx_set_profiling(jues_ctx *ctx, int on) {
-    return guarded([&] { C(ctx).profiling = on != 0; });
+    return guarded([&] { CX(ctx).profiling = on != 0; });
 }
 
 int jues_ctx_profile(jues_ctx *ctx, const char *prefix, double *total_ms, long long *launches) {
     return guarded([&] {
-        Ctx &c = C(ctx);
+        Ctx &c = CX(ctx);
         need(prefix, "prefix");
         c.flush_profile();
         double t = 0.0;
@@ -153,7 +154,7 @@ int jues_ctx_profile(jues_ctx *ctx, const char *prefix, double *total_ms, long l
 
 int jues_ctx_profile_reset(jues_ctx *ctx) {
     return guarded([&] {
-        Ctx &c = C(ctx);
+        Ctx &c = CX(ctx);
         c.flush_profile();
         for (auto &kv : c.prof) {
             kv.second.total_ms = 0.0;
@@ -164,11 +165,39 @@ int jues_ctx_profile_reset(jues_ctx *ctx) {
 
 long long jues_ctx_launch_count(jues_ctx *ctx) { return ctx ? ctx->impl.launches : -1; }
 
+int jues_gemm(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double alpha, const double *A,
+              int lda, const double *B, int ldb, double beta, double *C, int ldc, int precision) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(A, "A"); need(B, "B"); need(C, "C");
+        if (M < 0 || N < 0 || K < 0) throw Error(JUES_EINVAL, "negative GEMM dimension");
+        const int ar = transA ? K : M, br = transB ? N : K;
+        if (lda < std::max(1, ar) || ldb < std::max(1, br) || ldc < std::max(1, M))
+            throw Error(JUES_EINVAL, "leading dimension too small");
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        if (M == 0 || N == 0) return;
+        cudaSetDevice(c.device);
+        const size_t na = (size_t)lda * (transA ? M : K), nb = (size_t)ldb * (transB ? K : N),
+                     nc = (size_t)ldc * N;
+        DBuf<double> dA = h2d(c, A, na), dB = h2d(c, B, nb), dC = h2d(c, C, nc);
+        GettArgs g;
+        g.M = M; g.N = N; g.K = K;
+        g.alpha = alpha; g.beta = beta;
+        g.A = dA.p; g.mA = transA ? plain(lda) : plain(1); g.kA = transA ? plain(1) : plain(lda);
+        g.B = dB.p; g.kB = transB ? plain(ldb) : plain(1); g.nB = transB ? plain(1) : plain(ldb);
+        g.C = dC.p; g.mC = plain(1); g.nC = plain(ldc);
+        gett(&c, precision, g, "gemm");
+        d2h(c, C, dC.p, nc);
+        c.check_flags();
+    });
+}
+
 int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1, int d1, const double *C2,
                        int d2, const double *C3, int d3, const double *C4, int d4, int precision,
                        double *out) {
     return guarded([&] {
-        Ctx &c = C(ctx);
+        Ctx &c = CX(ctx);
         need(gao, "gao");
         need(C1, "C1"); need(C2, "C2"); need(C3, "C3"); need(C4, "C4");
         need(out, "out");
@@ -195,7 +224,7 @@ int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1
 int jues_get_eri(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,
                  const char *spec, int phys, int fcn, int precision, double *out) {
     return guarded([&] {
-        Ctx &c = C(ctx);
+        Ctx &c = CX(ctx);
         need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(spec, "spec"); need(out, "out");
         if (std::strlen(spec) != 4)
             throw Error(JUES_EINVAL, std::string("Invalid string given to get_eri: ") + spec);
@@ -227,7 +256,7 @@ int jues_get_eri(jues_ctx *ctx, const double *gao, int n, const double *Cocc, in
 int jues_rmp2(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,
               const double *eps, int precision, double *e_out, double *k_out) {
     return guarded([&] {
-        Ctx &c = C(ctx);
+        Ctx &c = CX(ctx);
         need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(e_out, "e_out");
         check_dims(n, o, v);
         if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
@@ -264,7 +293,7 @@ int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_devi
                    int o, const double *Cvir, int v, const double *eps, const jues_cc_opts *opts,
                    jues_cc **out) {
     return guarded([&] {
-        Ctx &c = C(ctx);
+        Ctx &c = CX(ctx);
         need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(out, "out");
         *out = nullptr;
         check_dims(n, o, v);

@@ -1,4 +1,6 @@
 // Context: stream, memory accounting, per-kernel event timing, error flags.
+#include <nvtx3/nvToolsExt.h>
+
 #include <cstring>
 
 #include "common.cuh"
@@ -50,6 +52,7 @@ void Ctx::free(void *p, size_t bytes) {
 
 Ctx::Scope::Scope(Ctx *c_, const char *name) : c(c_) {
     c->count_launch();
+    nvtxRangePushA(name);   // lets a profiler select launches by name
     if (!c->profiling) return;
     r = &c->prof[name];
     if (!r->pool.empty()) {
@@ -63,6 +66,7 @@ Ctx::Scope::Scope(Ctx *c_, const char *name) : c(c_) {
 }
 
 Ctx::Scope::~Scope() {
+    nvtxRangePop();
     if (!r) return;
     cudaEventRecord(ev.second, c->stream);
     r->pending.push_back(ev);

@@ -1,16 +1,495 @@
-// Split-precision (BF16 hi+lo, three products, FP32 accumulation) GEMM on the tcgen05 tensor
-// cores.  Placeholder until the tcgen05 kernel lands: refuses loudly.
+// Split-precision GEMM over tensor modes on the sm_103a tensor cores (tcgen05 + TMEM + TMA).
+//
+// Each FP64 operand x is written as two BF16 planes, hi = bf16(x) and lo = bf16(x - hi)
+// (|x - hi - lo| <= 2^-16 |x|), K-major and zero-padded to the tile grid.  One CTA computes a
+// 128 x BN tile of C = A.B^T as three tcgen05.mma products per K-step,
+//     A_hi.B_hi + A_hi.B_lo + A_lo.B_hi,
+// accumulated in FP32 in tensor memory; the dropped A_lo.B_lo term is O(2^-16).  Operand tiles
+// arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by mbarriers;
+// one thread issues the TMA loads, one thread issues the MMAs, and all four warps drain TMEM in
+// the epilogue, which applies alpha/beta in FP64 and scatters through the output tensor modes.
+// Every mbarrier wait is bounded by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips
+// its stores, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "common.cuh"
 
 namespace jues {
 
-struct PackCache {};
+namespace {
 
-void gett_tc(Ctx *, const GettArgs &, const char *) {
-    throw Error(JUES_EINVAL, "split-BF16 precision is not available in this build");
+constexpr int TBM = 128;   // tile rows (TMEM lanes)
+constexpr int TBK = 64;    // K elements per stage: 128 bytes of BF16 = one swizzle atom row
+constexpr unsigned long long WAIT_LIMIT_NS = 2ull * 1000 * 1000 * 1000;    // 2 s: legitimate waits last microseconds
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-void pack_cache_clear(Ctx *) {}
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; false when the time limit expired, another thread of the CTA aborted, or
+// another CTA already raised FLAG_TIMEOUT
+__device__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                          const volatile unsigned *gflags) {
+    unsigned long long t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            if (*abort_flag || (*gflags & FLAG_TIMEOUT)) return false;
+            unsigned long long t = gtimer();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > WAIT_LIMIT_NS) return false;
+        }
+    }
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
+                                            int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+// D[tmem] (+)= A[smem desc] . B[smem desc]^T, BF16 inputs, FP32 accumulation
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+// 32 lanes x 32 consecutive 32-bit TMEM columns -> 32 registers per thread
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// UMMA shared-memory descriptor of a K-major tile written by TMA with 128-byte swizzle:
+// start address >> 4, LBO unused (1), SBO = 1024 bytes between 8-row groups, version 1,
+// layout type 2 = SWIZZLE_128B.
+__device__ __forceinline__ uint64_t sw128_desc(const void *smem) {
+    const uint64_t a = smem_u32(smem);
+    return ((a & 0x3FFFFull) >> 4) | (1ull << 16) | (64ull << 32) | (1ull << 46) | (2ull << 61);
+}
+
+struct TcArgs {
+    long long M, N;        // logical GEMM extent (rows of A, rows of B)
+    int kblocks;           // padded K / TBK
+    long long mtiles;
+    double alpha, beta;
+    double *C;
+    const double *Cin;
+    Mode mC, nC;
+    unsigned *flags;
+};
+
+template <int BN, int STAGES>
+struct TcCfg {
+    static constexpr int A_BYTES = TBM * TBK * 2;
+    static constexpr int B_BYTES = BN * TBK * 2;
+    static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+    static constexpr int BAR_BYTES = 256;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 1024;
+    // instruction descriptor: FP32 accumulate, BF16 A and B, both K-major, M = 128, N = BN
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                      ((uint32_t)(TBM >> 4) << 24);
+};
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(128, 1)
+    gett_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs g) {
+    using Cfg = TcCfg<BN, STAGES>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *stages = smem;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * Cfg::STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *accf = empty + STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accf + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    long long *coloff = reinterpret_cast<long long *>(smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long mt = blockIdx.x % g.mtiles, nt = blockIdx.x / g.mtiles;
+    const int m0 = (int)(mt * TBM), n0 = (int)(nt * BN);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accf, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, BN);
+        tmem_relinquish();
+    }
+    for (int c = threadIdx.x; c < BN; c += blockDim.x) {
+        const long long n = (long long)n0 + c;
+        coloff[c] = n < g.N ? mode_off(g.nC, n) : -1;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int nk = g.kblocks;
+
+    if (warp == 0 && lane == 0) {
+        // TMA producer
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % STAGES;
+            const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+            if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, g.flags)) {
+                *abort_flag = 1;
+                break;
+            }
+            uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+            mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
+            tma_load_3d(st, &mapA, &full[s], kb * TBK, m0, 0);
+            tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kb * TBK, m0, 1);
+            tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kb * TBK, n0, 0);
+            tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kb * TBK, n0, 1);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % STAGES;
+            const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+            if (!mbar_wait(&full[s], ph, abort_flag, g.flags)) {
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+            const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
+            const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
+            const uint64_t bl = sw128_desc(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < TBK / 16; ++kk) {
+                const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
+                umma_bf16(tmem, ah + off, bh + off, Cfg::IDESC, (kb | kk) != 0 ? 1u : 0u);
+                umma_bf16(tmem, ah + off, bl + off, Cfg::IDESC, 1u);
+                umma_bf16(tmem, al + off, bh + off, Cfg::IDESC, 1u);
+            }
+            umma_commit(&empty[s]);   // stage s is free once these MMAs complete
+        }
+        umma_commit(accf);            // accumulator complete
+    }
+
+    // epilogue: warp w drains TMEM lanes [32w, 32w+32) = tile rows
+    const bool ok = mbar_wait(accf, 0u, abort_flag, g.flags);
+    __syncwarp();
+    tc_fence_after();
+    if (!ok || *abort_flag) {
+        if (lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
+    } else {
+        const long long m = (long long)m0 + warp * 32 + lane;
+        const long long rowoff = m < g.M ? mode_off(g.mC, m) : -1;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+            tmem_ld_wait();
+            if (rowoff >= 0) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const long long co = coloff[c0 + j];
+                    if (co >= 0) {
+                        double val = g.alpha * (double)__uint_as_float(r[j]);
+                        if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
+                        g.C[rowoff + co] = val;
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, BN);
+    }
+}
+
+// FP64 operand (rows via rmode, K via kmode) -> BF16 hi/lo planes [2][Rpad][Kpad], K-major
+constexpr int PR = 32, PK = 64;
+__global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
+                                                         long long R, long long K, long long Rpad,
+                                                         long long Kpad, int kfast,
+                                                         __nv_bfloat16 *__restrict__ dst) {
+    __shared__ double tile[PR][PK + 1];
+    __shared__ long long roff[PR], koff[PK];
+    const long long kblocks = Kpad / PK;
+    const long long r0 = (blockIdx.x / kblocks) * PR;
+    const long long k0 = (blockIdx.x % kblocks) * PK;
+    const int tid = threadIdx.x;
+    if (tid < PR) {
+        const long long r = r0 + tid;
+        roff[tid] = r < R ? mode_off(rmode, r) : -1;
+    } else if (tid >= 64 && tid < 64 + PK) {
+        const long long k = k0 + tid - 64;
+        koff[tid - 64] = k < K ? mode_off(kmode, k) : -1;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < (PR * PK) / 256; ++i) {
+        const int e = tid + i * 256;
+        const int kk = kfast ? (e % PK) : (e / PR);
+        const int rr = kfast ? (e / PK) : (e % PR);
+        const long long a = roff[rr], b = koff[kk];
+        tile[rr][kk] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
+    }
+    __syncthreads();
+    // each thread writes 8 consecutive K values of one row to both planes (16-byte stores)
+    const int rr = tid >> 3, kc = (tid & 7) * 8;
+    __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const double x = tile[rr][kc + j];
+        const __nv_bfloat16 h = __double2bfloat16(x);
+        hi[j] = h;
+        lo[j] = __double2bfloat16(x - (double)__bfloat162float(h));
+    }
+    const size_t base = (size_t)(r0 + rr) * (size_t)Kpad + (size_t)(k0 + kc);
+    *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
+    *reinterpret_cast<uint4 *>(dst + (size_t)Rpad * Kpad + base) = *reinterpret_cast<const uint4 *>(lo);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        JUES_CHECK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p)
+            throw Error(JUES_ECUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+CUtensorMap make_map(const __nv_bfloat16 *base, long long rows_pad, long long kpad, int box_rows) {
+    CUtensorMap m;
+    std::memset(&m, 0, sizeof(m));
+    cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, 2};
+    cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
+    cuuint32_t box[3] = {(cuuint32_t)TBK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dims,
+                              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(JUES_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return m;
+}
+
+long long roundup(long long x, long long m) { return (x + m - 1) / m * m; }
+
+bool same_mode(const Mode &a, const Mode &b) {
+    return a.d0 == b.d0 && a.d1 == b.d1 && a.s0 == b.s0 && a.s1 == b.s1 && a.s2 == b.s2;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// packed-operand cache: scratch planes for transient operands, persistent planes for
+// operands declared constant (integrals), dropped explicitly.
+// ---------------------------------------------------------------------------------------
+struct PackEntry {
+    const double *src;
+    Mode r, k;
+    long long R, K, Rpad, Kpad;
+    DBuf<__nv_bfloat16> buf;
+};
+struct PackCache {
+    std::vector<std::unique_ptr<PackEntry>> cached;
+    DBuf<__nv_bfloat16> scratch[2];
+};
+
 void pack_cache_destroy(PackCache *p) { delete p; }
-void pack_cache_drop(Ctx *, const void *) {}
+void pack_cache_clear(Ctx *ctx) {
+    if (ctx->pack) ctx->pack->cached.clear();
+}
+void pack_cache_drop(Ctx *ctx, const void *ptr) {
+    if (!ctx->pack) return;
+    auto &v = ctx->pack->cached;
+    v.erase(std::remove_if(v.begin(), v.end(), [&](const std::unique_ptr<PackEntry> &e) { return e->src == ptr; }),
+            v.end());
+}
+
+static const __nv_bfloat16 *pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm, const Mode &km,
+                                         long long R, long long K, long long Rpad, long long Kpad, bool cache) {
+    if (!ctx->pack) ctx->pack = new PackCache();
+    PackCache &pc = *ctx->pack;
+    if (cache) {
+        for (auto &e : pc.cached)
+            if (e->src == src && e->R == R && e->K == K && e->Rpad == Rpad && e->Kpad == Kpad &&
+                same_mode(e->r, rm) && same_mode(e->k, km))
+                return e->buf.p;
+    }
+    const size_t need = (size_t)2 * Rpad * Kpad;
+    __nv_bfloat16 *dst;
+    std::unique_ptr<PackEntry> ent;
+    if (cache) {
+        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__nv_bfloat16>(ctx, need)});
+        dst = ent->buf.p;
+    } else {
+        if (pc.scratch[slot].n < need) {
+            pc.scratch[slot].reset();
+            pc.scratch[slot] = DBuf<__nv_bfloat16>(ctx, need);
+        }
+        dst = pc.scratch[slot].p;
+    }
+    const long long blocks = (Rpad / PR) * (Kpad / PK);
+    JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
+    const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
+    {
+        Ctx::Scope s(ctx, "pack_split");
+        pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, dst);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    if (cache) pc.cached.push_back(std::move(ent));
+    return dst;
+}
+
+template <int BN, int STAGES>
+static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
+                      const char *name) {
+    using Cfg = TcCfg<BN, STAGES>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             Cfg::SMEM));
+        attr_set = true;
+    }
+    Ctx::Scope s(ctx, name);
+    gett_tc_kernel<BN, STAGES><<<(unsigned)tiles, 128, Cfg::SMEM, ctx->stream>>>(ma, mb, t);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
+    if (a0.M <= 0 || a0.N <= 0) return;
+    GettArgs a = a0;
+    // Orientation: the output's unit-stride mode on the row (TMEM lane) side lets each warp
+    // store 32 consecutive doubles per column; weigh that against the padding of both tile
+    // grids (rows pad to 128, columns to the chosen BN).
+    auto pad_cost = [](long long M, long long N, bool unit_rows) {
+        long long best = -1;
+        for (int cand : {256, 128, 64}) {
+            long long p = roundup(N, cand);
+            if (best < 0 || p < best) best = p;
+        }
+        return (double)roundup(M, TBM) * (double)best * (unit_rows ? 1.0 : 1.35);
+    };
+    const bool m_unit = a.mC.s0 == 1 && a.mC.d0 > 1;
+    const bool n_unit = a.nC.s0 == 1 && a.nC.d0 > 1;
+    if (pad_cost(a.N, a.M, n_unit) < pad_cost(a.M, a.N, m_unit)) {
+        std::swap(a.M, a.N);
+        std::swap(a.A, a.B);
+        std::swap(a.mA, a.nB);
+        std::swap(a.kA, a.kB);
+        std::swap(a.mC, a.nC);
+        std::swap(a.a_const, a.b_const);
+    }
+    // skinny or tiny contractions stay in FP64
+    if (a.N < 16 || a.M < 16 || a.K < 16) {
+        gett_f64(ctx, a0, name);
+        return;
+    }
+    // tile width: smallest padded N, preferring wider tiles on ties
+    int BN = 256;
+    {
+        long long best = -1;
+        for (int cand : {256, 128, 64}) {
+            long long p = roundup(a.N, cand);
+            if (best < 0 || p < best) { best = p; BN = cand; }
+        }
+    }
+    const long long Mpad = roundup(a.M, TBM), Npad = roundup(a.N, BN), Kpad = roundup(a.K, TBK);
+    JUES_REQUIRE(Mpad < (1LL << 31) && Npad < (1LL << 31) && Kpad / TBK < (1LL << 30),
+                 "GEMM extent exceeds the TMA coordinate range");
+    const __nv_bfloat16 *pa = pack_operand(ctx, 0, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, a.a_const);
+    const __nv_bfloat16 *pb = pack_operand(ctx, 1, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, a.b_const);
+    const CUtensorMap ma = make_map(pa, Mpad, Kpad, TBM);
+    const CUtensorMap mb = make_map(pb, Npad, Kpad, BN);
+    TcArgs t;
+    t.M = a.M;
+    t.N = a.N;
+    t.kblocks = (int)(Kpad / TBK);
+    t.mtiles = Mpad / TBM;
+    t.alpha = a.alpha;
+    t.beta = a.beta;
+    t.C = a.C;
+    t.Cin = a.Cin ? a.Cin : a.C;
+    t.mC = a.mC;
+    t.nC = a.nC;
+    t.flags = ctx->d_flags;
+    const long long tiles = t.mtiles * (Npad / BN);
+    JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
+    if (BN == 256)
+        launch_tc<256, 2>(ctx, ma, mb, t, tiles, name);
+    else if (BN == 128)
+        launch_tc<128, 3>(ctx, ma, mb, t, tiles, name);
+    else
+        launch_tc<64, 4>(ctx, ma, mb, t, tiles, name);
+}
 
 }  // namespace jues

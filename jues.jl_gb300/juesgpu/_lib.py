@@ -55,6 +55,8 @@ SIGNATURES = {
     "jues_ctx_profile": (C.c_int, [VP, C.c_char_p, DP, C.POINTER(C.c_longlong)]),
     "jues_ctx_profile_reset": (C.c_int, [VP]),
     "jues_ctx_launch_count": (C.c_longlong, [VP]),
+    "jues_gemm": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, DP, C.c_int,
+                            DP, C.c_int, C.c_double, DP, C.c_int, C.c_int]),
     "jues_tei_transform": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP,
                                      C.c_int, C.c_int, DP]),
     "jues_get_eri": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_char_p, C.c_int,
@@ -173,6 +175,23 @@ def ptr(a: Optional[np.ndarray]):
     if a is None:
         return None
     return a.ctypes.data_as(DP)
+
+
+def gemm(A, B, C=None, alpha=1.0, beta=0.0, transA=False, transB=False, precision="fp64",
+         device=0) -> np.ndarray:
+    """C = alpha op(A) op(B) + beta C on the GPU (column-major, like BLAS.gemm!)."""
+    A = f64(A)
+    B = f64(B)
+    M = A.shape[1] if transA else A.shape[0]
+    K = A.shape[0] if transA else A.shape[1]
+    N = B.shape[0] if transB else B.shape[1]
+    if (B.shape[1] if transB else B.shape[0]) != K:
+        raise ValueError("inner dimensions differ")
+    Cm = np.zeros((M, N), order="F") if C is None else f64(C).copy(order="F")
+    ctx = context(device)
+    check(ctx.lib.jues_gemm(ctx.h, int(transA), int(transB), M, N, K, alpha, ptr(A), max(1, A.shape[0]),
+                            ptr(B), max(1, B.shape[0]), beta, ptr(Cm), max(1, M), PREC[precision]))
+    return Cm
 
 
 def default_opts() -> CCOpts:

@@ -65,8 +65,9 @@ class SyntheticSystem:
         """(mu nu|lambda sigma) as an n^4 column-major array (Julia layout)."""
         n = self.nbf
         Bm = self.B.reshape(self.naux, n * n)
-        g = Bm.T @ Bm                       # symmetric n^2 x n^2
-        return np.asfortranarray(g.reshape(n, n, n, n, order="F"))
+        g = Bm.T @ Bm                       # symmetric n^2 x n^2 (C order)
+        # g.T is the same matrix as an F-ordered view, so no copy is made at nbf = 200
+        return g.T.reshape(n, n, n, n, order="F")
 
     def wfn(self, ao_eri: Optional[np.ndarray] = None) -> Wfn:
         g = self.ao_eri() if ao_eri is None else ao_eri

@@ -1,0 +1,118 @@
+"""GPU checks of the split-BF16 (tcgen05) form.
+
+Two bars: against an exact emulation of the three BF16 products (hi.hi + hi.lo + lo.hi, FP64
+sums) the kernel may differ only by FP32 accumulation (rel 2e-6); against FP64 the error is
+the split truncation, O(2^-16) per product.  Energies: within 1 uEh of the FP64 oracle.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import oracle
+from juesgpu.synthetic import make_named, make_system
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(x):
+    x32 = np.asarray(x, dtype=np.float64).astype(np.float32)
+    b = x32.view(np.uint32).astype(np.uint64)
+    r = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def split(x):
+    # the kernel rounds FP64 -> BF16 directly; rounding via FP32 first differs only on ties
+    hi = bf16(x)
+    return hi, bf16(x - hi)
+
+
+def emulate(A, B):
+    ah, al = split(A)
+    bh, bl = split(B)
+    return ah @ bh + ah @ bl + al @ bh
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from juesgpu import _lib
+    _lib.context(0)
+    return _lib
+
+
+SHAPES = [(128, 128, 64, False, False), (200, 72, 300, False, True), (1000, 257, 129, True, False),
+          (77, 1000, 640, True, True), (4096, 300, 2000, False, False), (640, 64, 6400, False, False),
+          (33, 4000, 513, False, True)]
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb", SHAPES)
+def test_gemm_fp64(lib, M, N, K, ta, tb):
+    rng = np.random.default_rng(M + N + K)
+    A = rng.normal(size=(K, M) if ta else (M, K))
+    B = rng.normal(size=(N, K) if tb else (K, N))
+    C0 = rng.normal(size=(M, N))
+    got = lib.gemm(A, B, C0, alpha=0.7, beta=-1.3, transA=ta, transB=tb)
+    want = 0.7 * ((A.T if ta else A) @ (B.T if tb else B)) - 1.3 * C0
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-11 * np.sqrt(K))
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb", SHAPES)
+def test_gemm_split_bf16(lib, M, N, K, ta, tb):
+    rng = np.random.default_rng(7 * M + N + K)
+    A = rng.normal(size=(K, M) if ta else (M, K))
+    B = rng.normal(size=(N, K) if tb else (K, N))
+    C0 = rng.normal(size=(M, N))
+    got = lib.gemm(A, B, C0, alpha=0.7, beta=-1.3, transA=ta, transB=tb, precision="split_bf16")
+    Aop, Bop = (A.T if ta else A), (B.T if tb else B)
+    emu = 0.7 * emulate(Aop, Bop) - 1.3 * C0
+    exact = 0.7 * (Aop @ Bop) - 1.3 * C0
+    scale = np.sqrt(K)
+    # only FP32 accumulation separates the kernel from the exact three-product emulation
+    assert np.abs(got - emu).max() < 2e-6 * scale
+    # and the split keeps ~16 bits: far better than one BF16 product (~4e-3 relative)
+    assert np.abs(got - exact).max() < 1e-4 * scale
+
+
+def test_transform_split(lib):
+    import juesgpu.Transformation as Tr
+    s = make_system(48, 12, 144, seed=9)
+    g = s.ao_eri()
+    rng = np.random.default_rng(1)
+    Cs = [s.C[:, :12], s.C[:, 12:], s.C[:, :12], s.C[:, 12:]]
+    got = Tr.tei_transform(g, *Cs, precision="split_bf16")
+    want = oracle.tei_transform(g, *Cs)
+    assert np.abs(got - want).max() < 1e-4 * np.abs(want).max()
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rmp2_split(lib, name):
+    from juesgpu import MollerPlesset
+    with open(os.path.join(GOLDEN, "synthetic_golden.json")) as f:
+        ref = json.load(f)[name]["mp2"]
+    e = MollerPlesset.do_rmp2(make_named(name).wfn(), precision="split_bf16")
+    assert abs(e - ref) < 1e-6
+
+
+@pytest.mark.parametrize("refine", [0, 2])
+def test_rccd_split_within_one_microhartree(lib, refine):
+    from juesgpu.CoupledCluster import mRCCD
+    with open(os.path.join(GOLDEN, "synthetic_golden.json")) as f:
+        ref = json.load(f)["S100"]["ccd_mp2guess_diis"]["energy"]
+    w = make_named("S100").wfn()
+    e, log = mRCCD.do_rccd(w, maxit=40, r_conv=1e-9, guess="mp2", precision="split_bf16",
+                           refine=refine, return_log=True)
+    assert abs(e - ref) < 1e-6, (e, ref, log)
+    if refine:
+        assert log[-1][4] == 0 and log[0][4] == 1      # closing sweeps ran in FP64
+
+
+def test_rccsd_split(lib):
+    from juesgpu.CoupledCluster import RCCSD
+    with open(os.path.join(GOLDEN, "synthetic_golden.json")) as f:
+        ref = json.load(f)["S25"]["ccsd_diis"]["energy"]
+    e = RCCSD.do_rccsd(make_named("S25").wfn(), maxit=60, diis=True, r_conv=1e-9,
+                       precision="split_bf16", refine=2)
+    assert abs(e - ref) < 1e-6
