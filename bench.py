@@ -142,22 +142,22 @@ def load_traffic():
         return {}
 
 
-def cpu_baseline(system, args):
-    """One sweep of the oracle's restatement of mRCCD.jl (FP64 numpy, all host cores)."""
-    from oracle import ccd
+CPU_SLICES = 16
+
+
+def cpu_sampler(system):
+    """The reference's RCCD.jl sweep on the host cores, sliced into CPU_SLICES shares."""
     from oracle.df_blocks import rccd_blocks_from_B
-    from oracle.mp2 import denominators
-    o = system.nocc
-    blocks = rccd_blocks_from_B(system.B, system.C, o)
-    oovv, ovov, ovvo, oooo, vvvv = blocks
-    D = denominators(system.eps, o)
-    T = oovv / D
-    times = []
-    for _ in range(args.cpu_steps):
-        t0 = time.perf_counter()
-        T = ccd.m_residual_update(T, oovv, vvvv, oooo, ovov, ovvo, D)
-        times.append(time.perf_counter() - t0)
-    return times
+    from oracle.sampled import SlicedSweep
+    blocks = rccd_blocks_from_B(system.B, system.C, system.nocc)
+    return SlicedSweep(*blocks, system.eps, system.nocc, slices=CPU_SLICES)
+
+
+def cpu_baseline(system, nsteps):
+    """s/iter estimate = mean time of one 1/CPU_SLICES share of the sweep x CPU_SLICES."""
+    sw = cpu_sampler(system)
+    times = [sw.step(k) for k in range(nsteps)]
+    return statistics.mean(times) * CPU_SLICES, times
 
 
 def run_reference(args):
@@ -165,22 +165,29 @@ def run_reference(args):
     if rank != 0:
         return
     from juesgpu.synthetic import make_named
-    system = make_named(SHAPE[0])
-    args.cpu_steps = max(1, args.steps)
+    name, n, o, naux = SHAPE
+    vir = n - o
+    system = make_named(name)
     t_all = time.perf_counter()
-    times = cpu_baseline(system, args)
-    v = statistics.mean(times)
+    sw = cpu_sampler(system)
+    for k in range(args.warmup):
+        sw.step(k)
+    times = [sw.step(args.warmup + k) for k in range(args.steps)]
+    v = statistics.mean(times) * CPU_SLICES
     cores = os.cpu_count()
-    o, vir = SHAPE[2], SHAPE[1] - SHAPE[2]
+    sample = (f"each step = 1/{CPU_SLICES} of one RCCD.jl-form sweep at nbf={n} (oracle restatement, "
+              "FP64 numpy/OpenBLAS): intermediates contracted over one slice of a virtual index, "
+              "T2 update for one slice of output columns; value = mean step time x "
+              f"{CPU_SLICES}")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/iter", "n_gpus": 1,
-            "steps": len(times), "warmup": 0, "ms_per_step": 1e3 * v, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "rccd_s200", "nbf": 200, "nocc": o, "nvir": vir, "naux": 600,
-                       "sweep": "mRCCD.jl GEMM form, FP64 numpy/OpenBLAS"},
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * v,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"rccd_{name.lower()}", "nbf": n, "nocc": o, "nvir": vir,
+                       "naux": naux, "sweep": "RCCD.jl einsum form, FP64 numpy/OpenBLAS"},
             "tflops_reference_flops": ccd_ref_flops(o, vir) / v / 1e12,
             "cpu_baseline": {"value": v, "unit": "s/iter", "cores": cores, "kind": "port",
-                             "sample": "full mRCCD.jl-form sweeps at nbf=200 (oracle restatement; "
-                                       "MO blocks from the B factors)"},
+                             "sample": sample},
             "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t_all}
     print(json.dumps(line), flush=True)
@@ -283,11 +290,11 @@ def run_gpu(args):
     traffic = load_traffic().get(f"ccd_pp_ladder_{name.lower()}")
     cpu = None
     if not args.skip_cpu and ws == 1:
-        args.cpu_steps = 1
-        ct = cpu_baseline(system, args)
-        cpu = {"value": statistics.mean(ct), "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one full mRCCD.jl-form sweep at nbf=200 (FP64 numpy/OpenBLAS, oracle "
-                         "restatement; MO blocks from the B factors)"}
+        val, ct = cpu_baseline(system, args.cpu_steps)
+        cpu = {"value": val, "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{len(ct)} of {CPU_SLICES} shares of one RCCD.jl-form sweep at nbf={n} "
+                         f"(oracle restatement, FP64 numpy/OpenBLAS, {sum(ct):.1f} s of CPU work); "
+                         f"value = mean share time x {CPU_SLICES}"}
     line = {
         "metric": METRIC, "value": s_per_iter / ws, "unit": "s/iter", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * s_per_iter, "higher_is_better": False,
@@ -324,6 +331,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-check", dest="check", action="store_false")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=4, help="CPU baseline shares to time")
     ap.add_argument("--shape", default="S200", choices=sorted(SHAPES),
                     help="S200 is the benchmark; S100 is the small case used for profiler captures")
     args = ap.parse_args()

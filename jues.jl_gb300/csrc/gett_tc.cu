@@ -6,8 +6,10 @@
 //     A_hi.B_hi + A_hi.B_lo + A_lo.B_hi,
 // accumulated in FP32 in tensor memory; the dropped A_lo.B_lo term is O(2^-16).  Operand tiles
 // arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by mbarriers;
-// one thread issues the TMA loads, one thread issues the MMAs, and all four warps drain TMEM in
-// the epilogue, which applies alpha/beta in FP64 and scatters through the output tensor modes.
+// one thread issues the TMA loads, one thread issues the MMAs into two alternating TMEM
+// accumulators (one per chunk of KC stages), and four warps add finished chunks into FP32
+// registers with round-to-nearest, then apply alpha/beta in FP64 and scatter through the
+// output tensor modes.
 // Every mbarrier wait is bounded by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips
 // its stores, frees its TMEM and returns.
 #include <cuda.h>
@@ -139,48 +141,66 @@ struct TcArgs {
     unsigned *flags;
 };
 
-template <int BN, int STAGES>
+// Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-5 drain TMEM.
+// The tensor core adds each MMA into its FP32 accumulator with truncation, so the error of a
+// long accumulation chain grows linearly with its length; the MMA warp therefore restarts
+// the accumulator every KC stages, alternating between two TMEM buffers, and the drain warps
+// add each finished chunk into FP32 registers with round-to-nearest while the next chunk runs.
+constexpr int TC_THREADS = 192;
+
+template <int BN, int STAGES, int KC>
 struct TcCfg {
     static constexpr int A_BYTES = TBM * TBK * 2;
     static constexpr int B_BYTES = BN * TBK * 2;
     static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
     static constexpr int BAR_BYTES = 256;
     static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 1024;
+    static constexpr uint32_t TMEM_COLS = 2 * BN;
     // instruction descriptor: FP32 accumulate, BF16 A and B, both K-major, M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                       ((uint32_t)(TBM >> 4) << 24);
 };
 
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int BN, int STAGES, int KC>
+__global__ void __launch_bounds__(TC_THREADS, 1)
     gett_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs g) {
-    using Cfg = TcCfg<BN, STAGES>;
+    using Cfg = TcCfg<BN, STAGES, KC>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *stages = smem;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * Cfg::STAGE_BYTES);
     uint64_t *empty = full + STAGES;
-    uint64_t *accf = empty + STAGES;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accf + 1);
+    uint64_t *cfull = empty + STAGES;    // [2] chunk accumulated in TMEM buffer
+    uint64_t *cempty = cfull + 2;        // [2] chunk drained, buffer reusable
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cempty + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     long long *coloff = reinterpret_cast<long long *>(smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long mt = blockIdx.x % g.mtiles, nt = blockIdx.x / g.mtiles;
     const int m0 = (int)(mt * TBM), n0 = (int)(nt * BN);
+    const int nk = g.kblocks;
+    const int nchunks = (nk + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accf, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&cfull[b], 1);
+            mbar_init(&cempty[b], 128);
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    if (warp == 0) {
-        tmem_alloc(tmem_slot, BN);
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, Cfg::TMEM_COLS);
         tmem_relinquish();
     }
     for (int c = threadIdx.x; c < BN; c += blockDim.x) {
@@ -191,70 +211,99 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int nk = g.kblocks;
 
-    if (warp == 0 && lane == 0) {
-        // TMA producer
-        for (int kb = 0; kb < nk; ++kb) {
-            const int s = kb % STAGES;
-            const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-            if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, g.flags)) {
-                *abort_flag = 1;
-                break;
+    if (warp == 0) {
+        if (lane == 0) {
+            // TMA producer
+            for (int kb = 0; kb < nk; ++kb) {
+                const int s = kb % STAGES;
+                const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+                if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, g.flags)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+                mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
+                tma_load_3d(st, &mapA, &full[s], kb * TBK, m0, 0);
+                tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kb * TBK, m0, 1);
+                tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kb * TBK, n0, 0);
+                tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kb * TBK, n0, 1);
             }
-            uint8_t *st = stages + s * Cfg::STAGE_BYTES;
-            mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
-            tma_load_3d(st, &mapA, &full[s], kb * TBK, m0, 0);
-            tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kb * TBK, m0, 1);
-            tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kb * TBK, n0, 0);
-            tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kb * TBK, n0, 1);
         }
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        for (int kb = 0; kb < nk; ++kb) {
-            const int s = kb % STAGES;
-            const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-            if (!mbar_wait(&full[s], ph, abort_flag, g.flags)) {
-                *abort_flag = 1;
-                break;
-            }
-            tc_fence_after();
-            uint8_t *st = stages + s * Cfg::STAGE_BYTES;
-            const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
-            const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
-            const uint64_t bl = sw128_desc(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES);
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer: chunk c accumulates stages [c*KC, c*KC+KC) into TMEM buffer c&1
+            for (int kb = 0; kb < nk; ++kb) {
+                const int chunk = kb / KC, buf = chunk & 1;
+                const bool first = (kb % KC) == 0;
+                if (first && chunk >= 2) {
+                    if (!mbar_wait(&cempty[buf], (uint32_t)((chunk >> 1) - 1) & 1u, abort_flag, g.flags)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                }
+                const int s = kb % STAGES;
+                const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+                if (!mbar_wait(&full[s], ph, abort_flag, g.flags)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+                const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
+                const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
+                const uint64_t bl = sw128_desc(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES);
+                const uint32_t d = tmem + (uint32_t)(buf * BN);
 #pragma unroll
-            for (int kk = 0; kk < TBK / 16; ++kk) {
-                const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
-                umma_bf16(tmem, ah + off, bh + off, Cfg::IDESC, (kb | kk) != 0 ? 1u : 0u);
-                umma_bf16(tmem, ah + off, bl + off, Cfg::IDESC, 1u);
-                umma_bf16(tmem, al + off, bh + off, Cfg::IDESC, 1u);
+                for (int kk = 0; kk < TBK / 16; ++kk) {
+                    const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
+                    umma_bf16(d, ah + off, bh + off, Cfg::IDESC, (first && kk == 0) ? 0u : 1u);
+                    umma_bf16(d, ah + off, bl + off, Cfg::IDESC, 1u);
+                    umma_bf16(d, al + off, bh + off, Cfg::IDESC, 1u);
+                }
+                umma_commit(&empty[s]);                       // stage s free once these complete
+                if ((kb % KC) == KC - 1 || kb == nk - 1) umma_commit(&cfull[buf]);   // chunk done
             }
-            umma_commit(&empty[s]);   // stage s is free once these MMAs complete
         }
-        umma_commit(accf);            // accumulator complete
-    }
-
-    // epilogue: warp w drains TMEM lanes [32w, 32w+32) = tile rows
-    const bool ok = mbar_wait(accf, 0u, abort_flag, g.flags);
-    __syncwarp();
-    tc_fence_after();
-    if (!ok || *abort_flag) {
-        if (lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
     } else {
-        const long long m = (long long)m0 + warp * 32 + lane;
-        const long long rowoff = m < g.M ? mode_off(g.mC, m) : -1;
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-            uint32_t r[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-            tmem_ld_wait();
-            if (rowoff >= 0) {
+        // drain warps 2-5: TMEM lane quarter (warp % 4), one tile row per thread
+        const int quarter = warp & 3;
+        float acc[BN];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const long long co = coloff[c0 + j];
+        for (int j = 0; j < BN; ++j) acc[j] = 0.f;
+        bool ok = true;
+        for (int c = 0; c < nchunks; ++c) {
+            const int buf = c & 1;
+            if (!mbar_wait(&cfull[buf], (uint32_t)(c >> 1) & 1u, abort_flag, g.flags)) {
+                ok = false;
+                *abort_flag = 1;
+                break;
+            }
+            __syncwarp();
+            tc_fence_after();
+#pragma unroll
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t r[32];
+                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + c0), r);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; ++j) acc[c0 + j] = __fadd_rn(acc[c0 + j], __uint_as_float(r[j]));
+            }
+            tc_fence_before();
+            mbar_arrive(&cempty[buf]);
+        }
+        if (!ok || *abort_flag) {
+            if (lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
+        } else {
+            const long long m = (long long)m0 + quarter * 32 + lane;
+            if (m < g.M) {
+                const long long rowoff = mode_off(g.mC, m);
+#pragma unroll
+                for (int j = 0; j < BN; ++j) {
+                    const long long co = coloff[j];
                     if (co >= 0) {
-                        double val = g.alpha * (double)__uint_as_float(r[j]);
+                        double val = g.alpha * (double)acc[j];
                         if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
                         g.C[rowoff + co] = val;
                     }
@@ -264,9 +313,9 @@ __global__ void __launch_bounds__(128, 1)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, BN);
+        tmem_dealloc(tmem, Cfg::TMEM_COLS);
     }
 }
 
@@ -410,18 +459,20 @@ static const __nv_bfloat16 *pack_operand(Ctx *ctx, int slot, const double *src, 
     return dst;
 }
 
+constexpr int TC_KC = 4;   // stages per accumulation chunk (K = 256)
+
 template <int BN, int STAGES>
 static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
                       const char *name) {
-    using Cfg = TcCfg<BN, STAGES>;
+    using Cfg = TcCfg<BN, STAGES, TC_KC>;
     static bool attr_set = false;
     if (!attr_set) {
-        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             Cfg::SMEM));
+        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES, TC_KC>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
         attr_set = true;
     }
     Ctx::Scope s(ctx, name);
-    gett_tc_kernel<BN, STAGES><<<(unsigned)tiles, 128, Cfg::SMEM, ctx->stream>>>(ma, mb, t);
+    gett_tc_kernel<BN, STAGES, TC_KC><<<(unsigned)tiles, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, t);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -433,7 +484,7 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     // grids (rows pad to 128, columns to the chosen BN).
     auto pad_cost = [](long long M, long long N, bool unit_rows) {
         long long best = -1;
-        for (int cand : {256, 128, 64}) {
+        for (int cand : {128, 64}) {
             long long p = roundup(N, cand);
             if (best < 0 || p < best) best = p;
         }
@@ -455,10 +506,10 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
         return;
     }
     // tile width: smallest padded N, preferring wider tiles on ties
-    int BN = 256;
+    int BN = 128;
     {
         long long best = -1;
-        for (int cand : {256, 128, 64}) {
+        for (int cand : {128, 64}) {
             long long p = roundup(a.N, cand);
             if (best < 0 || p < best) { best = p; BN = cand; }
         }
@@ -484,9 +535,7 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     t.flags = ctx->d_flags;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
-    if (BN == 256)
-        launch_tc<256, 2>(ctx, ma, mb, t, tiles, name);
-    else if (BN == 128)
+    if (BN == 128)
         launch_tc<128, 3>(ctx, ma, mb, t, tiles, name);
     else
         launch_tc<64, 4>(ctx, ma, mb, t, tiles, name);

@@ -1,0 +1,151 @@
+"""
+    JuESGPU
+
+Julia binding of libjuesgpu.so: GB300 implementations of the JuES hot path behind the same
+`Wfn`-taking entry points.  `JuESGPU.get_eri`, `tei_transform`, `do_rmp2`, `do_rccd` and
+`do_rccsd` take and return what `JuES.IntegralTransformation.get_eri`,
+`JuES.Transformation.tei_transform`, `JuES.MollerPlesset.do_rmp2`,
+`JuES.CoupledCluster.{mRCCD,RCCD}.do_rccd` and `JuES.CoupledCluster.{RCCSD,mRCCSD}.do_rccsd`
+do.  Arrays are passed as they are (Julia is column-major, as is the library); `Wfn{Float32}`
+is promoted to Float64.  Non-zero status codes become `error(...)` with the library message.
+
+Set `ENV["JUESGPU_LIB"]` to the path of libjuesgpu.so (default: ../lib/libjuesgpu.so).
+"""
+module JuESGPU
+
+using JuES.Wavefunction
+
+const LIB = get(ENV, "JUESGPU_LIB", joinpath(@__DIR__, "..", "lib", "libjuesgpu.so"))
+const PREC = Dict(:fp64 => Cint(0), :split_bf16 => Cint(1))
+const GUESS = Dict(:zero => Cint(0), :mp2 => Cint(1), :ovov => Cint(2))
+const ENOTCONV = 4
+
+struct CCOpts
+    maxit::Cint
+    e_conv::Cdouble
+    r_conv::Cdouble
+    diis::Cint
+    diis_size::Cint
+    precision::Cint
+    guess::Cint
+    refine::Cint
+end
+
+struct IterLog
+    iter::Cint
+    precision::Cint
+    energy::Cdouble
+    rnorm::Cdouble
+    ms::Cdouble
+end
+
+function lasterror()
+    buf = Vector{UInt8}(undef, 4096)
+    ccall((:jues_last_error, LIB), Cint, (Ptr{UInt8}, Csize_t), buf, length(buf))
+    return unsafe_string(pointer(buf))
+end
+
+check(st) = st == 0 ? nothing : error("libjuesgpu: " * lasterror())
+
+const CTX = Ref{Ptr{Cvoid}}(C_NULL)
+function ctx(device::Integer = 0)
+    if CTX[] == C_NULL
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:jues_ctx_create, LIB), Cint, (Cint, Ref{Ptr{Cvoid}}), device, r))
+        CTX[] = r[]
+    end
+    return CTX[]
+end
+
+f64(x) = convert(Array{Float64}, x)
+
+"tei_transform(gao, C1, C2, C3, C4, name) -- Transformation.jl:39-93"
+function tei_transform(gao::AbstractArray{<:Real,4}, C1, C2, C3, C4, name::String = "default";
+                       precision::Symbol = :fp64)
+    g = f64(gao); c1, c2, c3, c4 = f64(C1), f64(C2), f64(C3), f64(C4)
+    n = size(g, 1)
+    out = Array{Float64}(undef, size(c1, 2), size(c2, 2), size(c3, 2), size(c4, 2))
+    check(ccall((:jues_tei_transform, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                 Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Cint, Ptr{Cdouble}),
+                ctx(), g, n, c1, size(c1, 2), c2, size(c2, 2), c3, size(c3, 2), c4, size(c4, 2),
+                PREC[precision], out))
+    return out
+end
+tei_transform(gao::AbstractArray{<:Real,4}, C::AbstractMatrix, name::String = "default"; kw...) =
+    tei_transform(gao, C, C, C, C, name; kw...)
+
+"get_eri(wfn, spec; notation, fcn) -- IntegralTransformation.jl:38-101"
+function get_eri(wfn::Wfn, eri_string::String; notation::String = "phys", fcn::Int = 0,
+                 precision::Symbol = :fp64)
+    sizeof(eri_string) == 4 || error("Invalid string given to JuES.IntegralTransformation.get_eri: $eri_string")
+    s = notation == "phys" ? eri_string[[1, 3, 2, 4]] : eri_string
+    d = [c in ('o', 'O') ? wfn.nalpha - fcn : wfn.nvira for c in s]
+    shape = notation == "phys" ? (d[1], d[3], d[2], d[4]) : Tuple(d)
+    out = Array{Float64}(undef, shape...)
+    Co, Cv = f64(wfn.Cao), f64(wfn.Cav)
+    check(ccall((:jues_get_eri, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Cstring,
+                 Cint, Cint, Cint, Ptr{Cdouble}),
+                ctx(), f64(wfn.ao_eri), size(Co, 1), Co, size(Co, 2), Cv, size(Cv, 2), eri_string,
+                notation == "phys" ? 1 : 0, fcn, PREC[precision], out))
+    return out
+end
+
+"do_rmp2(refWfn) -- RMP2.jl:11-45"
+function do_rmp2(refWfn::Wfn; precision::Symbol = :fp64, kwargs...)
+    e = Ref{Cdouble}(0.0)
+    Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
+    check(ccall((:jues_rmp2, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                 Ptr{Cdouble}, Cint, Ref{Cdouble}, Ptr{Cdouble}),
+                ctx(), f64(refWfn.ao_eri), size(Co, 1), Co, size(Co, 2), Cv, size(Cv, 2),
+                f64(refWfn.epsa), PREC[precision], e, C_NULL))
+    return e[]
+end
+
+function cc_solve(method, refWfn; maxit, r_conv, e_conv, diis, diis_size, precision, guess, refine)
+    Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
+    o, v = size(Co, 2), size(Cv, 2)
+    opts = Ref(CCOpts(maxit, e_conv, r_conv, diis, diis_size, PREC[precision], GUESS[guess], refine))
+    e = Ref{Cdouble}(0.0)
+    nit = Ref{Cint}(0)
+    T2 = Array{Float64}(undef, o, o, v, v)
+    t1 = Array{Float64}(undef, o, v)
+    log = Vector{IterLog}(undef, max(1, maxit))
+    if method == 0
+        st = ccall((:jues_rccd, LIB), Cint,
+                   (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                    Ptr{Cdouble}, Ref{CCOpts}, Ref{Cdouble}, Ptr{Cdouble}, Ptr{IterLog}, Cint, Ref{Cint}),
+                   ctx(), f64(refWfn.ao_eri), size(Co, 1), Co, o, Cv, v, f64(refWfn.epsa), opts, e,
+                   T2, log, length(log), nit)
+    else
+        st = ccall((:jues_rccsd, LIB), Cint,
+                   (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                    Ptr{Cdouble}, Ref{CCOpts}, Ref{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+                    Ptr{IterLog}, Cint, Ref{Cint}),
+                   ctx(), f64(refWfn.ao_eri), size(Co, 1), Co, o, Cv, v, f64(refWfn.epsa), opts, e,
+                   t1, T2, log, length(log), nit)
+    end
+    st == ENOTCONV ? @warn(lasterror()) : check(st)   # mRCCD.jl stops silently at maxit
+    return e[], t1, T2, log[1:nit[]]
+end
+
+"mRCCD.do_rccd(refWfn; maxit=40, doprint=false, return_T2=false) -- mRCCD.jl:38-118"
+function do_rccd(refWfn::Wfn; maxit = 40, doprint = false, return_T2 = false, precision = :fp64,
+                 guess = :zero, r_conv = 1e-7, e_conv = 0.0, diis = true, diis_size = 6, refine = 2)
+    E, _, T2, log = cc_solve(0, refWfn; maxit, r_conv, e_conv, diis = Cint(diis), diis_size,
+                             precision, guess, refine)
+    doprint && foreach(r -> println("@CCD ", r.energy), log)
+    return return_T2 ? (E, T2) : E
+end
+
+"RCCSD.do_rccsd(refWfn; maxit=40, return_T=false) -- RCCSD.jl:33-116"
+function do_rccsd(refWfn::Wfn; maxit = 40, return_T = false, precision = :fp64, diis = false,
+                  r_conv = 0.0, e_conv = 0.0, diis_size = 6, refine = 0, kwargs...)
+    E, t1, T2, _ = cc_solve(1, refWfn; maxit, r_conv, e_conv, diis = Cint(diis), diis_size,
+                            precision, guess = :mp2, refine)
+    return return_T ? (E, T2) : E
+end
+
+end # module
