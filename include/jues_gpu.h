@@ -125,6 +125,17 @@ JUES_API int jues_rmp2(jues_ctx *ctx, const double *gao, int n,
               const double *Cocc, int o, const double *Cvir, int v,
               const double *eps, int precision, double *e_out, double *k_out);
 
+/* MP2 adjoint (no reference counterpart; the differentiation form): E as jues_rmp2 from the
+ * full n x n MO matrix C (occupied columns first) and, scaled by e_bar,
+ *   gao_bar[mu,nu,lam,sig] = dE/d(mu nu|lam sig)  (n^4, may be NULL)
+ *   C_bar[mu,p]            = dE/dC[mu,p]          (n x n, may be NULL)
+ * by back-transforming Gamma_iajb = 2(2K_iajb - K_ibja)/D.  The three-quarter transformed
+ * integrals that C_bar needs are recomputed, not stored.  C_bar assumes 8-fold symmetric
+ * AO integrals (real orbitals), as every ERI tensor has. */
+JUES_API int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, int o,
+                               const double *eps, int precision, double e_bar, double *e_out,
+                               double *gao_bar, double *C_bar);
+
 /* ---- coupled cluster ------------------------------------------------------------------
  * Whole solves.  t2_out (o*o*v*v, [i,j,a,b]) and t1_out (o*v, [i,a]) may be NULL; log may
  * be NULL, else it receives up to log_cap records.  Returns JUES_ENOTCONV (with e_out,

@@ -275,6 +275,78 @@ int jues_rmp2(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o
     });
 }
 
+int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, int o, const double *eps,
+                      int precision, double e_bar, double *e_out, double *gao_bar, double *C_bar) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(gao, "gao"); need(C, "C"); need(eps, "eps"); need(e_out, "e_out");
+        const int v = n - o;
+        check_dims(n, o, v);
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cudaSetDevice(c.device);
+        DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
+        DBuf<double> dC = h2d(c, C, (size_t)n * n);
+        DBuf<double> de = h2d(c, eps, (size_t)n);
+        const double *Co = dC.p, *Cv = dC.p + (size_t)n * o;
+        const long long ov = (long long)o * v;
+        const size_t nk = (size_t)(ov * ov);
+        // K = (ia|jb) in chemists' order
+        DBuf<double> K(&c, nk), G(&c, nk);
+        {
+            const double *Cs[4] = {Co, Cv, Co, Cv};
+            int d[4] = {o, v, o, v};
+            long long ostr[4] = {1, o, ov, ov * o};
+            transform4(&c, precision, g.p, n, Cs, d, K.p, ostr, true);
+        }
+        *e_out = mp2_gamma(&c, K.p, de.p, o, v, e_bar, G.p);
+        K.reset();
+        if (gao_bar) {
+            const double *Cs[4] = {Co, Cv, Co, Cv};
+            int d[4] = {o, v, o, v};
+            DBuf<double> gb(&c, (size_t)n * n * n * n);
+            backtransform4(&c, precision, G.p, d, n, Cs, gb.p);
+            d2h(c, gao_bar, gb.p, gb.n);
+        }
+        if (C_bar) {
+            DBuf<double> cb(&c, (size_t)n * n);
+            {
+                // H[mu,a,j,b] = (mu a|j b); dE/dC[mu,i] = 2 sum_{ajb} H[mu,(ajb)] G[i,(ajb)]
+                const double *Cs[4] = {nullptr, Cv, Co, Cv};
+                int d[4] = {n, v, o, v};
+                long long ostr[4] = {1, n, (long long)n * v, (long long)n * v * o};
+                DBuf<double> H(&c, (size_t)n * v * o * v);
+                transform4(&c, precision, g.p, n, Cs, d, H.p, ostr, true);
+                GettArgs a;
+                a.M = n; a.N = o; a.K = ov * v;
+                a.alpha = 2.0; a.beta = 0.0;
+                a.A = H.p; a.mA = plain(1); a.kA = plain(n);
+                a.B = G.p; a.kB = plain(o); a.nB = plain(1);
+                a.C = cb.p; a.mC = plain(1); a.nC = plain(n);
+                gett(&c, precision, a, "adjoint_cocc");
+            }
+            {
+                // H'[i,nu,j,b] = (i nu|j b); dE/dC[nu,a] = 2 sum_{ijb} H'[i,nu,j,b] G[i,a,j,b]
+                const double *Cs[4] = {Co, nullptr, Co, Cv};
+                int d[4] = {o, n, o, v};
+                long long ostr[4] = {1, o, (long long)o * n, (long long)o * n * o};
+                DBuf<double> H(&c, (size_t)o * n * o * v);
+                transform4(&c, precision, g.p, n, Cs, d, H.p, ostr, true);
+                GettArgs a;
+                a.M = n; a.N = v; a.K = (long long)o * o * v;
+                a.alpha = 2.0; a.beta = 0.0;
+                a.A = H.p; a.mA = plain(o); a.kA = mode3(o, o, 1, (long long)o * n, (long long)o * n * o);
+                a.B = G.p; a.kB = mode3(o, o, 1, ov, ov * o); a.nB = plain(o);
+                a.C = cb.p + (size_t)n * o; a.mC = plain(1); a.nC = plain(n);
+                gett(&c, precision, a, "adjoint_cvir");
+            }
+            d2h(c, C_bar, cb.p, cb.n);
+        }
+        pack_cache_drop(&c, g.p);
+        c.check_flags();
+    });
+}
+
 int jues_cc_default_opts(jues_cc_opts *opts) {
     return guarded([&] {
         need(opts, "opts");

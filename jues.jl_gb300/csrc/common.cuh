@@ -173,6 +173,8 @@ void axpby(Ctx *ctx, size_t n, double a, const double *x, double b, const double
 double dot(Ctx *ctx, size_t n, const double *x, const double *y);
 // MP2: sum K[i,j,a,b](2K[i,j,a,b]-K[i,j,b,a]) / D (K column-major [i,j,a,b])
 double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v);
+// MP2 adjoint seed: G[i,a,j,b] = 2 e_bar (2K[i,a,j,b] - K[i,b,j,a]) / D from chemists' K; returns E
+double mp2_gamma(Ctx *ctx, const double *K, const double *eps, int o, int v, double e_bar, double *G);
 // CC energy: sum oovv[i,j,a,b] (2 X[i,j,a,b] - X[j,i,a,b]) with X = T2 (+ t1 t1 when t1)
 double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t1, int o, int v);
 // T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a]) / D ; returns ||Tn - Told||^2

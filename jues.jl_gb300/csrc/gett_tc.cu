@@ -1,22 +1,26 @@
 // Split-precision GEMM over tensor modes on the sm_103a tensor cores (tcgen05 + TMEM + TMA).
 //
-// Each FP64 operand x is written as two BF16 planes, hi = bf16(x) and lo = bf16(x - hi)
-// (|x - hi - lo| <= 2^-16 |x|), K-major and zero-padded to the tile grid.  One CTA computes a
-// 128 x BN tile of C = A.B^T as three tcgen05.mma products per K-step,
-//     A_hi.B_hi + A_hi.B_lo + A_lo.B_hi,
-// accumulated in FP32 in tensor memory; the dropped A_lo.B_lo term is O(2^-16).  Operand tiles
-// arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by mbarriers;
-// one thread issues the TMA loads, one thread issues the MMAs into two alternating TMEM
-// accumulators (one per chunk of KC stages), and four warps add finished chunks into FP32
-// registers with round-to-nearest, then apply alpha/beta in FP64 and scatter through the
-// output tensor modes.
-// Every mbarrier wait is bounded by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips
-// its stores, frees its TMEM and returns.
+// Each FP64 operand row r (a row of A or of B, running over K) gets a power-of-two scale 2^e_r
+// with max_k |x_rk| < 2^e_r, and every element is written as two small integers carried in BF16,
+//     x = 2^(e_r - 7) (hi + 2^-8 lo),   hi = rint(x 2^(7 - e_r)),  |hi|, |lo| <= 128,
+// so |x - 2^(e_r-7)(hi + 2^-8 lo)| <= 2^(e_r-16).  One CTA computes a 128 x BN tile of
+// C = A.B^T with three tcgen05.mma products per K=16 step: hi.hi into a "main" TMEM accumulator
+// and hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-16), is dropped).  Because the
+// BF16 values are integers, every product and every partial sum of a chunk of KC stages
+// (< 2^23) is an exact FP32 integer: the tensor core's truncating accumulation never rounds.
+// Chunks alternate between two TMEM buffers; four warps add finished chunks into FP32
+// registers (round-to-nearest, unbiased) while the next chunk runs, then rescale by
+// 2^(e_r + e_c - 14) and apply alpha/beta in FP64 through the output tensor modes.  Operand
+// tiles arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by
+// mbarriers; one thread issues the TMA loads and one the MMAs.  Every mbarrier wait is bounded
+// by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips its stores, frees its TMEM and
+// returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <vector>
 
@@ -120,6 +124,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
           "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
 }
+// 32 lanes x 16 consecutive 32-bit TMEM columns -> 16 registers per thread
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // UMMA shared-memory descriptor of a K-major tile written by TMA with 128-byte swizzle:
@@ -134,6 +148,7 @@ struct TcArgs {
     long long M, N;        // logical GEMM extent (rows of A, rows of B)
     int kblocks;           // padded K / TBK
     long long mtiles;
+    const int *expA, *expB;   // per-row power-of-two scales of the packed operands
     double alpha, beta;
     double *C;
     const double *Cin;
@@ -142,10 +157,9 @@ struct TcArgs {
 };
 
 // Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-5 drain TMEM.
-// The tensor core adds each MMA into its FP32 accumulator with truncation, so the error of a
-// long accumulation chain grows linearly with its length; the MMA warp therefore restarts
-// the accumulator every KC stages, alternating between two TMEM buffers, and the drain warps
-// add each finished chunk into FP32 registers with round-to-nearest while the next chunk runs.
+// The MMA warp restarts both accumulators every KC stages (KC * 64 K values keeps every
+// partial sum below 2^23), alternating between two TMEM buffers, and the drain warps add each
+// finished chunk into FP32 registers with round-to-nearest while the next chunk runs.
 constexpr int TC_THREADS = 192;
 
 template <int BN, int STAGES, int KC>
@@ -154,8 +168,8 @@ struct TcCfg {
     static constexpr int B_BYTES = BN * TBK * 2;
     static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
     static constexpr int BAR_BYTES = 256;
-    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 1024;
-    static constexpr uint32_t TMEM_COLS = 2 * BN;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 16 + 1024;
+    static constexpr uint32_t TMEM_COLS = 4 * BN;   // 2 buffers x (main, correction)
     // instruction descriptor: FP32 accumulate, BF16 A and B, both K-major, M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                       ((uint32_t)(TBM >> 4) << 24);
@@ -179,6 +193,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cempty + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     long long *coloff = reinterpret_cast<long long *>(smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES);
+    double *colscale = reinterpret_cast<double *>(coloff + BN);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long mt = blockIdx.x % g.mtiles, nt = blockIdx.x / g.mtiles;
@@ -206,6 +221,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int c = threadIdx.x; c < BN; c += blockDim.x) {
         const long long n = (long long)n0 + c;
         coloff[c] = n < g.N ? mode_off(g.nC, n) : -1;
+        const int eb = n < g.N ? g.expB[n] : INT_MIN;
+        colscale[c] = eb == INT_MIN ? 0.0 : scalbn(1.0, eb);   // INT_MIN: all-zero row
     }
     tc_fence_before();
     __syncthreads();
@@ -254,13 +271,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
                 const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
                 const uint64_t bl = sw128_desc(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES);
-                const uint32_t d = tmem + (uint32_t)(buf * BN);
+                const uint32_t dmain = tmem + (uint32_t)(buf * 2 * BN);
+                const uint32_t dcorr = dmain + (uint32_t)BN;
 #pragma unroll
                 for (int kk = 0; kk < TBK / 16; ++kk) {
                     const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
-                    umma_bf16(d, ah + off, bh + off, Cfg::IDESC, (first && kk == 0) ? 0u : 1u);
-                    umma_bf16(d, ah + off, bl + off, Cfg::IDESC, 1u);
-                    umma_bf16(d, al + off, bh + off, Cfg::IDESC, 1u);
+                    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+                    umma_bf16(dmain, ah + off, bh + off, Cfg::IDESC, acc);
+                    umma_bf16(dcorr, ah + off, bl + off, Cfg::IDESC, acc);
+                    umma_bf16(dcorr, al + off, bh + off, Cfg::IDESC, 1u);
                 }
                 umma_commit(&empty[s]);                       // stage s free once these complete
                 if ((kb % KC) == KC - 1 || kb == nk - 1) umma_commit(&cfull[buf]);   // chunk done
@@ -283,12 +302,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             tc_fence_after();
 #pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                uint32_t r[32];
-                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + c0), r);
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                uint32_t rm[16], rc[16];
+                const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 2 * BN + c0);
+                tmem_ld16(base, rm);
+                tmem_ld16(base + (uint32_t)BN, rc);
                 tmem_ld_wait();
 #pragma unroll
-                for (int j = 0; j < 32; ++j) acc[c0 + j] = __fadd_rn(acc[c0 + j], __uint_as_float(r[j]));
+                for (int j = 0; j < 16; ++j)
+                    acc[c0 + j] = __fadd_rn(acc[c0 + j],
+                                            __fmaf_rn(__uint_as_float(rc[j]), 0.00390625f, __uint_as_float(rm[j])));
             }
             tc_fence_before();
             mbar_arrive(&cempty[buf]);
@@ -299,11 +322,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const long long m = (long long)m0 + quarter * 32 + lane;
             if (m < g.M) {
                 const long long rowoff = mode_off(g.mC, m);
+                const int ea = g.expA[m];
+                const double rs = ea == INT_MIN ? 0.0 : g.alpha * scalbn(1.0, ea - 14);
 #pragma unroll
                 for (int j = 0; j < BN; ++j) {
                     const long long co = coloff[j];
                     if (co >= 0) {
-                        double val = g.alpha * (double)acc[j];
+                        double val = rs * colscale[j] * (double)acc[j];
                         if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
                         g.C[rowoff + co] = val;
                     }
@@ -319,11 +344,50 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// FP64 operand (rows via rmode, K via kmode) -> BF16 hi/lo planes [2][Rpad][Kpad], K-major
+// Per-row power-of-two scale: rexp[r] = e with max_k |x_rk| < 2^e (INT_MIN for an all-zero row).
 constexpr int PR = 32, PK = 64;
+__global__ void __launch_bounds__(256) rowexp_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
+                                                     long long R, long long K, long long Kpad, int kfast,
+                                                     int *__restrict__ rexp) {
+    __shared__ long long roff[PR], koff[PK];
+    __shared__ int tmax[PR];
+    const long long kblocks = Kpad / PK;
+    const long long r0 = (blockIdx.x / kblocks) * PR;
+    const long long k0 = (blockIdx.x % kblocks) * PK;
+    const int tid = threadIdx.x;
+    if (tid < PR) {
+        const long long r = r0 + tid;
+        roff[tid] = r < R ? mode_off(rmode, r) : -1;
+        tmax[tid] = INT_MIN;
+    } else if (tid >= 64 && tid < 64 + PK) {
+        const long long k = k0 + tid - 64;
+        koff[tid - 64] = k < K ? mode_off(kmode, k) : -1;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < (PR * PK) / 256; ++i) {
+        const int e = tid + i * 256;
+        const int kk = kfast ? (e % PK) : (e / PR);
+        const int rr = kfast ? (e / PK) : (e % PR);
+        const long long a = roff[rr], b = koff[kk];
+        if (a >= 0 && b >= 0) {
+            const double x = __ldg(src + a + b);
+            if (x != 0.0) {
+                int ex;
+                frexp(x, &ex);   // |x| < 2^ex
+                atomicMax(&tmax[rr], ex);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid < PR && r0 + tid < R && tmax[tid] != INT_MIN) atomicMax(&rexp[r0 + tid], tmax[tid]);
+}
+
+// FP64 operand -> integer-valued BF16 planes [2][Rpad][Kpad], K-major:
+// hi = rint(x 2^(7-e_r)), lo = rint((x 2^(7-e_r) - hi) 2^8)
 __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
-                                                         long long Kpad, int kfast,
+                                                         long long Kpad, int kfast, const int *__restrict__ rexp,
                                                          __nv_bfloat16 *__restrict__ dst) {
     __shared__ double tile[PR][PK + 1];
     __shared__ long long roff[PR], koff[PK];
@@ -350,17 +414,28 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
     __syncthreads();
     // each thread writes 8 consecutive K values of one row to both planes (16-byte stores)
     const int rr = tid >> 3, kc = (tid & 7) * 8;
+    const long long r = r0 + rr;
+    const int ex = (r < R) ? rexp[r] : INT_MIN;
     __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-        const double x = tile[rr][kc + j];
-        const __nv_bfloat16 h = __double2bfloat16(x);
-        hi[j] = h;
-        lo[j] = __double2bfloat16(x - (double)__bfloat162float(h));
+        double h = 0.0, l = 0.0;
+        if (ex != INT_MIN) {
+            const double y = scalbn(tile[rr][kc + j], 7 - ex);   // |y| < 128, exact scaling
+            h = rint(y);
+            l = rint((y - h) * 256.0);
+        }
+        hi[j] = __double2bfloat16(h);   // integers of magnitude <= 128: exact in BF16
+        lo[j] = __double2bfloat16(l);
     }
-    const size_t base = (size_t)(r0 + rr) * (size_t)Kpad + (size_t)(k0 + kc);
+    const size_t base = (size_t)r * (size_t)Kpad + (size_t)(k0 + kc);
     *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
     *reinterpret_cast<uint4 *>(dst + (size_t)Rpad * Kpad + base) = *reinterpret_cast<const uint4 *>(lo);
+}
+
+__global__ void fill_int_kernel(int *p, long long n, int v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -407,10 +482,16 @@ struct PackEntry {
     Mode r, k;
     long long R, K, Rpad, Kpad;
     DBuf<__nv_bfloat16> buf;
+    DBuf<int> exps;
 };
 struct PackCache {
     std::vector<std::unique_ptr<PackEntry>> cached;
     DBuf<__nv_bfloat16> scratch[2];
+    DBuf<int> scratch_exp[2];
+};
+struct Packed {
+    const __nv_bfloat16 *planes;
+    const int *exps;
 };
 
 void pack_cache_destroy(PackCache *p) { delete p; }
@@ -424,39 +505,52 @@ void pack_cache_drop(Ctx *ctx, const void *ptr) {
             v.end());
 }
 
-static const __nv_bfloat16 *pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm, const Mode &km,
-                                         long long R, long long K, long long Rpad, long long Kpad, bool cache) {
+static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm, const Mode &km, long long R,
+                           long long K, long long Rpad, long long Kpad, bool cache) {
     if (!ctx->pack) ctx->pack = new PackCache();
     PackCache &pc = *ctx->pack;
     if (cache) {
         for (auto &e : pc.cached)
             if (e->src == src && e->R == R && e->K == K && e->Rpad == Rpad && e->Kpad == Kpad &&
                 same_mode(e->r, rm) && same_mode(e->k, km))
-                return e->buf.p;
+                return Packed{e->buf.p, e->exps.p};
     }
     const size_t need = (size_t)2 * Rpad * Kpad;
     __nv_bfloat16 *dst;
+    int *ex;
     std::unique_ptr<PackEntry> ent;
     if (cache) {
-        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__nv_bfloat16>(ctx, need)});
+        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__nv_bfloat16>(ctx, need),
+                                DBuf<int>(ctx, (size_t)Rpad)});
         dst = ent->buf.p;
+        ex = ent->exps.p;
     } else {
         if (pc.scratch[slot].n < need) {
             pc.scratch[slot].reset();
             pc.scratch[slot] = DBuf<__nv_bfloat16>(ctx, need);
         }
+        if (pc.scratch_exp[slot].n < (size_t)Rpad) {
+            pc.scratch_exp[slot].reset();
+            pc.scratch_exp[slot] = DBuf<int>(ctx, (size_t)Rpad);
+        }
         dst = pc.scratch[slot].p;
+        ex = pc.scratch_exp[slot].p;
     }
     const long long blocks = (Rpad / PR) * (Kpad / PK);
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     {
         Ctx::Scope s(ctx, "pack_split");
-        pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, dst);
+        fill_int_kernel<<<(unsigned)std::min<long long>((Rpad + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+            ex, Rpad, INT_MIN);
+        rowexp_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Kpad, kfast, ex);
+        pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
+                                                                     dst);
         JUES_CHECK_CUDA(cudaGetLastError());
+        ctx->launches += 2;
     }
     if (cache) pc.cached.push_back(std::move(ent));
-    return dst;
+    return Packed{dst, ex};
 }
 
 constexpr int TC_KC = 4;   // stages per accumulation chunk (K = 256)
@@ -517,10 +611,10 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     const long long Mpad = roundup(a.M, TBM), Npad = roundup(a.N, BN), Kpad = roundup(a.K, TBK);
     JUES_REQUIRE(Mpad < (1LL << 31) && Npad < (1LL << 31) && Kpad / TBK < (1LL << 30),
                  "GEMM extent exceeds the TMA coordinate range");
-    const __nv_bfloat16 *pa = pack_operand(ctx, 0, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, a.a_const);
-    const __nv_bfloat16 *pb = pack_operand(ctx, 1, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, a.b_const);
-    const CUtensorMap ma = make_map(pa, Mpad, Kpad, TBM);
-    const CUtensorMap mb = make_map(pb, Npad, Kpad, BN);
+    const Packed pa = pack_operand(ctx, 0, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, a.a_const);
+    const Packed pb = pack_operand(ctx, 1, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, a.b_const);
+    const CUtensorMap ma = make_map(pa.planes, Mpad, Kpad, TBM);
+    const CUtensorMap mb = make_map(pb.planes, Npad, Kpad, BN);
     TcArgs t;
     t.M = a.M;
     t.N = a.N;
@@ -533,6 +627,8 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     t.mC = a.mC;
     t.nC = a.nC;
     t.flags = ctx->d_flags;
+    t.expA = pa.exps;
+    t.expB = pb.exps;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
     if (BN == 128)

@@ -222,6 +222,37 @@ __global__ void t1_finalize_kernel(double *__restrict__ t1n, const double *__res
     if (threadIdx.x == 0) part[0] = acc;
 }
 
+// MP2 adjoint seed from chemists' K[i,a,j,b]: Gamma = 2 e_bar (2K_iajb - K_ibja)/D and the energy
+__global__ void mp2_gamma_kernel(const double *__restrict__ K, const double *__restrict__ eps, int o, int v,
+                                 double e_bar, double *__restrict__ G, double *part) {
+    const long long ov = (long long)o * v, oo = (long long)o * o;
+    const long long npair = (long long)v * (v + 1) / 2;
+    double acc = 0.0;
+    for (long long p = blockIdx.x; p < npair; p += gridDim.x) {
+        int a, b;
+        pair_ab(p, a, b);
+        const double ea = eps[o + a], eb = eps[o + b];
+        for (long long ij = threadIdx.x; ij < oo; ij += blockDim.x) {
+            const int i = (int)(ij % o), j = (int)(ij / o);
+            const long long x_off = i + (long long)o * a + ov * j + ov * o * b;   // K[i,a,j,b]
+            const long long y_off = i + (long long)o * b + ov * j + ov * o * a;   // K[i,b,j,a]
+            const double inv = 1.0 / (eps[i] + eps[j] - ea - eb);
+            const double x = K[x_off];
+            if (a == b) {
+                acc = fma(x * x, inv, acc);
+                G[x_off] = 2.0 * e_bar * x * inv;
+            } else {
+                const double y = K[y_off];
+                acc = fma(x * (2.0 * x - y) + y * (2.0 * y - x), inv, acc);
+                G[x_off] = 2.0 * e_bar * (2.0 * x - y) * inv;
+                G[y_off] = 2.0 * e_bar * (2.0 * y - x) * inv;
+            }
+        }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
 unsigned grid_for(long long n, int threads = 256) {
     long long b = (n + threads - 1) / threads;
     if (b > 152LL * 32) b = 152LL * 32;
@@ -294,6 +325,17 @@ double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v) {
     {
         Ctx::Scope s(ctx, "mp2_energy");
         mp2_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(K, eps, o, v, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    return finish_reduce(ctx, nb);
+}
+
+double mp2_gamma(Ctx *ctx, const double *K, const double *eps, int o, int v, double e_bar, double *G) {
+    long long npair = (long long)v * (v + 1) / 2;
+    int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
+    {
+        Ctx::Scope s(ctx, "mp2_gamma");
+        mp2_gamma_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(K, eps, o, v, e_bar, G, ctx->d_red);
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     return finish_reduce(ctx, nb);

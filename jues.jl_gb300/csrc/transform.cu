@@ -25,16 +25,25 @@ double transform4_flops(int n, const int d[4]) {
     return f;
 }
 
-void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const C[4], const int d[4],
+void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const C[4], const int d_in[4],
                 double *out, const long long ostr[4], bool g_const) {
-    for (int p = 0; p < 4; ++p) JUES_REQUIRE(d[p] >= 0, "negative MO dimension");
+    // a null C[p] keeps AO index p (three-quarter transforms for the MP2 adjoint)
+    int d[4];
+    for (int p = 0; p < 4; ++p) {
+        d[p] = C[p] ? d_in[p] : n;
+        JUES_REQUIRE(d[p] >= 0, "negative MO dimension");
+    }
     if (d[0] == 0 || d[1] == 0 || d[2] == 0 || d[3] == 0) return;
+    int nsteps = 0;
+    for (int p = 0; p < 4; ++p) nsteps += C[p] ? 1 : 0;
+    JUES_REQUIRE(nsteps > 0, "transform4 needs at least one coefficient matrix");
     long long dims[4] = {n, n, n, n};
-    bool done[4] = {false, false, false, false};
+    bool done[4];
+    for (int p = 0; p < 4; ++p) done[p] = !C[p];
     const double *cur = g;
     DBuf<double> bufs[2];
     int which = 0;
-    for (int step = 0; step < 4; ++step) {
+    for (int step = 0; step < nsteps; ++step) {
         int p = -1;
         for (int q = 0; q < 4; ++q)
             if (!done[q] && (p < 0 || d[q] < d[p])) p = q;
@@ -44,7 +53,7 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
         for (int q = 0; q < 4; ++q) nd[q] = dims[q];
         nd[p] = d[p];
         double *dst;
-        if (step == 3) {
+        if (step == nsteps - 1) {
             for (int q = 0; q < 4; ++q) sY[q] = ostr[q];
             dst = out;
         } else {
@@ -81,7 +90,62 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
         done[p] = true;
         cur = dst;
         which ^= 1;
-        // the buffer two steps back is now free for reuse
+    }
+}
+
+void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, const double *const C[4],
+                    double *out) {
+    // out[mu,nu,lam,sig] = sum X[i,a,j,b] C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b]; the last step
+    // costs 2 n^4 d_last, so the largest MO dimension is expanded first
+    long long dims[4] = {d[0], d[1], d[2], d[3]};
+    bool done[4] = {false, false, false, false};
+    const double *cur = X;
+    DBuf<double> bufs[2];
+    int which = 0;
+    for (int step = 0; step < 4; ++step) {
+        int p = -1;
+        for (int q = 0; q < 4; ++q)
+            if (!done[q] && (p < 0 || d[q] > d[p])) p = q;
+        long long sX[4], nd[4], sY[4];
+        sX[0] = 1;
+        for (int q = 1; q < 4; ++q) sX[q] = sX[q - 1] * dims[q - 1];
+        for (int q = 0; q < 4; ++q) nd[q] = dims[q];
+        nd[p] = n;
+        sY[0] = 1;
+        for (int q = 1; q < 4; ++q) sY[q] = sY[q - 1] * nd[q - 1];
+        double *dst;
+        if (step == 3) {
+            dst = out;
+        } else {
+            size_t cnt = (size_t)(nd[0] * nd[1] * nd[2] * nd[3]);
+            if (bufs[which].n < cnt) bufs[which] = DBuf<double>(ctx, cnt);
+            dst = bufs[which].p;
+        }
+        int q1 = -1, q2 = -1, q3 = -1;
+        for (int q = 0; q < 4; ++q) {
+            if (q == p) continue;
+            if (q1 < 0) q1 = q; else if (q2 < 0) q2 = q; else q3 = q;
+        }
+        GettArgs a;
+        a.M = dims[q1] * dims[q2] * dims[q3];
+        a.N = n;
+        a.K = d[p];
+        a.alpha = 1.0;
+        a.beta = 0.0;
+        a.A = cur;
+        a.mA = mode3(dims[q1], dims[q2], sX[q1], sX[q2], sX[q3]);
+        a.kA = plain(sX[p]);
+        a.B = C[p];            // B[k=d, n=mu] = C[mu, d]
+        a.kB = plain(n);
+        a.nB = plain(1);
+        a.C = dst;
+        a.mC = mode3(nd[q1], nd[q2], sY[q1], sY[q2], sY[q3]);
+        a.nC = plain(sY[p]);
+        gett(ctx, prec, a, "backtransform");
+        for (int q = 0; q < 4; ++q) dims[q] = nd[q];
+        done[p] = true;
+        cur = dst;
+        which ^= 1;
     }
 }
 

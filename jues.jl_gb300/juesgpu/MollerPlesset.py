@@ -1,5 +1,8 @@
 """Mirror of ``JuES.MollerPlesset.do_rmp2`` (src/MollerPlesset/RMP2.jl:11-45)."""
 import ctypes as C
+import ctypes as C_
+
+import numpy as np
 
 from . import _lib
 
@@ -19,3 +22,27 @@ def do_rmp2(refWfn, *, precision: str = "fp64", device: int = 0, doprint: bool =
     if doprint:
         print(f"   @RMP2 {e.value:>20.17f} Eh")
     return e.value
+
+
+def rmp2_adjoint(refWfn=None, *, gao=None, C=None, nocc=None, eps=None, e_bar: float = 1.0,
+                 want_gao: bool = True, want_C: bool = True, precision: str = "fp64", device: int = 0):
+    """(E, dE/dgao * e_bar, dE/dC * e_bar) of the closed-shell MP2 energy.
+
+    C is the full n x n MO matrix (occupied columns first).  The gradient with respect to
+    the AO integrals treats every element as independent; dE/dC assumes 8-fold symmetric
+    integrals.  Either pass a Wfn or gao, C, nocc, eps.
+    """
+    if refWfn is not None:
+        gao, C, nocc, eps = refWfn.ao_eri, refWfn.Ca, refWfn.nalpha, refWfn.epsa
+    g = _lib.f64(gao)
+    Cm = _lib.f64(C)
+    e = _lib.f64(eps)
+    n = g.shape[0]
+    gb = np.empty_like(g, order="F") if want_gao else None
+    cb = np.empty_like(Cm, order="F") if want_C else None
+    E = C_.c_double()
+    ctx = _lib.context(device)
+    _lib.check(ctx.lib.jues_rmp2_adjoint(ctx.h, _lib.ptr(g), n, _lib.ptr(Cm), int(nocc), _lib.ptr(e),
+                                         _lib.PREC[precision], float(e_bar), C_.byref(E), _lib.ptr(gb),
+                                         _lib.ptr(cb)))
+    return E.value, gb, cb

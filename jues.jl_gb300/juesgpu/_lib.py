@@ -62,6 +62,7 @@ SIGNATURES = {
     "jues_get_eri": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_char_p, C.c_int,
                                C.c_int, C.c_int, DP]),
     "jues_rmp2": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, DP]),
+    "jues_rmp2_adjoint": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_double, DP, DP, DP]),
     "jues_cc_default_opts": (C.c_int, [C.POINTER(CCOpts)]),
     "jues_rccd": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts), DP,
                             DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),

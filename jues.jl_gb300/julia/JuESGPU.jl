@@ -104,6 +104,47 @@ function do_rmp2(refWfn::Wfn; precision::Symbol = :fp64, kwargs...)
     return e[]
 end
 
+"""
+    rmp2_energy(gao, C, nocc, eps; precision = :fp64)
+
+Closed-shell MP2 energy from AO integrals and the full MO matrix; differentiable through the
+`rrule` below (dE/dgao and dE/dC from jues_rmp2_adjoint).
+"""
+function rmp2_energy(gao::AbstractArray{<:Real,4}, C::AbstractMatrix, nocc::Integer,
+                     eps::AbstractVector; precision::Symbol = :fp64)
+    E, _, _ = rmp2_adjoint(gao, C, nocc, eps, 1.0; want_gao = false, want_C = false, precision)
+    return E
+end
+
+function rmp2_adjoint(gao, C, nocc, eps, ebar; want_gao = true, want_C = true, precision = :fp64)
+    g, Cm, e = f64(gao), f64(C), f64(eps)
+    n = size(g, 1)
+    gb = want_gao ? similar(g) : nothing
+    cb = want_C ? similar(Cm) : nothing
+    E = Ref{Cdouble}(0.0)
+    check(ccall((:jues_rmp2_adjoint, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Cdouble,
+                 Ref{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                ctx(), g, n, Cm, nocc, e, PREC[precision], ebar, E,
+                gb === nothing ? C_NULL : gb, cb === nothing ? C_NULL : cb))
+    return E[], gb, cb
+end
+
+# ChainRulesCore rule (loaded when ChainRulesCore is available in the environment)
+try
+    @eval import ChainRulesCore
+    @eval function ChainRulesCore.rrule(::typeof(rmp2_energy), gao, C, nocc, eps; precision = :fp64)
+        E, gb, cb = rmp2_adjoint(gao, C, nocc, eps, 1.0; precision)
+        function rmp2_pullback(Ebar)
+            s = ChainRulesCore.unthunk(Ebar)
+            return (ChainRulesCore.NoTangent(), s .* gb, s .* cb, ChainRulesCore.NoTangent(),
+                    ChainRulesCore.NoTangent())
+        end
+        return E, rmp2_pullback
+    end
+catch
+end
+
 function cc_solve(method, refWfn; maxit, r_conv, e_conv, diis, diis_size, precision, guess, refine)
     Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
     o, v = size(Co, 2), size(Cv, 2)
