@@ -136,6 +136,30 @@ JUES_API int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const do
                                const double *eps, int precision, double e_bar, double *e_out,
                                double *gao_bar, double *C_bar);
 
+/* ---- batched MP2 (no reference counterpart; the batched form) --------------------------
+ * Energies and, when the pointer arrays are given, adjoints of many independent closed-shell
+ * systems of uneven size.  All systems run in one CUDA graph of grouped persistent GETT
+ * launches (13 stages); tile shapes are autotuned and the graph is cached for a repeated batch
+ * signature.  Host arrays; gao_bar / C_bar are arrays of nsys host pointers (entries may be
+ * NULL, the arrays themselves may be NULL). */
+typedef struct {
+    int n, o;             /* nbf and nocc; nvir = n - o                               */
+    const double *gao;    /* n^4 AO integrals, column-major                            */
+    const double *C;      /* n x n MO coefficients, occupied columns first             */
+    const double *eps;    /* n orbital energies                                        */
+} jues_mp2_system;
+
+typedef struct {
+    double upload_ms, graph_ms, download_ms;   /* CUDA-event times on the context stream */
+    int graph_nodes;      /* kernels in the captured graph                              */
+    int tuned;            /* 1 if this call built, autotuned and captured the plan       */
+    int nstages;          /* grouped GETT stages                                         */
+    int tile_shape[16];   /* chosen shape per stage: 0 64x64, 1 32x64, 2 64x32, 3 32x32  */
+} jues_batch_info;
+
+JUES_API int jues_batch_rmp2(jues_ctx *ctx, int nsys, const jues_mp2_system *systems, double e_bar,
+                             double *e_out, double **gao_bar, double **C_bar, jues_batch_info *info);
+
 /* ---- coupled cluster ------------------------------------------------------------------
  * Whole solves.  t2_out (o*o*v*v, [i,j,a,b]) and t1_out (o*v, [i,a]) may be NULL; log may
  * be NULL, else it receives up to log_cap records.  Returns JUES_ENOTCONV (with e_out,

@@ -347,6 +347,17 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
     });
 }
 
+int jues_batch_rmp2(jues_ctx *ctx, int nsys, const jues_mp2_system *systems, double e_bar, double *e_out,
+                    double **gao_bar, double **C_bar, jues_batch_info *info) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(systems, "systems");
+        need(e_out, "e_out");
+        cudaSetDevice(c.device);
+        batch_rmp2(&c, nsys, systems, e_bar, e_out, gao_bar, C_bar, info);
+    });
+}
+
 int jues_cc_default_opts(jues_cc_opts *opts) {
     return guarded([&] {
         need(opts, "opts");

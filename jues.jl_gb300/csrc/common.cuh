@@ -70,6 +70,7 @@ struct ProfRec {
 };
 
 struct PackCache;  // split-precision operand cache (gett_tc.cu)
+struct BatchCache;  // batched MP2 plans and graphs (batch.cu)
 
 struct Ctx {
     int device = 0;
@@ -82,6 +83,7 @@ struct Ctx {
     unsigned int *d_flags = nullptr;   // device error flags (timeouts, non-finite)
     double *d_red = nullptr;           // reduction scratch (1 << 16 doubles)
     PackCache *pack = nullptr;         // owned; destroyed by pack_cache_destroy
+    BatchCache *batch = nullptr;       // owned; destroyed by batch_cache_destroy
     Ctx();
     ~Ctx();
 
@@ -154,6 +156,9 @@ void gett_tc(Ctx *ctx, const GettArgs &g, const char *name);   // split BF16 on 
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
 void pack_cache_clear(Ctx *ctx);
 void pack_cache_destroy(PackCache *p);
+void batch_cache_destroy(BatchCache *p);
+void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, double *e_out, double **gao_bar,
+                double **C_bar, jues_batch_info *info);
 void pack_cache_drop(Ctx *ctx, const void *ptr);
 
 // ---------------------------------------------------------------------------------------

@@ -17,6 +17,8 @@ Ctx::~Ctx() {
     if (stream) cudaStreamSynchronize(stream);
     pack_cache_destroy(pack);
     pack = nullptr;
+    batch_cache_destroy(batch);
+    batch = nullptr;
     for (auto &kv : prof) {
         for (auto &e : kv.second.pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto &e : kv.second.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }

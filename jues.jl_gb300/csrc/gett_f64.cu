@@ -1,105 +1,101 @@
 // FP64 tensor contraction as a GEMM over composite tensor modes (the plain, drop-in form).
 //
 // GB300 executes FP64 on its CUDA cores only (there is no FP64 kind for tcgen05), so this
-// kernel is DFMA-issue bound: 64x64 output tiles, 4x4 register blocking per thread, operand
-// tiles staged in shared memory with the per-row / per-column element offsets of the
-// composite modes precomputed once per tile.
+// kernel is DFMA-issue bound: BM x BN output tiles, (BM/16) x (BN/16) register blocking per
+// thread, operand tiles staged in shared memory with the per-row / per-column element offsets
+// of the composite modes precomputed once per tile.  The same tile routine serves single
+// problems and the grouped (batched) form, whose persistent CTAs walk a tile list that spans
+// many independent problems.
+#include <algorithm>
+
 #include "common.cuh"
+#include "gett_f64.cuh"
 
 namespace jues {
 
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+constexpr int BK = 16, NT = 256;
 
-struct KArgs {
-    long long M, N, K;
-    double alpha, beta;
-    const double *A; Mode mA, kA;
-    const double *B; Mode kB, nB;
-    double *C; Mode mC, nC;
-    const double *Cin;
-    long long mtiles;
-    int a_mfast, b_nfast, c_mfast;
+template <int BM, int BN>
+struct TileSmem {
+    double As[BK][BM + 1];
+    double Bs[BK][BN + 1];
+    long long offA[BM], offB[BN], offCm[BM], offCn[BN];
+    long long koA[BK], koB[BK];
 };
 
-__global__ void __launch_bounds__(NT) gett_f64_kernel(KArgs g) {
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
-    __shared__ long long offA[BM], offB[BN], offCm[BM], offCn[BN];
-    __shared__ long long koA[BK], koB[BK];
-
+template <int BM, int BN>
+__device__ __forceinline__ void gett_tile(const GroupProblem &g, long long tile, TileSmem<BM, BN> &sm) {
+    constexpr int TM = BM / 16, TN = BN / 16;
     const int tid = threadIdx.x;
-    const long long tile = blockIdx.x;
     const long long m0 = (tile % g.mtiles) * BM;
     const long long n0 = (tile / g.mtiles) * BN;
-
-    if (tid < BM) {
-        long long m = m0 + tid;
-        offA[tid] = m < g.M ? mode_off(g.mA, m) : -1;
-        offCm[tid] = m < g.M ? mode_off(g.mC, m) : -1;
-    } else if (tid < BM + BN) {
-        long long n = n0 + tid - BM;
-        offB[tid - BM] = n < g.N ? mode_off(g.nB, n) : -1;
-        offCn[tid - BM] = n < g.N ? mode_off(g.nC, n) : -1;
+    const int a_mfast = (g.mA.s0 == 1 && g.mA.d0 > 1);
+    const int b_nfast = (g.nB.s0 == 1 && g.nB.d0 > 1);
+    const int c_mfast = (g.mC.s0 == 1 && g.mC.d0 > 1);
+    __syncthreads();   // the previous tile of a persistent CTA is done with the tables
+    for (int r = tid; r < BM; r += NT) {
+        const long long m = m0 + r;
+        sm.offA[r] = m < g.M ? mode_off(g.mA, m) : -1;
+        sm.offCm[r] = m < g.M ? mode_off(g.mC, m) : -1;
     }
-
-    // thread tile: 4 rows x 4 cols, strided by 16 to keep shared-memory reads conflict-free
-    const int tr = g.c_mfast ? (tid & 15) : (tid >> 4);
-    const int tc = g.c_mfast ? (tid >> 4) : (tid & 15);
-    double acc[4][4];
+    for (int c = tid; c < BN; c += NT) {
+        const long long n = n0 + c;
+        sm.offB[c] = n < g.N ? mode_off(g.nB, n) : -1;
+        sm.offCn[c] = n < g.N ? mode_off(g.nC, n) : -1;
+    }
+    const int tr = c_mfast ? (tid & 15) : (tid >> 4);
+    const int tc = c_mfast ? (tid >> 4) : (tid & 15);
+    double acc[TM][TN];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < TN; ++j) acc[i][j] = 0.0;
 
     for (long long k0 = 0; k0 < g.K; k0 += BK) {
         __syncthreads();
         if (tid < BK) {
-            long long k = k0 + tid;
-            koA[tid] = k < g.K ? mode_off(g.kA, k) : -1;
+            const long long k = k0 + tid;
+            sm.koA[tid] = k < g.K ? mode_off(g.kA, k) : -1;
         } else if (tid >= 32 && tid < 32 + BK) {
-            long long k = k0 + tid - 32;
-            koB[tid - 32] = k < g.K ? mode_off(g.kB, k) : -1;
+            const long long k = k0 + tid - 32;
+            sm.koB[tid - 32] = k < g.K ? mode_off(g.kB, k) : -1;
         }
         __syncthreads();
-#pragma unroll
-        for (int i = 0; i < (BM * BK) / NT; ++i) {
-            int e = tid + i * NT;
-            int m = g.a_mfast ? (e % BM) : (e / BK);
-            int k = g.a_mfast ? (e / BM) : (e % BK);
-            long long om = offA[m], ok = koA[k];
-            As[k][m] = (om >= 0 && ok >= 0) ? __ldg(g.A + om + ok) : 0.0;
+        for (int e = tid; e < BM * BK; e += NT) {
+            const int m = a_mfast ? (e % BM) : (e / BK);
+            const int k = a_mfast ? (e / BM) : (e % BK);
+            const long long om = sm.offA[m], ok = sm.koA[k];
+            sm.As[k][m] = (om >= 0 && ok >= 0) ? __ldg(g.A + om + ok) : 0.0;
         }
-#pragma unroll
-        for (int i = 0; i < (BN * BK) / NT; ++i) {
-            int e = tid + i * NT;
-            int n = g.b_nfast ? (e % BN) : (e / BK);
-            int k = g.b_nfast ? (e / BN) : (e % BK);
-            long long on = offB[n], ok = koB[k];
-            Bs[k][n] = (on >= 0 && ok >= 0) ? __ldg(g.B + on + ok) : 0.0;
+        for (int e = tid; e < BN * BK; e += NT) {
+            const int n = b_nfast ? (e % BN) : (e / BK);
+            const int k = b_nfast ? (e / BN) : (e % BK);
+            const long long on = sm.offB[n], ok = sm.koB[k];
+            sm.Bs[k][n] = (on >= 0 && ok >= 0) ? __ldg(g.B + on + ok) : 0.0;
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            double a[4], b[4];
+            double a[TM], b[TN];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][tr + 16 * i];
+            for (int i = 0; i < TM; ++i) a[i] = sm.As[kk][tr + 16 * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tc + 16 * j];
+            for (int j = 0; j < TN; ++j) b[j] = sm.Bs[kk][tc + 16 * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
         }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        long long om = offCm[tr + 16 * i];
+    for (int i = 0; i < TM; ++i) {
+        const long long om = sm.offCm[tr + 16 * i];
         if (om < 0) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            long long on = offCn[tc + 16 * j];
+        for (int j = 0; j < TN; ++j) {
+            const long long on = sm.offCn[tc + 16 * j];
             if (on < 0) continue;
             double v = g.alpha * acc[i][j];
             if (g.beta != 0.0) v = fma(g.beta, g.Cin[om + on], v);
@@ -108,8 +104,29 @@ __global__ void __launch_bounds__(NT) gett_f64_kernel(KArgs g) {
     }
 }
 
+template <int BM, int BN>
+__global__ void __launch_bounds__(NT) gett_f64_kernel(GroupProblem g) {
+    __shared__ TileSmem<BM, BN> sm;
+    gett_tile<BM, BN>(g, blockIdx.x, sm);
+}
+
+// persistent grouped form: problem p owns tiles [tile_start[p], tile_start[p+1])
+template <int BM, int BN>
+__global__ void __launch_bounds__(NT) gett_f64_grouped(const GroupProblem *__restrict__ probs, int nprob,
+                                                       long long total) {
+    __shared__ TileSmem<BM, BN> sm;
+    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
+        }
+        gett_tile<BM, BN>(probs[lo], t - probs[lo].tile_start, sm);
+    }
+}
+
 // skinny GEMM (N <= 8): one warp per output row, lanes split K
-__global__ void gett_f64_skinny(KArgs g) {
+__global__ void gett_f64_skinny(GroupProblem g) {
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= g.M) return;
@@ -146,20 +163,22 @@ __global__ void gett_f64_skinny(KArgs g) {
 
 }  // namespace
 
-void gett_f64(Ctx *ctx, const GettArgs &a, const char *name) {
-    if (a.M <= 0 || a.N <= 0) return;
-    KArgs g;
+GroupProblem to_problem(const GettArgs &a) {
+    GroupProblem g;
     g.M = a.M; g.N = a.N; g.K = a.K;
     g.alpha = a.alpha; g.beta = a.beta;
     g.A = a.A; g.mA = a.mA; g.kA = a.kA;
     g.B = a.B; g.kB = a.kB; g.nB = a.nB;
     g.C = a.C; g.mC = a.mC; g.nC = a.nC;
     g.Cin = a.Cin ? a.Cin : a.C;
-    g.mtiles = (a.M + BM - 1) / BM;
-    long long ntiles = (a.N + BN - 1) / BN;
-    g.a_mfast = (a.mA.s0 == 1 && a.mA.d0 > 1) ? 1 : 0;
-    g.b_nfast = (a.nB.s0 == 1 && a.nB.d0 > 1) ? 1 : 0;
-    g.c_mfast = (a.mC.s0 == 1 && a.mC.d0 > 1) ? 1 : 0;
+    g.mtiles = 1;
+    g.tile_start = 0;
+    return g;
+}
+
+void gett_f64(Ctx *ctx, const GettArgs &a, const char *name) {
+    if (a.M <= 0 || a.N <= 0) return;
+    GroupProblem g = to_problem(a);
     if (a.N <= 8) {
         long long blocks = (a.M * 32 + 255) / 256;
         JUES_REQUIRE(blocks < (1LL << 31), "GEMM too large for one launch");
@@ -168,10 +187,38 @@ void gett_f64(Ctx *ctx, const GettArgs &a, const char *name) {
         JUES_CHECK_CUDA(cudaGetLastError());
         return;
     }
-    long long tiles = g.mtiles * ntiles;
+    g.mtiles = (a.M + 63) / 64;
+    const long long tiles = g.mtiles * ((a.N + 63) / 64);
     JUES_REQUIRE(tiles < (1LL << 31), "GEMM too large for one launch");
     Ctx::Scope s(ctx, name);
-    gett_f64_kernel<<<(unsigned)tiles, NT, 0, ctx->stream>>>(g);
+    gett_f64_kernel<64, 64><<<(unsigned)tiles, NT, 0, ctx->stream>>>(g);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+const TileShape kTileShapes[kNumTileShapes] = {{64, 64}, {32, 64}, {64, 32}, {32, 32}};
+
+long long grouped_tiles(std::vector<GroupProblem> &probs, int shape) {
+    const int BM = kTileShapes[shape].bm, BN = kTileShapes[shape].bn;
+    long long start = 0;
+    for (auto &p : probs) {
+        p.mtiles = (p.M + BM - 1) / BM;
+        p.tile_start = start;
+        start += (p.M > 0 && p.N > 0) ? p.mtiles * ((p.N + BN - 1) / BN) : 0;
+    }
+    return start;
+}
+
+void gett_f64_grouped_launch(Ctx *ctx, const GroupProblem *d_probs, int nprob, long long total, int shape,
+                             const char *name) {
+    if (total <= 0) return;
+    const long long grid = std::min<long long>(total, 152LL * 4);   // persistent: 4 CTAs per SM
+    Ctx::Scope s(ctx, name);
+    switch (shape) {
+        case 0: gett_f64_grouped<64, 64><<<(unsigned)grid, NT, 0, ctx->stream>>>(d_probs, nprob, total); break;
+        case 1: gett_f64_grouped<32, 64><<<(unsigned)grid, NT, 0, ctx->stream>>>(d_probs, nprob, total); break;
+        case 2: gett_f64_grouped<64, 32><<<(unsigned)grid, NT, 0, ctx->stream>>>(d_probs, nprob, total); break;
+        default: gett_f64_grouped<32, 32><<<(unsigned)grid, NT, 0, ctx->stream>>>(d_probs, nprob, total); break;
+    }
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 

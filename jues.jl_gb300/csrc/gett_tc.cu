@@ -1,16 +1,17 @@
 // Split-precision GEMM over tensor modes on the sm_103a tensor cores (tcgen05 + TMEM + TMA).
 //
-// Each FP64 operand row r (a row of A or of B, running over K) gets a power-of-two scale 2^e_r
-// with max_k |x_rk| < 2^e_r, and every element is written as two small integers carried in BF16,
-//     x = 2^(e_r - 7) (hi + 2^-8 lo),   hi = rint(x 2^(7 - e_r)),  |hi|, |lo| <= 128,
-// so |x - 2^(e_r-7)(hi + 2^-8 lo)| <= 2^(e_r-16).  One CTA computes a 128 x BN tile of
-// C = A.B^T with three tcgen05.mma products per K=16 step: hi.hi into a "main" TMEM accumulator
-// and hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-16), is dropped).  Because the
-// BF16 values are integers, every product and every partial sum of a chunk of KC stages
-// (< 2^23) is an exact FP32 integer: the tensor core's truncating accumulation never rounds.
-// Chunks alternate between two TMEM buffers; four warps add finished chunks into FP32
-// registers (round-to-nearest, unbiased) while the next chunk runs, then rescale by
-// 2^(e_r + e_c - 14) and apply alpha/beta in FP64 through the output tensor modes.  Operand
+// Each FP64 operand row r (a row of A or of B, running over K) is cut into chunks of KCH = 128
+// K values; chunk c gets a power-of-two scale 2^e with max |x| < 2^e over the chunk, and every
+// element is written as two small integers carried in BF16,
+//     x = 2^(e - 8) (hi + 2^-8 lo),   hi = rint(x 2^(8 - e)),  |hi| <= 256, |lo| <= 128,
+// so |x - 2^(e-8)(hi + 2^-8 lo)| <= 2^(e-17).  One CTA computes a 128 x BN tile of C = A.B^T
+// with three tcgen05.mma products per K=16 step: hi.hi into a "main" TMEM accumulator and
+// hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-17), is dropped).  Because the
+// BF16 values are integers, every product and every partial sum of one chunk (< 2^23) is an
+// exact FP32 integer: the tensor core's truncating accumulation never rounds.  Chunks alternate
+// between two TMEM buffers; four warps scale each finished chunk by 2^(e_r + e_c - 16) and add
+// it into FP32 registers (round-to-nearest, unbiased) while the next chunk runs, then apply
+// alpha/beta in FP64 through the output tensor modes.  Operand
 // tiles arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by
 // mbarriers; one thread issues the TMA loads and one the MMAs.  Every mbarrier wait is bounded
 // by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips its stores, frees its TMEM and
@@ -148,7 +149,8 @@ struct TcArgs {
     long long M, N;        // logical GEMM extent (rows of A, rows of B)
     int kblocks;           // padded K / TBK
     long long mtiles;
-    const int *expA, *expB;   // per-row power-of-two scales of the packed operands
+    const int *expA, *expB;   // per-(chunk,row) power-of-two scales, [chunk][row]
+    long long expA_ld, expB_ld;   // padded row counts (chunk strides)
     double alpha, beta;
     double *C;
     const double *Cin;
@@ -157,9 +159,8 @@ struct TcArgs {
 };
 
 // Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-5 drain TMEM.
-// The MMA warp restarts both accumulators every KC stages (KC * 64 K values keeps every
-// partial sum below 2^23), alternating between two TMEM buffers, and the drain warps add each
-// finished chunk into FP32 registers with round-to-nearest while the next chunk runs.
+// The MMA warp restarts both accumulators every KC stages (one scaling chunk of KCH = KC * 64
+// K values, which keeps every partial sum below 2^23), alternating between two TMEM buffers.
 constexpr int TC_THREADS = 192;
 
 template <int BN, int STAGES, int KC>
@@ -168,7 +169,7 @@ struct TcCfg {
     static constexpr int B_BYTES = BN * TBK * 2;
     static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
     static constexpr int BAR_BYTES = 256;
-    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 16 + 1024;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 1024;
     static constexpr uint32_t TMEM_COLS = 4 * BN;   // 2 buffers x (main, correction)
     // instruction descriptor: FP32 accumulate, BF16 A and B, both K-major, M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -193,7 +194,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cempty + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     long long *coloff = reinterpret_cast<long long *>(smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES);
-    double *colscale = reinterpret_cast<double *>(coloff + BN);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long mt = blockIdx.x % g.mtiles, nt = blockIdx.x / g.mtiles;
@@ -221,8 +221,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int c = threadIdx.x; c < BN; c += blockDim.x) {
         const long long n = (long long)n0 + c;
         coloff[c] = n < g.N ? mode_off(g.nC, n) : -1;
-        const int eb = n < g.N ? g.expB[n] : INT_MIN;
-        colscale[c] = eb == INT_MIN ? 0.0 : scalbn(1.0, eb);   // INT_MIN: all-zero row
     }
     tc_fence_before();
     __syncthreads();
@@ -301,6 +299,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             __syncwarp();
             tc_fence_after();
+            const long long mrow = (long long)m0 + quarter * 32 + lane;
+            const int ea = g.expA[(long long)c * g.expA_ld + mrow];
+            const int *ebp = g.expB + (long long)c * g.expB_ld + n0;
 #pragma unroll
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 uint32_t rm[16], rc[16];
@@ -309,9 +310,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 tmem_ld16(base + (uint32_t)BN, rc);
                 tmem_ld_wait();
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    acc[c0 + j] = __fadd_rn(acc[c0 + j],
-                                            __fmaf_rn(__uint_as_float(rc[j]), 0.00390625f, __uint_as_float(rm[j])));
+                for (int j = 0; j < 16; ++j) {
+                    const int eb = __ldg(ebp + c0 + j);
+                    const int sh = (ea == INT_MIN || eb == INT_MIN) ? -1000 : ea + eb - 16;
+                    // 2^sh as an FP32 scale (0 below the normal range; exponents of real data
+                    // stay far from the top of the range)
+                    const float sc = sh < -126 ? 0.f : __int_as_float((sh + 127) << 23);
+                    const float part = __fmaf_rn(__uint_as_float(rc[j]), 0.00390625f, __uint_as_float(rm[j]));
+                    acc[c0 + j] = __fmaf_rn(part, sc, acc[c0 + j]);
+                }
             }
             tc_fence_before();
             mbar_arrive(&cempty[buf]);
@@ -322,13 +329,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const long long m = (long long)m0 + quarter * 32 + lane;
             if (m < g.M) {
                 const long long rowoff = mode_off(g.mC, m);
-                const int ea = g.expA[m];
-                const double rs = ea == INT_MIN ? 0.0 : g.alpha * scalbn(1.0, ea - 14);
 #pragma unroll
                 for (int j = 0; j < BN; ++j) {
                     const long long co = coloff[j];
                     if (co >= 0) {
-                        double val = rs * colscale[j] * (double)acc[j];
+                        double val = g.alpha * (double)acc[j];
                         if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
                         g.C[rowoff + co] = val;
                     }
@@ -344,11 +349,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// Per-row power-of-two scale: rexp[r] = e with max_k |x_rk| < 2^e (INT_MIN for an all-zero row).
-constexpr int PR = 32, PK = 64;
+// Per-(chunk,row) power-of-two scale: rexp[c*Rpad + r] = e with max |x_rk| < 2^e over the K
+// values of chunk c (INT_MIN when they are all zero).
+constexpr int PR = 32, PK = 64, KCH = 128;
 __global__ void __launch_bounds__(256) rowexp_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
-                                                     long long R, long long K, long long Kpad, int kfast,
-                                                     int *__restrict__ rexp) {
+                                                     long long R, long long K, long long Rpad, long long Kpad,
+                                                     int kfast, int *__restrict__ rexp) {
     __shared__ long long roff[PR], koff[PK];
     __shared__ int tmax[PR];
     const long long kblocks = Kpad / PK;
@@ -380,11 +386,12 @@ __global__ void __launch_bounds__(256) rowexp_kernel(const double *__restrict__ 
         }
     }
     __syncthreads();
-    if (tid < PR && r0 + tid < R && tmax[tid] != INT_MIN) atomicMax(&rexp[r0 + tid], tmax[tid]);
+    if (tid < PR && r0 + tid < R && tmax[tid] != INT_MIN)
+        atomicMax(&rexp[(k0 / KCH) * Rpad + r0 + tid], tmax[tid]);
 }
 
 // FP64 operand -> integer-valued BF16 planes [2][Rpad][Kpad], K-major:
-// hi = rint(x 2^(7-e_r)), lo = rint((x 2^(7-e_r) - hi) 2^8)
+// hi = rint(x 2^(8-e)), lo = rint((x 2^(8-e) - hi) 2^8) with e the (chunk,row) scale
 __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
                                                          long long Kpad, int kfast, const int *__restrict__ rexp,
@@ -415,17 +422,17 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
     // each thread writes 8 consecutive K values of one row to both planes (16-byte stores)
     const int rr = tid >> 3, kc = (tid & 7) * 8;
     const long long r = r0 + rr;
-    const int ex = (r < R) ? rexp[r] : INT_MIN;
+    const int ex = (r < R) ? rexp[(k0 / KCH) * Rpad + r] : INT_MIN;
     __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         double h = 0.0, l = 0.0;
         if (ex != INT_MIN) {
-            const double y = scalbn(tile[rr][kc + j], 7 - ex);   // |y| < 128, exact scaling
+            const double y = scalbn(tile[rr][kc + j], 8 - ex);   // |y| < 256, exact scaling
             h = rint(y);
             l = rint((y - h) * 256.0);
         }
-        hi[j] = __double2bfloat16(h);   // integers of magnitude <= 128: exact in BF16
+        hi[j] = __double2bfloat16(h);   // integers of magnitude <= 256: exact in BF16
         lo[j] = __double2bfloat16(l);
     }
     const size_t base = (size_t)r * (size_t)Kpad + (size_t)(k0 + kc);
@@ -516,12 +523,13 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
                 return Packed{e->buf.p, e->exps.p};
     }
     const size_t need = (size_t)2 * Rpad * Kpad;
+    const long long nchunk = (Kpad + KCH - 1) / KCH;
     __nv_bfloat16 *dst;
     int *ex;
     std::unique_ptr<PackEntry> ent;
     if (cache) {
         ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__nv_bfloat16>(ctx, need),
-                                DBuf<int>(ctx, (size_t)Rpad)});
+                                DBuf<int>(ctx, (size_t)nchunk * Rpad)});
         dst = ent->buf.p;
         ex = ent->exps.p;
     } else {
@@ -529,9 +537,9 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
             pc.scratch[slot].reset();
             pc.scratch[slot] = DBuf<__nv_bfloat16>(ctx, need);
         }
-        if (pc.scratch_exp[slot].n < (size_t)Rpad) {
+        if (pc.scratch_exp[slot].n < (size_t)(nchunk * Rpad)) {
             pc.scratch_exp[slot].reset();
-            pc.scratch_exp[slot] = DBuf<int>(ctx, (size_t)Rpad);
+            pc.scratch_exp[slot] = DBuf<int>(ctx, (size_t)(nchunk * Rpad));
         }
         dst = pc.scratch[slot].p;
         ex = pc.scratch_exp[slot].p;
@@ -541,9 +549,9 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     {
         Ctx::Scope s(ctx, "pack_split");
-        fill_int_kernel<<<(unsigned)std::min<long long>((Rpad + 255) / 256, 4096), 256, 0, ctx->stream>>>(
-            ex, Rpad, INT_MIN);
-        rowexp_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Kpad, kfast, ex);
+        fill_int_kernel<<<(unsigned)std::min<long long>((nchunk * Rpad + 255) / 256, 4096), 256, 0,
+                          ctx->stream>>>(ex, nchunk * Rpad, INT_MIN);
+        rowexp_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex);
         pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
                                                                      dst);
         JUES_CHECK_CUDA(cudaGetLastError());
@@ -553,7 +561,7 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     return Packed{dst, ex};
 }
 
-constexpr int TC_KC = 4;   // stages per accumulation chunk (K = 256)
+constexpr int TC_KC = KCH / TBK;   // stages per accumulation chunk (one scaling chunk)
 
 template <int BN, int STAGES>
 static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
@@ -629,6 +637,8 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     t.flags = ctx->d_flags;
     t.expA = pa.exps;
     t.expB = pb.exps;
+    t.expA_ld = Mpad;
+    t.expB_ld = Npad;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
     if (BN == 128)

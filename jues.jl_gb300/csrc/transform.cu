@@ -7,6 +7,7 @@
 // (F = sum_k 2 n^(5-k) prod_{m<=k} d_(m)).  The last quarter writes straight into the caller's
 // layout: chemists' [i,a,j,b] or, for get_eri's physicists' notation, [i,j,a,b].
 #include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 #include "transform.cuh"
@@ -25,15 +26,16 @@ double transform4_flops(int n, const int d[4]) {
     return f;
 }
 
-void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const C[4], const int d_in[4],
-                double *out, const long long ostr[4], bool g_const) {
+std::vector<GettArgs> transform4_plan(const double *g, int n, const double *const C[4], const int d_in[4],
+                                      double *out, const long long ostr[4], double *buf0, double *buf1) {
     // a null C[p] keeps AO index p (three-quarter transforms for the MP2 adjoint)
     int d[4];
     for (int p = 0; p < 4; ++p) {
         d[p] = C[p] ? d_in[p] : n;
         JUES_REQUIRE(d[p] >= 0, "negative MO dimension");
     }
-    if (d[0] == 0 || d[1] == 0 || d[2] == 0 || d[3] == 0) return;
+    std::vector<GettArgs> steps;
+    if (d[0] == 0 || d[1] == 0 || d[2] == 0 || d[3] == 0) return steps;
     int nsteps = 0;
     for (int p = 0; p < 4; ++p) nsteps += C[p] ? 1 : 0;
     JUES_REQUIRE(nsteps > 0, "transform4 needs at least one coefficient matrix");
@@ -41,7 +43,7 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
     bool done[4];
     for (int p = 0; p < 4; ++p) done[p] = !C[p];
     const double *cur = g;
-    DBuf<double> bufs[2];
+    double *bufs[2] = {buf0, buf1};
     int which = 0;
     for (int step = 0; step < nsteps; ++step) {
         int p = -1;
@@ -59,9 +61,7 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
         } else {
             sY[0] = 1;
             for (int q = 1; q < 4; ++q) sY[q] = sY[q - 1] * nd[q - 1];
-            size_t cnt = (size_t)(nd[0] * nd[1] * nd[2] * nd[3]);
-            if (bufs[which].n < cnt) bufs[which] = DBuf<double>(ctx, cnt);
-            dst = bufs[which].p;
+            dst = bufs[which];
         }
         int q1 = -1, q2 = -1, q3 = -1;
         for (int q = 0; q < 4; ++q) {
@@ -83,25 +83,55 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
         a.C = dst;
         a.mC = mode3(nd[q1], nd[q2], sY[q1], sY[q2], sY[q3]);
         a.nC = plain(sY[p]);
-        a.a_const = (step == 0) && g_const;
-        a.b_const = false;
-        gett(ctx, prec, a, step == 0 ? "transform_q1" : "transform_q234");
+        steps.push_back(a);
         for (int q = 0; q < 4; ++q) dims[q] = nd[q];
         done[p] = true;
         cur = dst;
         which ^= 1;
     }
+    return steps;
 }
 
-void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, const double *const C[4],
-                    double *out) {
+long long transform4_scratch(int n, const double *const C[4], const int d_in[4]) {
+    // largest intermediate of transform4_plan
+    int d[4];
+    for (int p = 0; p < 4; ++p) d[p] = C[p] ? d_in[p] : n;
+    long long dims[4] = {n, n, n, n}, best = 0;
+    bool done[4];
+    int nsteps = 0;
+    for (int p = 0; p < 4; ++p) { done[p] = !C[p]; nsteps += C[p] ? 1 : 0; }
+    for (int step = 0; step + 1 < nsteps; ++step) {
+        int p = -1;
+        for (int q = 0; q < 4; ++q)
+            if (!done[q] && (p < 0 || d[q] < d[p])) p = q;
+        dims[p] = d[p];
+        done[p] = true;
+        best = std::max(best, dims[0] * dims[1] * dims[2] * dims[3]);
+    }
+    return best;
+}
+
+void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const C[4], const int d_in[4],
+                double *out, const long long ostr[4], bool g_const) {
+    const long long need = transform4_scratch(n, C, d_in);
+    DBuf<double> b0(ctx, (size_t)need), b1(ctx, (size_t)need);
+    std::vector<GettArgs> steps = transform4_plan(g, n, C, d_in, out, ostr, b0.p, b1.p);
+    for (size_t k = 0; k < steps.size(); ++k) {
+        steps[k].a_const = (k == 0) && g_const;
+        gett(ctx, prec, steps[k], k == 0 ? "transform_q1" : "transform_q234");
+    }
+}
+
+std::vector<GettArgs> backtransform4_plan(const double *X, const int d[4], int n, const double *const C[4],
+                                          double *out, double *buf0, double *buf1) {
     // out[mu,nu,lam,sig] = sum X[i,a,j,b] C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b]; the last step
     // costs 2 n^4 d_last, so the largest MO dimension is expanded first
     long long dims[4] = {d[0], d[1], d[2], d[3]};
     bool done[4] = {false, false, false, false};
     const double *cur = X;
-    DBuf<double> bufs[2];
+    double *bufs[2] = {buf0, buf1};
     int which = 0;
+    std::vector<GettArgs> steps;
     for (int step = 0; step < 4; ++step) {
         int p = -1;
         for (int q = 0; q < 4; ++q)
@@ -113,14 +143,7 @@ void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, 
         nd[p] = n;
         sY[0] = 1;
         for (int q = 1; q < 4; ++q) sY[q] = sY[q - 1] * nd[q - 1];
-        double *dst;
-        if (step == 3) {
-            dst = out;
-        } else {
-            size_t cnt = (size_t)(nd[0] * nd[1] * nd[2] * nd[3]);
-            if (bufs[which].n < cnt) bufs[which] = DBuf<double>(ctx, cnt);
-            dst = bufs[which].p;
-        }
+        double *dst = step == 3 ? out : bufs[which];
         int q1 = -1, q2 = -1, q3 = -1;
         for (int q = 0; q < 4; ++q) {
             if (q == p) continue;
@@ -141,12 +164,34 @@ void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, 
         a.C = dst;
         a.mC = mode3(nd[q1], nd[q2], sY[q1], sY[q2], sY[q3]);
         a.nC = plain(sY[p]);
-        gett(ctx, prec, a, "backtransform");
+        steps.push_back(a);
         for (int q = 0; q < 4; ++q) dims[q] = nd[q];
         done[p] = true;
         cur = dst;
         which ^= 1;
     }
+    return steps;
+}
+
+long long backtransform4_scratch(const int d[4], int n) {
+    long long dims[4] = {d[0], d[1], d[2], d[3]}, best = 0;
+    bool done[4] = {false, false, false, false};
+    for (int step = 0; step < 3; ++step) {
+        int p = -1;
+        for (int q = 0; q < 4; ++q)
+            if (!done[q] && (p < 0 || d[q] > d[p])) p = q;
+        dims[p] = n;
+        done[p] = true;
+        best = std::max(best, dims[0] * dims[1] * dims[2] * dims[3]);
+    }
+    return best;
+}
+
+void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, const double *const C[4],
+                    double *out) {
+    const long long need = backtransform4_scratch(d, n);
+    DBuf<double> b0(ctx, (size_t)need), b1(ctx, (size_t)need);
+    for (auto &a : backtransform4_plan(X, d, n, C, out, b0.p, b1.p)) gett(ctx, prec, a, "backtransform");
 }
 
 void get_eri_block(Ctx *ctx, int prec, const double *g, int n, const double *Cocc, int o,

@@ -1,4 +1,6 @@
 #pragma once
+#include <vector>
+
 #include "common.cuh"
 
 namespace jues {
@@ -10,6 +12,14 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
 // out[mu,nu,lam,sig] = sum X[i,a,j,b] C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b], out n^4 column-major
 void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, const double *const C[4],
                     double *out);
+// the GETT steps of transform4 / backtransform4 with caller-provided ping-pong buffers of
+// transform4_scratch / backtransform4_scratch elements each (used by the batched form)
+std::vector<GettArgs> transform4_plan(const double *g, int n, const double *const C[4], const int d[4],
+                                      double *out, const long long ostr[4], double *buf0, double *buf1);
+long long transform4_scratch(int n, const double *const C[4], const int d[4]);
+std::vector<GettArgs> backtransform4_plan(const double *X, const int d[4], int n, const double *const C[4],
+                                          double *out, double *buf0, double *buf1);
+long long backtransform4_scratch(const int d[4], int n);
 // spec: 4 chars of o/O/v/V; phys: physicists' notation; fcn: frozen core count
 void get_eri_block(Ctx *ctx, int prec, const double *g, int n, const double *Cocc, int o,
                    const double *Cvir, int v, const char spec[4], bool phys, int fcn, double *out,

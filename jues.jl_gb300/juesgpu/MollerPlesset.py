@@ -46,3 +46,34 @@ def rmp2_adjoint(refWfn=None, *, gao=None, C=None, nocc=None, eps=None, e_bar: f
                                          _lib.PREC[precision], float(e_bar), C_.byref(E), _lib.ptr(gb),
                                          _lib.ptr(cb)))
     return E.value, gb, cb
+
+
+def batch_rmp2(systems, *, e_bar: float = 1.0, adjoint: bool = False, device: int = 0):
+    """MP2 energies (and adjoints) of many independent systems in one CUDA graph.
+
+    systems: iterable of (gao, C, nocc, eps) or Wfn objects.  Returns (energies, gao_bars,
+    C_bars, info) with the gradient lists None unless ``adjoint``.
+    """
+    items = []
+    for s in systems:
+        if hasattr(s, "ao_eri"):
+            s = (s.ao_eri, s.Ca, s.nalpha, s.epsa)
+        g, Cm, o, e = s
+        items.append((_lib.f64(g), _lib.f64(Cm), int(o), _lib.f64(e)))
+    nsys = len(items)
+    arr = (_lib.MP2System * nsys)()
+    for k, (g, Cm, o, e) in enumerate(items):
+        arr[k] = _lib.MP2System(g.shape[0], o, _lib.ptr(g), _lib.ptr(Cm), _lib.ptr(e))
+    energies = np.zeros(nsys)
+    gbs = cbs = None
+    gptr = cptr = None
+    if adjoint:
+        gbs = [np.empty_like(g, order="F") for g, _, _, _ in items]
+        cbs = [np.empty_like(Cm, order="F") for _, Cm, _, _ in items]
+        gptr = (_lib.DP * nsys)(*[_lib.ptr(x) for x in gbs])
+        cptr = (_lib.DP * nsys)(*[_lib.ptr(x) for x in cbs])
+    info = _lib.BatchInfo()
+    ctx = _lib.context(device)
+    _lib.check(ctx.lib.jues_batch_rmp2(ctx.h, nsys, arr, float(e_bar), _lib.ptr(energies), gptr, cptr,
+                                       C_.byref(info)))
+    return energies, gbs, cbs, info

@@ -41,6 +41,17 @@ class IterLog(C.Structure):
                 ("rnorm", C.c_double), ("ms", C.c_double)]
 
 
+class MP2System(C.Structure):
+    _fields_ = [("n", C.c_int), ("o", C.c_int), ("gao", C.POINTER(C.c_double)),
+                ("C", C.POINTER(C.c_double)), ("eps", C.POINTER(C.c_double))]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("upload_ms", C.c_double), ("graph_ms", C.c_double), ("download_ms", C.c_double),
+                ("graph_nodes", C.c_int), ("tuned", C.c_int), ("nstages", C.c_int),
+                ("tile_shape", C.c_int * 16)]
+
+
 DP = C.POINTER(C.c_double)
 VP = C.c_void_p
 
@@ -63,6 +74,8 @@ SIGNATURES = {
                                C.c_int, C.c_int, DP]),
     "jues_rmp2": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, DP]),
     "jues_rmp2_adjoint": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_double, DP, DP, DP]),
+    "jues_batch_rmp2": (C.c_int, [VP, C.c_int, C.POINTER(MP2System), C.c_double, DP, C.POINTER(DP),
+                                  C.POINTER(DP), C.POINTER(BatchInfo)]),
     "jues_cc_default_opts": (C.c_int, [C.POINTER(CCOpts)]),
     "jues_rccd": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts), DP,
                             DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
