@@ -29,7 +29,7 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "jues.jl_gb300")]
 
 import numpy as np  # noqa: E402
 
-METRIC = "RCCD s/iter at nbf=200 (split-BF16 tcgen05, FP64 beside)"
+METRIC = "RCCD s/iter & TFLOP/s at nbf=200: split-BF16 vs FP64 on 1 GB300 at \u22641 \u00b5Eh"
 SHAPES = {"S200": ("S200", 200, 40, 600), "S100": ("S100", 100, 20, 300)}
 SHAPE = SHAPES["S200"]
 
@@ -258,13 +258,37 @@ def run_gpu(args):
     e_split = None
     if args.check:
         s2 = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
-                       guess="mp2", diis=True, r_conv=1e-9, refine=2, maxit=60)
+                       guess="mp2", diis=True, r_conv=1e-9, refine=2, maxit=60, transform_precision="fp64")
         s2.iterate(60)
         e_split = s2.energy()
         nconv = len(s2.log())
         s2.close()
         if golden is not None and rank == 0:
             err = e_split - golden
+
+    # ---------------- transform: <ij|ab> block, FP64 vs split (library kernel events) ----------
+    from juesgpu import MollerPlesset
+    wt = system.wfn(ao_eri=gao)
+    tr = {}
+    for prec in ("fp64", "split_bf16"):
+        ctx.set_profiling(True)
+        ctx.profile_reset()
+        e_mp2 = MollerPlesset.do_rmp2(wt, precision=prec, device=local)
+        t_q, _ = ctx.profile("transform")
+        t_p, _ = ctx.profile("pack_split")
+        ctx.set_profiling(False)
+        tr[prec] = {"ms": t_q + t_p, "mp2": e_mp2}
+    mp2_golden = None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "synthetic_golden.json")) as f:
+            mp2_golden = json.load(f).get(name, {}).get("mp2")
+    except OSError:
+        pass
+    transform = {"block": "<ij|ab> (ov|ov)", "fp64_ms": tr["fp64"]["ms"], "split_ms": tr["split_bf16"]["ms"],
+                 "speedup": tr["fp64"]["ms"] / max(tr["split_bf16"]["ms"], 1e-9),
+                 "mp2_fp64": tr["fp64"]["mp2"], "mp2_split": tr["split_bf16"]["mp2"],
+                 "mp2_split_error_eh": tr["split_bf16"]["mp2"] - tr["fp64"]["mp2"],
+                 "mp2_fp64_vs_oracle_eh": (tr["fp64"]["mp2"] - mp2_golden) if mp2_golden else None}
 
     # ---------------- e2e through the C ABI with host buffers ----------------
     e2e = None
@@ -307,6 +331,7 @@ def run_gpu(args):
         "fp64_s_per_iter": fp64,
         "speedup_vs_fp64": (fp64 / s_per_iter) if fp64 else None,
         "energy_split": e_split, "energy_fp64_golden": golden, "energy_error_eh": err,
+        "transform": transform,
         "wall_s_timed": wall, "setup_s": setup_s,
         "kernels_ms_per_step": {"pp_ladder": pp_ms / args.steps, "ring": ring_ms / args.steps,
                                 "pack_split": pack_ms / args.steps},

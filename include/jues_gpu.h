@@ -67,6 +67,7 @@ typedef struct {
     int precision;    /* JUES_PREC_*                                                       */
     int guess;        /* JUES_GUESS_*                                                      */
     int refine;       /* split precision only: number of closing FP64 sweeps               */
+    int transform_precision; /* precision of the integral transform; -1 = same as precision */
 } jues_cc_opts;
 
 typedef struct {

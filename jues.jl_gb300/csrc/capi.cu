@@ -66,6 +66,8 @@ void check_opts(const jues_cc_opts &o) {
         throw Error(JUES_EINVAL, "unknown precision");
     if (o.guess < 0 || o.guess > 2) throw Error(JUES_EINVAL, "unknown guess");
     if (o.refine < 0) throw Error(JUES_EINVAL, "refine must be >= 0");
+    if (o.transform_precision < -1 || o.transform_precision > 1)
+        throw Error(JUES_EINVAL, "unknown transform_precision");
 }
 
 }  // namespace
@@ -369,6 +371,7 @@ int jues_cc_default_opts(jues_cc_opts *opts) {
         opts->precision = JUES_PREC_FP64;
         opts->guess = JUES_GUESS_ZERO;   // mRCCD.jl:245
         opts->refine = 2;
+        opts->transform_precision = -1;
     });
 }
 

@@ -221,7 +221,7 @@ CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *C
     s->eps = DBuf<double>(ctx, n);
     d2d(ctx, s->eps.p, eps_dev, n);
     // integral blocks (mRCCD.jl:120-127, mRCCSD.jl:102-110), physicists' notation
-    const int iprec = opts.precision;   // transform in the same precision form
+    const int iprec = opts.transform_precision >= 0 ? opts.transform_precision : opts.precision;
     s->oovv = DBuf<double>(ctx, t2n);
     s->ovov = DBuf<double>(ctx, t2n);
     s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));

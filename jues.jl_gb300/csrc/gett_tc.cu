@@ -1,23 +1,25 @@
 // Split-precision GEMM over tensor modes on the sm_103a tensor cores (tcgen05 + TMEM + TMA).
 //
-// Each FP64 operand row r (a row of A or of B, running over K) is cut into chunks of KCH = 128
-// K values; chunk c gets a power-of-two scale 2^e with max |x| < 2^e over the chunk, and every
-// element is written as two small integers carried in BF16,
-//     x = 2^(e - 8) (hi + 2^-8 lo),   hi = rint(x 2^(8 - e)),  |hi| <= 256, |lo| <= 128,
-// so |x - 2^(e-8)(hi + 2^-8 lo)| <= 2^(e-17).  One CTA computes a 128 x BN tile of C = A.B^T
-// with three tcgen05.mma products per K=16 step: hi.hi into a "main" TMEM accumulator and
-// hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-17), is dropped).  Because the
-// BF16 values are integers, every product and every partial sum of one chunk (< 2^23) is an
-// exact FP32 integer: the tensor core's truncating accumulation never rounds.  Chunks alternate
-// between two TMEM buffers; four warps scale each finished chunk by 2^(e_r + e_c - 16) and add
-// it into FP32 registers (round-to-nearest, unbiased) while the next chunk runs, then apply
-// alpha/beta in FP64 through the output tensor modes.  Operand
+// Each FP64 operand row r (a row of A or of B, running over K) is cut into chunks of KCH = 64
+// K values (one pipeline stage); chunk c gets a power-of-two scale 2^e with max |x| < 2^e over
+// the chunk, and every element is written as two integers carried exactly in FP16,
+//     x = 2^(e - 9) (hi + 2^-10 lo),   hi = rint(x 2^(9 - e)),  |hi|, |lo| <= 512,
+// so |x - 2^(e-9)(hi + 2^-10 lo)| <= 2^(e-20).  One CTA computes a 128 x BN tile of C = A.B^T
+// with three tcgen05.mma (kind::f16) products per K=16 step: hi.hi into a "main" TMEM
+// accumulator and hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-20), is dropped).
+// Because the FP16 values are integers, every product and every partial sum of the main
+// accumulator over one chunk (<= 64 * 2^18 = 2^24) is an exact FP32 integer: the tensor core's
+// truncating accumulation never rounds where it matters (the correction term is 2^-10 smaller,
+// so its rounding is below 1e-10 of the result).  Chunks alternate between two TMEM buffers;
+// four warps scale each finished chunk by 2^(e_r + e_c - 18) and add it into FP32 registers
+// (round-to-nearest, unbiased) while the next chunk runs, then apply alpha/beta in FP64
+// through the output tensor modes.  Operand
 // tiles arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by
 // mbarriers; one thread issues the TMA loads and one the MMAs.  Every mbarrier wait is bounded
 // by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips its stores, frees its TMEM and
 // returns.
 #include <cuda.h>
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -32,7 +34,7 @@ namespace jues {
 namespace {
 
 constexpr int TBM = 128;   // tile rows (TMEM lanes)
-constexpr int TBK = 64;    // K elements per stage: 128 bytes of BF16 = one swizzle atom row
+constexpr int TBK = 64;    // K elements per stage: 128 bytes of FP16 = one swizzle atom row
 constexpr unsigned long long WAIT_LIMIT_NS = 2ull * 1000 * 1000 * 1000;    // 2 s: legitimate waits last microseconds
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -97,7 +99,7 @@ __device__ __forceinline__ void tmem_relinquish() {
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
-// D[tmem] (+)= A[smem desc] . B[smem desc]^T, BF16 inputs, FP32 accumulation
+// D[tmem] (+)= A[smem desc] . B[smem desc]^T, 16-bit inputs, FP32 accumulation
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
     asm volatile(
@@ -171,9 +173,9 @@ struct TcCfg {
     static constexpr int BAR_BYTES = 256;
     static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 1024;
     static constexpr uint32_t TMEM_COLS = 4 * BN;   // 2 buffers x (main, correction)
-    // instruction descriptor: FP32 accumulate, BF16 A and B, both K-major, M = 128, N = BN
-    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                                      ((uint32_t)(TBM >> 4) << 24);
+    // instruction descriptor: FP32 accumulate, FP16 A and B (format 0), both K-major,
+    // M = 128, N = BN
+    static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -312,11 +314,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int eb = __ldg(ebp + c0 + j);
-                    const int sh = (ea == INT_MIN || eb == INT_MIN) ? -1000 : ea + eb - 16;
+                    const int sh = (ea == INT_MIN || eb == INT_MIN) ? -1000 : ea + eb - 18;
                     // 2^sh as an FP32 scale (0 below the normal range; exponents of real data
                     // stay far from the top of the range)
                     const float sc = sh < -126 ? 0.f : __int_as_float((sh + 127) << 23);
-                    const float part = __fmaf_rn(__uint_as_float(rc[j]), 0.00390625f, __uint_as_float(rm[j]));
+                    const float part = __fmaf_rn(__uint_as_float(rc[j]), 0.0009765625f, __uint_as_float(rm[j]));
                     acc[c0 + j] = __fmaf_rn(part, sc, acc[c0 + j]);
                 }
             }
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // Per-(chunk,row) power-of-two scale: rexp[c*Rpad + r] = e with max |x_rk| < 2^e over the K
 // values of chunk c (INT_MIN when they are all zero).
-constexpr int PR = 32, PK = 64, KCH = 128;
+constexpr int PR = 32, PK = 64, KCH = 64;
 __global__ void __launch_bounds__(256) rowexp_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                      long long R, long long K, long long Rpad, long long Kpad,
                                                      int kfast, int *__restrict__ rexp) {
@@ -390,12 +392,12 @@ __global__ void __launch_bounds__(256) rowexp_kernel(const double *__restrict__ 
         atomicMax(&rexp[(k0 / KCH) * Rpad + r0 + tid], tmax[tid]);
 }
 
-// FP64 operand -> integer-valued BF16 planes [2][Rpad][Kpad], K-major:
-// hi = rint(x 2^(8-e)), lo = rint((x 2^(8-e) - hi) 2^8) with e the (chunk,row) scale
+// FP64 operand -> integer-valued FP16 planes [2][Rpad][Kpad], K-major:
+// hi = rint(x 2^(9-e)), lo = rint((x 2^(9-e) - hi) 2^10) with e the (chunk,row) scale
 __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
                                                          long long Kpad, int kfast, const int *__restrict__ rexp,
-                                                         __nv_bfloat16 *__restrict__ dst) {
+                                                         __half *__restrict__ dst) {
     __shared__ double tile[PR][PK + 1];
     __shared__ long long roff[PR], koff[PK];
     const long long kblocks = Kpad / PK;
@@ -423,17 +425,17 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
     const int rr = tid >> 3, kc = (tid & 7) * 8;
     const long long r = r0 + rr;
     const int ex = (r < R) ? rexp[(k0 / KCH) * Rpad + r] : INT_MIN;
-    __align__(16) __nv_bfloat16 hi[8], lo[8];
+    __align__(16) __half hi[8], lo[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         double h = 0.0, l = 0.0;
         if (ex != INT_MIN) {
-            const double y = scalbn(tile[rr][kc + j], 8 - ex);   // |y| < 256, exact scaling
+            const double y = scalbn(tile[rr][kc + j], 9 - ex);   // |y| < 512, exact scaling
             h = rint(y);
-            l = rint((y - h) * 256.0);
+            l = rint((y - h) * 1024.0);
         }
-        hi[j] = __double2bfloat16(h);   // integers of magnitude <= 256: exact in BF16
-        lo[j] = __double2bfloat16(l);
+        hi[j] = __float2half_rn((float)h);   // integers of magnitude <= 512: exact in FP16
+        lo[j] = __float2half_rn((float)l);
     }
     const size_t base = (size_t)r * (size_t)Kpad + (size_t)(k0 + kc);
     *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
@@ -458,14 +460,14 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     return fn;
 }
 
-CUtensorMap make_map(const __nv_bfloat16 *base, long long rows_pad, long long kpad, int box_rows) {
+CUtensorMap make_map(const __half *base, long long rows_pad, long long kpad, int box_rows) {
     CUtensorMap m;
     std::memset(&m, 0, sizeof(m));
     cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, 2};
     cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
     cuuint32_t box[3] = {(cuuint32_t)TBK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dims,
+    CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half *>(base), dims,
                               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(JUES_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -488,16 +490,16 @@ struct PackEntry {
     const double *src;
     Mode r, k;
     long long R, K, Rpad, Kpad;
-    DBuf<__nv_bfloat16> buf;
+    DBuf<__half> buf;
     DBuf<int> exps;
 };
 struct PackCache {
     std::vector<std::unique_ptr<PackEntry>> cached;
-    DBuf<__nv_bfloat16> scratch[2];
+    DBuf<__half> scratch[2];
     DBuf<int> scratch_exp[2];
 };
 struct Packed {
-    const __nv_bfloat16 *planes;
+    const __half *planes;
     const int *exps;
 };
 
@@ -524,18 +526,18 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     }
     const size_t need = (size_t)2 * Rpad * Kpad;
     const long long nchunk = (Kpad + KCH - 1) / KCH;
-    __nv_bfloat16 *dst;
+    __half *dst;
     int *ex;
     std::unique_ptr<PackEntry> ent;
     if (cache) {
-        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__nv_bfloat16>(ctx, need),
+        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__half>(ctx, need),
                                 DBuf<int>(ctx, (size_t)nchunk * Rpad)});
         dst = ent->buf.p;
         ex = ent->exps.p;
     } else {
         if (pc.scratch[slot].n < need) {
             pc.scratch[slot].reset();
-            pc.scratch[slot] = DBuf<__nv_bfloat16>(ctx, need);
+            pc.scratch[slot] = DBuf<__half>(ctx, need);
         }
         if (pc.scratch_exp[slot].n < (size_t)(nchunk * Rpad)) {
             pc.scratch_exp[slot].reset();

@@ -8,10 +8,10 @@ from ._solve import solve
 
 
 def do_rccd(refWfn, maxit=40, doprint=False, return_T2=False, *, precision="fp64", guess="zero",
-            r_conv=1e-7, e_conv=0.0, diis=True, diis_size=6, refine=2, device=0, return_log=False):
+            r_conv=1e-7, e_conv=0.0, diis=True, diis_size=6, refine=2, transform_precision=None, device=0, return_log=False):
     e, _, T2, nit, log = solve(0, refWfn, device=device, maxit=maxit, e_conv=e_conv, r_conv=r_conv,
                                diis=diis, diis_size=diis_size, precision=precision, guess=guess,
-                               refine=refine)
+                               refine=refine, transform_precision=transform_precision)
     if doprint:
         for it, en, rn, ms, _p in log:
             print(f"@CCD {en:20.17f}")

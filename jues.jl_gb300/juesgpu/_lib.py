@@ -33,7 +33,7 @@ class NotConverged(JuESError):
 class CCOpts(C.Structure):
     _fields_ = [("maxit", C.c_int), ("e_conv", C.c_double), ("r_conv", C.c_double),
                 ("diis", C.c_int), ("diis_size", C.c_int), ("precision", C.c_int),
-                ("guess", C.c_int), ("refine", C.c_int)]
+                ("guess", C.c_int), ("refine", C.c_int), ("transform_precision", C.c_int)]
 
 
 class IterLog(C.Structure):

@@ -29,6 +29,7 @@ struct CCOpts
     precision::Cint
     guess::Cint
     refine::Cint
+    transform_precision::Cint
 end
 
 struct IterLog
@@ -148,7 +149,7 @@ end
 function cc_solve(method, refWfn; maxit, r_conv, e_conv, diis, diis_size, precision, guess, refine)
     Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
     o, v = size(Co, 2), size(Cv, 2)
-    opts = Ref(CCOpts(maxit, e_conv, r_conv, diis, diis_size, PREC[precision], GUESS[guess], refine))
+    opts = Ref(CCOpts(maxit, e_conv, r_conv, diis, diis_size, PREC[precision], GUESS[guess], refine, Cint(-1)))
     e = Ref{Cdouble}(0.0)
     nit = Ref{Cint}(0)
     T2 = Array{Float64}(undef, o, o, v, v)
