@@ -102,6 +102,23 @@ JUES_API int jues_gemm(jues_ctx *ctx, int transA, int transB, int M, int N, int 
                        const double *A, int lda, const double *B, int ldb, double beta,
                        double *C, int ldc, int precision);
 
+/* Allocation-free variant of jues_gemm's split-precision path.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory when they contract: code running
+ * under CUDA graph capture (where cudaMalloc is not permitted), hosts whose device memory is
+ * owned by their own pool allocator, and fixed-budget callers.  A, B and C are DEVICE
+ * pointers (column-major, C = alpha op(A) op(B) + beta C); the call allocates nothing: the
+ * packed operands go to a static device array of 64 MiB that every GPU loading the library
+ * holds until the process exits.  Problems whose packed operands,
+ * 4 (Mpad + Npad) Kpad + 4 ceil(Kpad/64) (Mpad + Npad) bytes with Mpad, Npad and Kpad rounded
+ * up to 128, 128 and 64, exceed it are rejected with JUES_EINVAL.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress, with that device current); make
+ * that first call before any stream capture.  All calls share the one array: calls whose
+ * execution overlaps on the GPU (other streams, other contexts on the same device) race on it.
+ * Runs on the context's stream and is synchronous at return. */
+JUES_API int jues_gemm_noalloc(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double alpha,
+                               const double *A_dev, int lda, const double *B_dev, int ldb, double beta,
+                               double *C_dev, int ldc);
+
 /* ---- four-index transformation -------------------------------------------------------
  * out[i,a,j,b] = sum C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b] gao[mu,nu,lam,sig]
  * (chemists' (C1 C2|C3 C4)); gao is n^4, Ck is n x dk, out is d1 x d2 x d3 x d4.

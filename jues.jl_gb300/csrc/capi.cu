@@ -195,6 +195,29 @@ int jues_gemm(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double
     });
 }
 
+int jues_gemm_noalloc(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double alpha,
+                      const double *A_dev, int lda, const double *B_dev, int ldb, double beta, double *C_dev,
+                      int ldc) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(A_dev, "A"); need(B_dev, "B"); need(C_dev, "C");
+        if (M < 0 || N < 0 || K < 0) throw Error(JUES_EINVAL, "negative GEMM dimension");
+        const int ar = transA ? K : M, br = transB ? N : K;
+        if (lda < std::max(1, ar) || ldb < std::max(1, br) || ldc < std::max(1, M))
+            throw Error(JUES_EINVAL, "leading dimension too small");
+        if (M == 0 || N == 0) return;
+        JUES_CHECK_CUDA(cudaSetDevice(c.device));
+        GettArgs g;
+        g.M = M; g.N = N; g.K = K;
+        g.alpha = alpha; g.beta = beta;
+        g.A = A_dev; g.mA = transA ? plain(lda) : plain(1); g.kA = transA ? plain(1) : plain(lda);
+        g.B = B_dev; g.kB = transB ? plain(ldb) : plain(1); g.nB = transB ? plain(1) : plain(ldb);
+        g.C = C_dev; g.mC = plain(1); g.nC = plain(ldc);
+        gett_tc_noalloc(&c, g);
+        c.check_flags();
+    });
+}
+
 int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1, int d1, const double *C2,
                        int d2, const double *C3, int d3, const double *C4, int d4, int precision,
                        double *out) {

@@ -154,6 +154,9 @@ struct GettArgs {
 void gett_f64(Ctx *ctx, const GettArgs &g, const char *name);
 void gett_tc(Ctx *ctx, const GettArgs &g, const char *name);   // split BF16 on tcgen05
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
+// split GEMM that packs into a static device array instead of allocating (see gett_tc.cu)
+void gett_tc_noalloc(Ctx *ctx, const GettArgs &g);
+size_t gett_tc_noalloc_limit();
 void pack_cache_clear(Ctx *ctx);
 void pack_cache_destroy(PackCache *p);
 void batch_cache_destroy(BatchCache *p);

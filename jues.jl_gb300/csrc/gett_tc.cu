@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -647,6 +648,107 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
         launch_tc<128, 3>(ctx, ma, mb, t, tiles, name);
     else
         launch_tc<64, 4>(ctx, ma, mb, t, tiles, name);
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant of the split GEMM (jues_gemm_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they need a contraction: code
+// running while a CUDA graph is being captured (cudaMalloc is not allowed there), host
+// frameworks whose device memory is owned entirely by their own pool allocator, and
+// fixed-budget or real-time callers that must not grow their footprint after start-up.
+// For them this variant packs its operands into one statically sized device array that is
+// part of the loaded module (every GPU that loads the library holds it until the process
+// exits) and allocates nothing itself.  The caller provides inputs and output in device
+// memory.
+// ---------------------------------------------------------------------------------------
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(64) << 20;   // 64 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void *g_noalloc_addr[kMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of the static scratch on the current device.  Host code sees the array's
+// name only as a host-side stand-in, so the address is fetched from the runtime once per
+// device (with that device current) and cached.
+void *noalloc_scratch_address(int device) {
+    JUES_REQUIRE(device >= 0 && device < kMaxDevices, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        JUES_CHECK_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        if (!p) throw Error(JUES_ECUDA, "cudaGetSymbolAddress returned a null scratch address");
+        g_noalloc_addr[device] = p;
+    }
+    return g_noalloc_addr[device];
+}
+
+void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
+               long long Rpad, long long Kpad, __half *dst, int *ex) {
+    const long long nchunk = (Kpad + KCH - 1) / KCH;
+    const long long blocks = (Rpad / PR) * (Kpad / PK);
+    JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
+    const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
+    Ctx::Scope s(ctx, "pack_split_noalloc");
+    fill_int_kernel<<<(unsigned)std::min<long long>((nchunk * Rpad + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+        ex, nchunk * Rpad, INT_MIN);
+    rowexp_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex);
+    pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex, dst);
+    JUES_CHECK_CUDA(cudaGetLastError());
+    ctx->launches += 2;
+}
+}  // namespace
+
+size_t gett_tc_noalloc_limit() { return NOALLOC_SCRATCH_BYTES; }
+
+void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
+    if (a.M <= 0 || a.N <= 0) return;
+    JUES_REQUIRE(a.K >= 1, "K must be positive");
+    // fixed orientation and tile width: BN = 128, the A operand on the TMEM-lane side
+    constexpr int BN = 128;
+    const long long Mpad = roundup(a.M, TBM), Npad = roundup(a.N, BN), Kpad = roundup(a.K, TBK);
+    const long long nchunk = (Kpad + KCH - 1) / KCH;
+    const size_t planesA = (size_t)2 * Mpad * Kpad * sizeof(__half);
+    const size_t planesB = (size_t)2 * Npad * Kpad * sizeof(__half);
+    const size_t expsA = (size_t)nchunk * Mpad * sizeof(int), expsB = (size_t)nchunk * Npad * sizeof(int);
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t need = up(planesA) + up(planesB) + up(expsA) + up(expsB);
+    if (need > NOALLOC_SCRATCH_BYTES)
+        throw Error(JUES_EINVAL, "jues_gemm_noalloc: this GEMM needs " + std::to_string(need) +
+                                     " bytes of packed operands, more than the static scratch of " +
+                                     std::to_string(NOALLOC_SCRATCH_BYTES) + " bytes");
+    unsigned char *base = static_cast<unsigned char *>(noalloc_scratch_address(ctx->device));
+    __half *pa = reinterpret_cast<__half *>(base);
+    __half *pb = reinterpret_cast<__half *>(base + up(planesA));
+    int *ea = reinterpret_cast<int *>(base + up(planesA) + up(planesB));
+    int *eb = reinterpret_cast<int *>(base + up(planesA) + up(planesB) + up(expsA));
+    // every byte the kernels read is rewritten here: planes including their zero padding, and
+    // the scales (reset to "all zero" before the row-maximum pass)
+    pack_into(ctx, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, pa, ea);
+    pack_into(ctx, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, pb, eb);
+    const CUtensorMap ma = make_map(pa, Mpad, Kpad, TBM);
+    const CUtensorMap mb = make_map(pb, Npad, Kpad, BN);
+    TcArgs t;
+    t.M = a.M;
+    t.N = a.N;
+    t.kblocks = (int)(Kpad / TBK);
+    t.mtiles = Mpad / TBM;
+    t.alpha = a.alpha;
+    t.beta = a.beta;
+    t.C = a.C;
+    t.Cin = a.Cin ? a.Cin : a.C;
+    t.mC = a.mC;
+    t.nC = a.nC;
+    t.flags = ctx->d_flags;
+    t.expA = ea;
+    t.expB = eb;
+    t.expA_ld = Mpad;
+    t.expB_ld = Npad;
+    const long long tiles = t.mtiles * (Npad / BN);
+    JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
+    launch_tc<BN, 3>(ctx, ma, mb, t, tiles, "gemm_noalloc");
 }
 
 }  // namespace jues
