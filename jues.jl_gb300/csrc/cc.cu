@@ -33,10 +33,13 @@ double ccd_reference_flops(int o_, int v_) {
 
 namespace {
 
-// C = alpha * A.B + beta * Cin over the given modes
+// C = alpha * A.B + beta * Cin over the given modes.  With s->cache_operands set, split-precision
+// packs of every operand are kept until the operand's buffer is dropped (see ccd_sweep).
 void G(CCState *s, int prec, const char *name, long long M, long long N, long long K, double alpha,
        const double *A, Mode mA, Mode kA, const double *B, Mode kB, Mode nB, double beta, double *C,
        Mode mC, Mode nC, const double *Cin = nullptr, bool a_const = false, bool b_const = false) {
+    a_const = a_const || s->cache_operands;
+    b_const = b_const || s->cache_operands;
     GettArgs g;
     g.M = M; g.N = N; g.K = K;
     g.alpha = alpha; g.beta = beta;
@@ -61,6 +64,12 @@ double ccd_sweep(CCState *s, int prec) {
     Ctx *ctx = s->ctx;
     const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v, vv = v * v;
     const double *T = s->T.p;
+    // Every operand of this sweep is read-only once formed, so its split-precision packs can be
+    // shared between the GEMMs that use it; the buffers that change from sweep to sweep lose
+    // their packs here (the integrals keep theirs).
+    for (const double *p : {s->T.p, s->Tn.p, s->Tt.p, s->Wp.p, s->WJ.p, s->WK.p, s->W12.p, s->Fae.p, s->Fmi.p})
+        pack_cache_drop(ctx, p);
+    s->cache_operands = (prec == JUES_PREC_SPLIT_BF16);
     // T~[i,j,a,b] = 2T[i,j,a,b] - T[j,i,a,b]
     t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
     const double *Tt = s->Tt.p;
@@ -111,6 +120,7 @@ double ccd_sweep(CCState *s, int prec) {
     G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
       plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
 
+    s->cache_operands = false;
     return t2_finalize(ctx, s->L.p, Z, s->eps.p, (int)o, (int)v, T, s->Tn.p);
 }
 

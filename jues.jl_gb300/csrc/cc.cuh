@@ -28,7 +28,8 @@ struct CCState {
     std::vector<int> dorder;   // slots in insertion order
     double energy = 0.0, e_prev = 0.0;
     int iters = 0;
-    int refine_left = -1;   // split precision: closing FP64 sweeps left (-1 = not started)
+    int refine_left = -1;
+    bool cache_operands = false;   // keep split packs of sweep operands (CCD only)   // split precision: closing FP64 sweeps left (-1 = not started)
     bool converged = false;
     std::vector<jues_iter_log> log;
     double sweep_flops(int prec) const;

@@ -161,10 +161,12 @@ struct TcArgs {
     unsigned *flags;
 };
 
-// Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-5 drain TMEM.
+// Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-9 drain TMEM (two
+// warps per 32-lane TMEM quarter, each owning half of the tile's columns).
 // The MMA warp restarts both accumulators every KC stages (one scaling chunk of KCH = KC * 64
 // K values, which keeps every partial sum below 2^23), alternating between two TMEM buffers.
-constexpr int TC_THREADS = 192;
+constexpr int TC_THREADS = 320;
+constexpr int TC_DRAIN = 256;   // drain threads (warps 2-9)
 
 template <int BN, int STAGES, int KC>
 struct TcCfg {
@@ -172,7 +174,7 @@ struct TcCfg {
     static constexpr int B_BYTES = BN * TBK * 2;
     static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
     static constexpr int BAR_BYTES = 256;
-    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 1024;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 2 * BN * 4 + 1024;
     static constexpr uint32_t TMEM_COLS = 4 * BN;   // 2 buffers x (main, correction)
     // instruction descriptor: FP32 accumulate, FP16 A and B (format 0), both K-major,
     // M = 128, N = BN
@@ -197,6 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cempty + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     long long *coloff = reinterpret_cast<long long *>(smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES);
+    float *colsc = reinterpret_cast<float *>(coloff + BN);   // [2][BN] per-chunk column scales
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long mt = blockIdx.x % g.mtiles, nt = blockIdx.x / g.mtiles;
@@ -211,7 +214,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&cfull[b], 1);
-            mbar_init(&cempty[b], 128);
+            mbar_init(&cempty[b], TC_DRAIN);
         }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -287,14 +290,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
     } else {
-        // drain warps 2-5: TMEM lane quarter (warp % 4), one tile row per thread
+        // drain warps 2-9: TMEM lane quarter (warp % 4), one tile row per thread, half the columns
+        constexpr int HB = BN / 2;
         const int quarter = warp & 3;
-        float acc[BN];
+        const int half = (warp - 2) >> 2;
+        const int dt = threadIdx.x - 64;   // 0..255 among the drain threads
+        float acc[HB];
 #pragma unroll
-        for (int j = 0; j < BN; ++j) acc[j] = 0.f;
+        for (int j = 0; j < HB; ++j) acc[j] = 0.f;
+        const long long mrow = (long long)m0 + quarter * 32 + lane;
         bool ok = true;
         for (int c = 0; c < nchunks; ++c) {
             const int buf = c & 1;
+            // column scales of this chunk: 2^e_col, staged once for all drain warps
+            if (dt < BN) {
+                const int eb = g.expB[(long long)c * g.expB_ld + n0 + dt];
+                colsc[buf * BN + dt] = (eb == INT_MIN || eb < -126) ? 0.f : __int_as_float((eb + 127) << 23);
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(TC_DRAIN) : "memory");
             if (!mbar_wait(&cfull[buf], (uint32_t)(c >> 1) & 1u, abort_flag, g.flags)) {
                 ok = false;
                 *abort_flag = 1;
@@ -302,25 +315,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             __syncwarp();
             tc_fence_after();
-            const long long mrow = (long long)m0 + quarter * 32 + lane;
             const int ea = g.expA[(long long)c * g.expA_ld + mrow];
-            const int *ebp = g.expB + (long long)c * g.expB_ld + n0;
+            // row factor 2^(e_row - 18); the column factor comes from shared memory
+            const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
+            const float *cs = colsc + buf * BN + half * HB;
 #pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 16) {
+            for (int c0 = 0; c0 < HB; c0 += 16) {
                 uint32_t rm[16], rc[16];
-                const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 2 * BN + c0);
+                const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                      (uint32_t)(buf * 2 * BN + half * HB + c0);
                 tmem_ld16(base, rm);
                 tmem_ld16(base + (uint32_t)BN, rc);
                 tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    const int eb = __ldg(ebp + c0 + j);
-                    const int sh = (ea == INT_MIN || eb == INT_MIN) ? -1000 : ea + eb - 18;
-                    // 2^sh as an FP32 scale (0 below the normal range; exponents of real data
-                    // stay far from the top of the range)
-                    const float sc = sh < -126 ? 0.f : __int_as_float((sh + 127) << 23);
                     const float part = __fmaf_rn(__uint_as_float(rc[j]), 0.0009765625f, __uint_as_float(rm[j]));
-                    acc[c0 + j] = __fmaf_rn(part, sc, acc[c0 + j]);
+                    acc[c0 + j] = __fmaf_rn(part, rs * cs[c0 + j], acc[c0 + j]);
                 }
             }
             tc_fence_before();
@@ -328,18 +338,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         if (!ok || *abort_flag) {
             if (lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
-        } else {
-            const long long m = (long long)m0 + quarter * 32 + lane;
-            if (m < g.M) {
-                const long long rowoff = mode_off(g.mC, m);
+        } else if (mrow < g.M) {
+            const long long rowoff = mode_off(g.mC, mrow);
 #pragma unroll
-                for (int j = 0; j < BN; ++j) {
-                    const long long co = coloff[j];
-                    if (co >= 0) {
-                        double val = g.alpha * (double)acc[j];
-                        if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
-                        g.C[rowoff + co] = val;
-                    }
+            for (int j = 0; j < HB; ++j) {
+                const long long co = coloff[half * HB + j];
+                if (co >= 0) {
+                    double val = g.alpha * (double)acc[j];
+                    if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
+                    g.C[rowoff + co] = val;
                 }
             }
         }
@@ -352,52 +359,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// Per-(chunk,row) power-of-two scale: rexp[c*Rpad + r] = e with max |x_rk| < 2^e over the K
-// values of chunk c (INT_MIN when they are all zero).
-constexpr int PR = 32, PK = 64, KCH = 64;
-__global__ void __launch_bounds__(256) rowexp_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
-                                                     long long R, long long K, long long Rpad, long long Kpad,
-                                                     int kfast, int *__restrict__ rexp) {
-    __shared__ long long roff[PR], koff[PK];
-    __shared__ int tmax[PR];
-    const long long kblocks = Kpad / PK;
-    const long long r0 = (blockIdx.x / kblocks) * PR;
-    const long long k0 = (blockIdx.x % kblocks) * PK;
-    const int tid = threadIdx.x;
-    if (tid < PR) {
-        const long long r = r0 + tid;
-        roff[tid] = r < R ? mode_off(rmode, r) : -1;
-        tmax[tid] = INT_MIN;
-    } else if (tid >= 64 && tid < 64 + PK) {
-        const long long k = k0 + tid - 64;
-        koff[tid - 64] = k < K ? mode_off(kmode, k) : -1;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < (PR * PK) / 256; ++i) {
-        const int e = tid + i * 256;
-        const int kk = kfast ? (e % PK) : (e / PR);
-        const int rr = kfast ? (e / PK) : (e % PR);
-        const long long a = roff[rr], b = koff[kk];
-        if (a >= 0 && b >= 0) {
-            const double x = __ldg(src + a + b);
-            if (x != 0.0) {
-                int ex;
-                frexp(x, &ex);   // |x| < 2^ex
-                atomicMax(&tmax[rr], ex);
-            }
-        }
-    }
-    __syncthreads();
-    if (tid < PR && r0 + tid < R && tmax[tid] != INT_MIN)
-        atomicMax(&rexp[(k0 / KCH) * Rpad + r0 + tid], tmax[tid]);
+constexpr int PR = 32, PK = 64, KCH = 64;   // pack tile; scaling chunk = one pipeline stage
+
+// FP64 operand -> integer-valued FP16 planes [2][Rpad][Kpad], K-major, and the per-(chunk,row)
+// scales, in one pass.  A block covers 32 rows x 64 K = exactly one scaling chunk per row, so
+// the chunk maximum is a block-local reduction.  The split works on the IEEE-754 bit pattern
+// with integer arithmetic only (GB300 runs FP64 arithmetic at a small fraction of its integer
+// rate): for x = +-m 2^(E-1075) (m the 53-bit significand) and chunk scale e,
+//     q = rint(x 2^(19-e)) = round(m >> (1056 + e - E)),  hi = (q + 512) >> 10,  lo = q - 1024 hi,
+// so x ~ 2^(e-19) q = 2^(e-9) (hi + 2^-10 lo) with |hi| <= 512, |lo| <= 512.  Every element
+// of the padded tile and every scale is written, so nothing has to be cleared beforehand.
+__device__ __forceinline__ int exp_bound(double x) {
+    // smallest e with |x| < 2^e (INT_MIN for zero and subnormals, which are flushed)
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7FF);
+    return E == 0 ? INT_MIN : E - 1022;
+}
+__device__ __forceinline__ long long fixed_q(double x, int e) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7FF);
+    if (E == 0 || e == INT_MIN) return 0;
+    const unsigned long long m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int r = 1056 + e - E;   // >= 34 because |x| < 2^e
+    const unsigned long long q = r > 60 ? 0ull : ((m + (1ull << (r - 1))) >> r);
+    return (b >> 63) ? -(long long)q : (long long)q;
 }
 
-// FP64 operand -> integer-valued FP16 planes [2][Rpad][Kpad], K-major:
-// hi = rint(x 2^(9-e)), lo = rint((x 2^(9-e) - hi) 2^10) with e the (chunk,row) scale
 __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
-                                                         long long Kpad, int kfast, const int *__restrict__ rexp,
+                                                         long long Kpad, int kfast, int *__restrict__ rexp,
                                                          __half *__restrict__ dst) {
     __shared__ double tile[PR][PK + 1];
     __shared__ long long roff[PR], koff[PK];
@@ -422,31 +412,28 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
         tile[rr][kk] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
     }
     __syncthreads();
-    // each thread writes 8 consecutive K values of one row to both planes (16-byte stores)
+    // the 8 threads of a row are consecutive lanes: reduce the chunk exponent with shuffles
     const int rr = tid >> 3, kc = (tid & 7) * 8;
+    int ex = INT_MIN;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) ex = max(ex, exp_bound(tile[rr][kc + j]));
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, d));
     const long long r = r0 + rr;
-    const int ex = (r < R) ? rexp[(k0 / KCH) * Rpad + r] : INT_MIN;
+    if ((tid & 7) == 0) rexp[(k0 / KCH) * Rpad + r] = ex;
     __align__(16) __half hi[8], lo[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-        double h = 0.0, l = 0.0;
-        if (ex != INT_MIN) {
-            const double y = scalbn(tile[rr][kc + j], 9 - ex);   // |y| < 512, exact scaling
-            h = rint(y);
-            l = rint((y - h) * 1024.0);
-        }
-        hi[j] = __float2half_rn((float)h);   // integers of magnitude <= 512: exact in FP16
-        lo[j] = __float2half_rn((float)l);
+        const long long q = fixed_q(tile[rr][kc + j], ex);
+        const long long h = (q + 512) >> 10;
+        hi[j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
+        lo[j] = __int2half_rn((int)(q - (h << 10)));
     }
     const size_t base = (size_t)r * (size_t)Kpad + (size_t)(k0 + kc);
     *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
     *reinterpret_cast<uint4 *>(dst + (size_t)Rpad * Kpad + base) = *reinterpret_cast<const uint4 *>(lo);
 }
 
-__global__ void fill_int_kernel(int *p, long long n, int v) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        p[i] = v;
-}
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -498,7 +485,23 @@ struct PackCache {
     std::vector<std::unique_ptr<PackEntry>> cached;
     DBuf<__half> scratch[2];
     DBuf<int> scratch_exp[2];
+    // buffers of dropped entries, reused by later entries (no cudaFree/cudaMalloc per sweep)
+    std::vector<DBuf<__half>> free_planes;
+    std::vector<DBuf<int>> free_exps;
 };
+
+template <class T>
+static DBuf<T> take_buffer(Ctx *ctx, std::vector<DBuf<T>> &pool, size_t need) {
+    int best = -1;
+    for (int i = 0; i < (int)pool.size(); ++i)
+        if (pool[i].n >= need && (best < 0 || pool[i].n < pool[best].n)) best = i;
+    if (best >= 0 && pool[best].n <= 2 * need) {
+        DBuf<T> b = std::move(pool[best]);
+        pool.erase(pool.begin() + best);
+        return b;
+    }
+    return DBuf<T>(ctx, need);
+}
 struct Packed {
     const __half *planes;
     const int *exps;
@@ -506,11 +509,21 @@ struct Packed {
 
 void pack_cache_destroy(PackCache *p) { delete p; }
 void pack_cache_clear(Ctx *ctx) {
-    if (ctx->pack) ctx->pack->cached.clear();
+    if (ctx->pack) {
+        ctx->pack->cached.clear();
+        ctx->pack->free_planes.clear();
+        ctx->pack->free_exps.clear();
+    }
 }
 void pack_cache_drop(Ctx *ctx, const void *ptr) {
     if (!ctx->pack) return;
-    auto &v = ctx->pack->cached;
+    PackCache &pc = *ctx->pack;
+    auto &v = pc.cached;
+    for (auto &e : v)
+        if (e->src == ptr) {
+            pc.free_planes.push_back(std::move(e->buf));
+            pc.free_exps.push_back(std::move(e->exps));
+        }
     v.erase(std::remove_if(v.begin(), v.end(), [&](const std::unique_ptr<PackEntry> &e) { return e->src == ptr; }),
             v.end());
 }
@@ -531,8 +544,8 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     int *ex;
     std::unique_ptr<PackEntry> ent;
     if (cache) {
-        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, DBuf<__half>(ctx, need),
-                                DBuf<int>(ctx, (size_t)nchunk * Rpad)});
+        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, take_buffer(ctx, pc.free_planes, need),
+                                take_buffer(ctx, pc.free_exps, (size_t)nchunk * Rpad)});
         dst = ent->buf.p;
         ex = ent->exps.p;
     } else {
@@ -552,13 +565,9 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     {
         Ctx::Scope s(ctx, "pack_split");
-        fill_int_kernel<<<(unsigned)std::min<long long>((nchunk * Rpad + 255) / 256, 4096), 256, 0,
-                          ctx->stream>>>(ex, nchunk * Rpad, INT_MIN);
-        rowexp_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex);
         pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
                                                                      dst);
         JUES_CHECK_CUDA(cudaGetLastError());
-        ctx->launches += 2;
     }
     if (cache) pc.cached.push_back(std::move(ent));
     return Packed{dst, ex};
@@ -692,12 +701,8 @@ void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     Ctx::Scope s(ctx, "pack_split_noalloc");
-    fill_int_kernel<<<(unsigned)std::min<long long>((nchunk * Rpad + 255) / 256, 4096), 256, 0, ctx->stream>>>(
-        ex, nchunk * Rpad, INT_MIN);
-    rowexp_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex);
     pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex, dst);
     JUES_CHECK_CUDA(cudaGetLastError());
-    ctx->launches += 2;
 }
 }  // namespace
 
@@ -725,7 +730,7 @@ void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
     int *ea = reinterpret_cast<int *>(base + up(planesA) + up(planesB));
     int *eb = reinterpret_cast<int *>(base + up(planesA) + up(planesB) + up(expsA));
     // every byte the kernels read is rewritten here: planes including their zero padding, and
-    // the scales (reset to "all zero" before the row-maximum pass)
+    // every (chunk,row) scale
     pack_into(ctx, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, pa, ea);
     pack_into(ctx, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, pb, eb);
     const CUtensorMap ma = make_map(pa, Mpad, Kpad, TBM);
