@@ -193,6 +193,42 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch_measure(count, local):
+    """Batched MP2 energy + adjoint (one CUDA graph) vs a per-system loop of the same C-ABI calls."""
+    from juesgpu import MollerPlesset
+    from juesgpu.synthetic import batch_specs, make_system
+    t0 = time.perf_counter()
+    systems = []
+    for n, o, naux, sub in batch_specs(count):
+        s = make_system(n, o, naux, seed=sub)
+        systems.append((s.ao_eri(), np.asfortranarray(s.C), o, s.eps))
+    gen_s = time.perf_counter() - t0
+    # per-system launch loop through the single-system adjoint entry point
+    t0 = time.perf_counter()
+    loop = [MollerPlesset.rmp2_adjoint(gao=g, C=C, nocc=o, eps=e, device=local) for g, C, o, e in systems]
+    loop_s = time.perf_counter() - t0
+    # batched: first call plans, autotunes and captures the graph; then timed replays
+    t0 = time.perf_counter()
+    e_b, gbs, cbs, info = MollerPlesset.batch_rmp2(systems, adjoint=True, device=local)
+    first_s = time.perf_counter() - t0
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e_b, gbs, cbs, info = MollerPlesset.batch_rmp2(systems, adjoint=True, device=local)
+    batch_s = (time.perf_counter() - t0) / reps
+    err_e = max(abs(a - b[0]) for a, b in zip(e_b, loop))
+    err_g = max(float(np.abs(gb - b[1]).max()) for gb, b in zip(gbs, loop))
+    err_c = max(float(np.abs(cb - b[2]).max()) for cb, b in zip(cbs, loop))
+    nbf = [g.shape[0] for g, _, _, _ in systems]
+    return {"systems": count, "nbf_range": [min(nbf), max(nbf)], "generate_s": gen_s,
+            "loop_s": loop_s, "loop_systems_per_s": count / loop_s,
+            "batch_first_call_s": first_s, "batch_s": batch_s, "batch_systems_per_s": count / batch_s,
+            "speedup": loop_s / batch_s, "graph_ms": info.graph_ms, "upload_ms": info.upload_ms,
+            "download_ms": info.download_ms, "graph_nodes": info.graph_nodes,
+            "tile_shapes": [info.tile_shape[k] for k in range(info.nstages)],
+            "max_energy_diff_eh": err_e, "max_gao_bar_diff": err_g, "max_C_bar_diff": err_c}
+
+
 def run_gpu(args):
     ws, rank, local, pg = dist_setup(args.gpus)
     import juesgpu
@@ -304,6 +340,7 @@ def run_gpu(args):
                "d2h_bytes_per_step": 8, "sweeps": len(lg), "includes": "H2D of AO ERIs, split transform "
                "of the 5 RCCD blocks, sweeps, energy read-back"}
 
+    batch = run_batch_measure(args.batch, local) if args.batch > 0 else None
     if rank != 0:
         return
     pk, pk_kind = peaks()
@@ -342,6 +379,7 @@ def run_gpu(args):
                      "flops_per_launch": pp_flops_exec, "launch_ms": 1e3 * pp_avg_s if pp_avg_s else None,
                      "traffic": traffic},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+        "batch": batch,
     }
     print(json.dumps(line), flush=True)
 
@@ -357,6 +395,8 @@ def main():
     ap.add_argument("--no-check", dest="check", action="store_false")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=4, help="CPU baseline shares to time")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also measure the batched MP2 energy+adjoint form on this many systems")
     ap.add_argument("--shape", default="S200", choices=sorted(SHAPES),
                     help="S200 is the benchmark; S100 is the small case used for profiler captures")
     args = ap.parse_args()

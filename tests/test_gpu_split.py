@@ -32,9 +32,12 @@ def split_rows(X):
     for c0 in range(0, K, KCH):
         mx = np.abs(X[:, c0:c0 + KCH]).max(axis=1)
         e[:, c0:c0 + KCH] = np.where(mx > 0, np.frexp(mx)[1], 0)[:, None]
-    y = np.ldexp(X, 9 - e)
-    h = np.rint(y)
-    lo = np.rint((y - h) * 1024.0)
+    # q = rint(x 2^(19-e)) with ties away from zero, hi = floor((q + 512) / 1024), lo = q - 1024 hi
+    # (exactly the kernel's integer procedure; the scaling by 2^(19-e) is exact)
+    t = np.ldexp(np.abs(X), 19 - e)
+    q = np.sign(X) * np.floor(t + 0.5)
+    h = np.floor((q + 512.0) / 1024.0)
+    lo = q - 1024.0 * h
     return h, lo, e
 
 
