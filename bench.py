@@ -267,8 +267,14 @@ def run_gpu(args):
     log = sess.log()[n0:]
     dev_s = sum(r[3] for r in log) / 1e3
     pp_ms, pp_n = ctx.profile("ccd_pp_ladder")
+    pp_n -= ctx.profile("ccd_pp_ladder.reduce")[1]      # split-K reductions are not GEMM launches
     ring_ms, ring_n = ctx.profile("ccd_ring")
     pack_ms, pack_n = ctx.profile("pack_split")
+    other_ms = {k: sum(ctx.profile(p)[0] for p in ps) / args.steps
+                for k, ps in (("fae_fmi", ("ccd_fae", "ccd_fmi", "ccd_z_fae", "ccd_z_fmi")),
+                              ("x_hh_ladder", ("ccd_x", "ccd_hh_ladder")),
+                              ("wj_wk", ("ccd_wj", "ccd_wk")),
+                              ("t2_finalize", ("t2_finalize",)))}
     ctx.set_profiling(False)
     dev_s = max_over_ranks(pg, dev_s)
     s_per_iter = dev_s / args.steps
@@ -371,7 +377,7 @@ def run_gpu(args):
         "transform": transform,
         "wall_s_timed": wall, "setup_s": setup_s,
         "kernels_ms_per_step": {"pp_ladder": pp_ms / args.steps, "ring": ring_ms / args.steps,
-                                "pack_split": pack_ms / args.steps},
+                                "pack_split": pack_ms / args.steps, **other_ms},
         "roofline": {"bound": "tensor", "kernel": "ccd_pp_ladder (tcgen05 split-BF16 GEMM)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if achieved else None,

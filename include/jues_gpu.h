@@ -143,6 +143,15 @@ JUES_API int jues_rmp2(jues_ctx *ctx, const double *gao, int n,
               const double *Cocc, int o, const double *Cvir, int v,
               const double *eps, int precision, double *e_out, double *k_out);
 
+/* Density-fitted MP2 (src/MollerPlesset/DF-RMP2.jl:1-46) on the outputs of setup_df
+ * (src/Backend/DF.jl:30-51): pqP[mu,nu,P] (n x n x naux, column-major) and Jpqh = J^-1/2
+ * (naux x naux).  b[mu,nu,Q] = pqP Jpqh (skipped when Jpqh is NULL: pqP is then already b),
+ * B[i,a,Q] = Cocc^T b Cvir, (ia|jb) = sum_Q B[i,a,Q] B[j,b,Q], then the pair sum of jues_rmp2.
+ * The libint/psi4 integrals behind setup_df are not part of this library. */
+JUES_API int jues_df_rmp2(jues_ctx *ctx, const double *pqP, int n, int naux, const double *Jpqh,
+                          const double *Cocc, int o, const double *Cvir, int v, const double *eps,
+                          int precision, double *e_out);
+
 /* MP2 adjoint (no reference counterpart; the differentiation form): E as jues_rmp2 from the
  * full n x n MO matrix C (occupied columns first) and, scaled by e_bar,
  *   gao_bar[mu,nu,lam,sig] = dE/d(mu nu|lam sig)  (n^4, may be NULL)

@@ -300,6 +300,73 @@ int jues_rmp2(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o
     });
 }
 
+int jues_df_rmp2(jues_ctx *ctx, const double *pqP, int n, int naux, const double *Jpqh, const double *Cocc,
+                 int o, const double *Cvir, int v, const double *eps, int precision, double *e_out) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(pqP, "pqP"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(e_out, "e_out");
+        check_dims(n, o, v);
+        if (naux <= 0) throw Error(JUES_EINVAL, "naux must be positive");
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cudaSetDevice(c.device);
+        const long long nn = (long long)n * n, ov = (long long)o * v;
+        DBuf<double> db = h2d(c, pqP, (size_t)(nn * naux));
+        if (Jpqh) {
+            // b[mu,nu,Q] = sum_P pqP[mu,nu,P] Jpqh[P,Q]   (DF.jl:52-57)
+            DBuf<double> dj = h2d(c, Jpqh, (size_t)naux * naux);
+            DBuf<double> fitted(&c, (size_t)(nn * naux));
+            GettArgs a;
+            a.M = nn; a.N = naux; a.K = naux;
+            a.alpha = 1.0; a.beta = 0.0;
+            a.A = db.p; a.mA = plain(1); a.kA = plain(nn);
+            a.B = dj.p; a.kB = plain(1); a.nB = plain(naux);
+            a.C = fitted.p; a.mC = plain(1); a.nC = plain(nn);
+            gett(&c, precision, a, "df_fit");
+            db = std::move(fitted);
+        }
+        DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
+        DBuf<double> de = h2d(c, eps, (size_t)n);
+        // b_inu[i,nu,Q] = sum_mu Cocc[mu,i] b[mu,nu,Q]   (DF-RMP2.jl:17-19)
+        DBuf<double> biv(&c, (size_t)(o * (long long)n * naux));
+        {
+            GettArgs a;
+            a.M = o; a.N = (long long)n * naux; a.K = n;
+            a.alpha = 1.0; a.beta = 0.0;
+            a.A = co.p; a.mA = plain(n); a.kA = plain(1);
+            a.B = db.p; a.kB = plain(1); a.nB = plain(n);
+            a.C = biv.p; a.mC = plain(1); a.nC = plain(o);
+            gett(&c, precision, a, "df_half");
+        }
+        // B[i,a,Q] = sum_nu Cvir[nu,a] b_inu[i,nu,Q]   (DF-RMP2.jl:20-22)
+        DBuf<double> bia(&c, (size_t)(ov * naux));
+        {
+            GettArgs a;
+            a.M = (long long)o * naux; a.N = v; a.K = n;
+            a.alpha = 1.0; a.beta = 0.0;
+            a.A = biv.p; a.mA = mode2(o, 1, (long long)o * n); a.kA = plain(o);
+            a.B = cv.p; a.kB = plain(1); a.nB = plain(n);
+            a.C = bia.p; a.mC = mode2(o, 1, ov); a.nC = plain(o);
+            gett(&c, precision, a, "df_half");
+        }
+        biv.reset();
+        db.reset();
+        // (ia|jb) = sum_Q B[(ia),Q] B[(jb),Q], chemists' [i,a,j,b]   (DF-RMP2.jl:28-34)
+        DBuf<double> K(&c, (size_t)(ov * ov));
+        {
+            GettArgs a;
+            a.M = ov; a.N = ov; a.K = naux;
+            a.alpha = 1.0; a.beta = 0.0;
+            a.A = bia.p; a.mA = plain(1); a.kA = plain(ov);
+            a.B = bia.p; a.kB = plain(ov); a.nB = plain(1);
+            a.C = K.p; a.mC = plain(1); a.nC = plain(ov);
+            gett(&c, precision, a, "df_iajb");
+        }
+        *e_out = mp2_gamma(&c, K.p, de.p, o, v, 1.0, nullptr);   // DF-RMP2.jl:36-42
+        c.check_flags();
+    });
+}
+
 int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, int o, const double *eps,
                       int precision, double e_bar, double *e_out, double *gao_bar, double *C_bar) {
     return guarded([&] {

@@ -84,11 +84,14 @@ struct Ctx {
     double *d_red = nullptr;           // reduction scratch (1 << 16 doubles)
     PackCache *pack = nullptr;         // owned; destroyed by pack_cache_destroy
     BatchCache *batch = nullptr;       // owned; destroyed by batch_cache_destroy
+    void *splitk_ws = nullptr;         // split-K partial sums, grown on demand
+    size_t splitk_bytes = 0;
     Ctx();
     ~Ctx();
 
     void *alloc(size_t bytes);
     void free(void *p, size_t bytes);
+    void *splitk_scratch(size_t bytes);   // stream-ordered reuse: one split-K GEMM at a time
     void sync() { JUES_CHECK_CUDA(cudaStreamSynchronize(stream)); }
     // bracket a launch with profiling events when profiling is on
     struct Scope {
@@ -153,6 +156,14 @@ struct GettArgs {
 
 void gett_f64(Ctx *ctx, const GettArgs &g, const char *name);
 void gett_tc(Ctx *ctx, const GettArgs &g, const char *name);   // split BF16 on tcgen05
+// split-K epilogue: C[mC(m) + nC(n)] = alpha sum_s ws[s sstride + n ld + m] + beta Cin[...],
+// the partials summed in FP64 in split order (deterministic)
+void splitk_reduce(Ctx *ctx, const float *ws, int ks, long long sstride, long long ld, long long M, long long N,
+                   double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
+                   const char *name);
+void splitk_reduce(Ctx *ctx, const double *ws, int ks, long long sstride, long long ld, long long M, long long N,
+                   double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
+                   const char *name);
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
 // split GEMM that packs into a static device array instead of allocating (see gett_tc.cu)
 void gett_tc_noalloc(Ctx *ctx, const GettArgs &g);
@@ -181,7 +192,8 @@ void axpby(Ctx *ctx, size_t n, double a, const double *x, double b, const double
 double dot(Ctx *ctx, size_t n, const double *x, const double *y);
 // MP2: sum K[i,j,a,b](2K[i,j,a,b]-K[i,j,b,a]) / D (K column-major [i,j,a,b])
 double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v);
-// MP2 adjoint seed: G[i,a,j,b] = 2 e_bar (2K[i,a,j,b] - K[i,b,j,a]) / D from chemists' K; returns E
+// MP2 adjoint seed: G[i,a,j,b] = 2 e_bar (2K[i,a,j,b] - K[i,b,j,a]) / D from chemists' K (G may be
+// null: energy only); returns E
 double mp2_gamma(Ctx *ctx, const double *K, const double *eps, int o, int v, double e_bar, double *G);
 // CC energy: sum oovv[i,j,a,b] (2 X[i,j,a,b] - X[j,i,a,b]) with X = T2 (+ t1 t1 when t1)
 double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t1, int o, int v);

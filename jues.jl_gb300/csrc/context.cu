@@ -3,6 +3,8 @@
 
 #include <cstring>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace jues {
@@ -23,6 +25,7 @@ Ctx::~Ctx() {
         for (auto &e : kv.second.pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto &e : kv.second.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
     }
+    if (splitk_ws) cudaFree(splitk_ws);
     if (d_flags) cudaFree(d_flags);
     if (d_red) cudaFree(d_red);
     if (stream) cudaStreamDestroy(stream);
@@ -50,6 +53,19 @@ void Ctx::free(void *p, size_t bytes) {
     if (!p) return;
     cudaFree(p);
     mem_used -= bytes;
+}
+
+void *Ctx::splitk_scratch(size_t bytes) {
+    if (bytes > splitk_bytes) {
+        // cudaFree waits for the device, so no launch still reads the old buffer
+        free(splitk_ws, splitk_bytes);
+        splitk_ws = nullptr;
+        splitk_bytes = 0;
+        const size_t grown = std::max(bytes, (size_t)16 << 20);
+        splitk_ws = alloc(grown);
+        splitk_bytes = grown;
+    }
+    return splitk_ws;
 }
 
 Ctx::Scope::Scope(Ctx *c_, const char *name) : c(c_) {

@@ -7,6 +7,7 @@
 // problems and the grouped (batched) form, whose persistent CTAs walk a tile list that spans
 // many independent problems.
 #include <algorithm>
+#include <string>
 
 #include "common.cuh"
 #include "gett_f64.cuh"
@@ -26,7 +27,8 @@ struct TileSmem {
 };
 
 template <int BM, int BN>
-__device__ __forceinline__ void gett_tile(const GroupProblem &g, long long tile, TileSmem<BM, BN> &sm) {
+__device__ __forceinline__ void gett_tile(const GroupProblem &g, long long tile, TileSmem<BM, BN> &sm,
+                                          long long kbeg, long long kend) {
     constexpr int TM = BM / 16, TN = BN / 16;
     const int tid = threadIdx.x;
     const long long m0 = (tile % g.mtiles) * BM;
@@ -53,14 +55,14 @@ __device__ __forceinline__ void gett_tile(const GroupProblem &g, long long tile,
 #pragma unroll
         for (int j = 0; j < TN; ++j) acc[i][j] = 0.0;
 
-    for (long long k0 = 0; k0 < g.K; k0 += BK) {
+    for (long long k0 = kbeg; k0 < kend; k0 += BK) {
         __syncthreads();
         if (tid < BK) {
             const long long k = k0 + tid;
-            sm.koA[tid] = k < g.K ? mode_off(g.kA, k) : -1;
+            sm.koA[tid] = k < kend ? mode_off(g.kA, k) : -1;
         } else if (tid >= 32 && tid < 32 + BK) {
             const long long k = k0 + tid - 32;
-            sm.koB[tid - 32] = k < g.K ? mode_off(g.kB, k) : -1;
+            sm.koB[tid - 32] = k < kend ? mode_off(g.kB, k) : -1;
         }
         __syncthreads();
         for (int e = tid; e < BM * BK; e += NT) {
@@ -107,7 +109,49 @@ __device__ __forceinline__ void gett_tile(const GroupProblem &g, long long tile,
 template <int BM, int BN>
 __global__ void __launch_bounds__(NT) gett_f64_kernel(GroupProblem g) {
     __shared__ TileSmem<BM, BN> sm;
-    gett_tile<BM, BN>(g, blockIdx.x, sm);
+    gett_tile<BM, BN>(g, blockIdx.x, sm, 0, g.K);
+}
+
+// split-K form: CTA b contracts K range [s kper, min(K, (s+1) kper)), s = b / tiles, of tile
+// b % tiles into the plain column-major partial ws[s] (M x N; g's output modes describe it)
+template <int BM, int BN>
+__global__ void __launch_bounds__(NT) gett_f64_splitk(GroupProblem g, long long tiles, long long kper) {
+    __shared__ TileSmem<BM, BN> sm;
+    const long long s = blockIdx.x / tiles;
+    g.C += s * g.M * g.N;
+    g.Cin = g.C;
+    gett_tile<BM, BN>(g, blockIdx.x % tiles, sm, s * kper, min(g.K, (s + 1) * kper));
+}
+
+template <class T>
+__global__ void splitk_reduce_kernel(const T *__restrict__ ws, int ks, long long sstride, long long ld, long long M,
+                                     long long N, double alpha, double beta, double *C, const double *Cin, Mode mC,
+                                     Mode nC) {
+    const long long total = M * N;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long m = i % M, n = i / M;
+        const T *p = ws + n * ld + m;
+        double acc = 0.0;
+        for (int s = 0; s < ks; ++s) acc += (double)p[s * sstride];
+        const long long off = mode_off(mC, m) + mode_off(nC, n);
+        double v = alpha * acc;
+        if (beta != 0.0) v = fma(beta, Cin[off], v);
+        C[off] = v;
+    }
+}
+
+template <class T>
+void splitk_reduce_t(Ctx *ctx, const T *ws, int ks, long long sstride, long long ld, long long M, long long N,
+                     double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
+                     const char *name) {
+    const long long total = M * N;
+    const long long blocks = std::min<long long>((total + 255) / 256, 152LL * 8);
+    const std::string nm = std::string(name) + ".reduce";
+    Ctx::Scope sc(ctx, nm.c_str());
+    splitk_reduce_kernel<T><<<(unsigned)blocks, 256, 0, ctx->stream>>>(ws, ks, sstride, ld, M, N, alpha, beta, C,
+                                                                      Cin ? Cin : C, mC, nC);
+    JUES_CHECK_CUDA(cudaGetLastError());
 }
 
 // persistent grouped form: problem p owns tiles [tile_start[p], tile_start[p+1])
@@ -121,7 +165,7 @@ __global__ void __launch_bounds__(NT) gett_f64_grouped(const GroupProblem *__res
             const int mid = (lo + hi + 1) >> 1;
             if (probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
         }
-        gett_tile<BM, BN>(probs[lo], t - probs[lo].tile_start, sm);
+        gett_tile<BM, BN>(probs[lo], t - probs[lo].tile_start, sm, 0, probs[lo].K);
     }
 }
 
@@ -190,9 +234,46 @@ void gett_f64(Ctx *ctx, const GettArgs &a, const char *name) {
     g.mtiles = (a.M + 63) / 64;
     const long long tiles = g.mtiles * ((a.N + 63) / 64);
     JUES_REQUIRE(tiles < (1LL << 31), "GEMM too large for one launch");
+    // A grid below four CTAs per SM with a long K splits K (at least 512 per split); the
+    // partials are reduced in FP64 in split order.
+    constexpr long long kTarget = 152LL * 4;
+    if (tiles < kTarget && a.K >= 1024) {
+        const long long want = std::min<long long>((kTarget + tiles - 1) / tiles, a.K / 512);
+        long long kper = (a.K + want - 1) / want;
+        kper = (kper + BK - 1) / BK * BK;
+        const long long ks = (a.K + kper - 1) / kper;
+        if (ks > 1) {
+            double *ws = static_cast<double *>(ctx->splitk_scratch((size_t)(ks * a.M * a.N) * sizeof(double)));
+            GroupProblem p = g;
+            p.C = ws;
+            p.Cin = ws;
+            p.mC = plain(1);
+            p.nC = plain(a.M);
+            p.alpha = 1.0;
+            p.beta = 0.0;
+            {
+                Ctx::Scope s(ctx, name);
+                gett_f64_splitk<64, 64><<<(unsigned)(tiles * ks), NT, 0, ctx->stream>>>(p, tiles, kper);
+                JUES_CHECK_CUDA(cudaGetLastError());
+            }
+            splitk_reduce(ctx, ws, (int)ks, a.M * a.N, a.M, a.M, a.N, a.alpha, a.beta, a.C, g.Cin, a.mC, a.nC, name);
+            return;
+        }
+    }
     Ctx::Scope s(ctx, name);
     gett_f64_kernel<64, 64><<<(unsigned)tiles, NT, 0, ctx->stream>>>(g);
     JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void splitk_reduce(Ctx *ctx, const float *ws, int ks, long long sstride, long long ld, long long M, long long N,
+                   double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
+                   const char *name) {
+    splitk_reduce_t(ctx, ws, ks, sstride, ld, M, N, alpha, beta, C, Cin, mC, nC, name);
+}
+void splitk_reduce(Ctx *ctx, const double *ws, int ks, long long sstride, long long ld, long long M, long long N,
+                   double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
+                   const char *name) {
+    splitk_reduce_t(ctx, ws, ks, sstride, ld, M, N, alpha, beta, C, Cin, mC, nC, name);
 }
 
 const TileShape kTileShapes[kNumTileShapes] = {{64, 64}, {32, 64}, {64, 32}, {32, 32}};

@@ -159,6 +159,13 @@ struct TcArgs {
     const double *Cin;
     Mode mC, nC;
     unsigned *flags;
+    // split-K: CTA b computes tile b % tiles over stages [s kper, min(kblocks, (s+1) kper)),
+    // s = b / tiles.  With ksplit > 1 the tile's FP32 sums go to partial[s][Npad][Mpad]
+    // (rows contiguous) and splitk_reduce applies alpha and beta.
+    long long tiles = 0;
+    int ksplit = 1;
+    int kper = 0;
+    float *partial = nullptr;
 };
 
 // Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-9 drain TMEM (two
@@ -179,6 +186,9 @@ struct TcCfg {
     // instruction descriptor: FP32 accumulate, FP16 A and B (format 0), both K-major,
     // M = 128, N = BN
     static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+    // the same with N = 2 BN: A_hi against the stacked [B_hi; B_lo] rows, writing the main and
+    // correction accumulators (adjacent TMEM columns) in one instruction
+    static constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(2 * BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -202,10 +212,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     float *colsc = reinterpret_cast<float *>(coloff + BN);   // [2][BN] per-chunk column scales
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long mt = blockIdx.x % g.mtiles, nt = blockIdx.x / g.mtiles;
+    const long long tile = blockIdx.x % g.tiles, split = blockIdx.x / g.tiles;
+    const long long mt = tile % g.mtiles, nt = tile / g.mtiles;
     const int m0 = (int)(mt * TBM), n0 = (int)(nt * BN);
-    const int nk = g.kblocks;
+    const int kb0 = (int)split * g.kper;                      // first stage of this split
+    const int nk = min(g.kblocks - kb0, g.kper);              // stages of this split (>= 1)
     const int nchunks = (nk + KC - 1) / KC;
+    const int chunk0 = kb0 / KC;                              // kper is a multiple of KC
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -244,11 +257,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 }
                 uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+                const int kx = (kb0 + kb) * TBK;
                 mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
-                tma_load_3d(st, &mapA, &full[s], kb * TBK, m0, 0);
-                tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kb * TBK, m0, 1);
-                tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kb * TBK, n0, 0);
-                tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kb * TBK, n0, 1);
+                tma_load_3d(st, &mapA, &full[s], kx, m0, 0);
+                tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kx, m0, 1);
+                tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kx, n0, 0);
+                tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kx, n0, 1);
             }
         }
     } else if (warp == 1) {
@@ -274,15 +288,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 uint8_t *st = stages + s * Cfg::STAGE_BYTES;
                 const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
                 const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
-                const uint64_t bl = sw128_desc(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES);
                 const uint32_t dmain = tmem + (uint32_t)(buf * 2 * BN);
                 const uint32_t dcorr = dmain + (uint32_t)BN;
+                // B_lo's rows follow B_hi's in shared memory (B_BYTES = BN 128-byte rows, whole
+                // 8-row swizzle groups) and the correction columns follow the main ones in TMEM,
+                // so hi*hi and hi*lo are one N = 2 BN instruction; lo*hi adds to the correction.
 #pragma unroll
                 for (int kk = 0; kk < TBK / 16; ++kk) {
                     const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
                     const uint32_t acc = (first && kk == 0) ? 0u : 1u;
-                    umma_bf16(dmain, ah + off, bh + off, Cfg::IDESC, acc);
-                    umma_bf16(dcorr, ah + off, bl + off, Cfg::IDESC, acc);
+                    umma_bf16(dmain, ah + off, bh + off, Cfg::IDESC2, acc);
                     umma_bf16(dcorr, al + off, bh + off, Cfg::IDESC, 1u);
                 }
                 umma_commit(&empty[s]);                       // stage s free once these complete
@@ -300,12 +315,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int j = 0; j < HB; ++j) acc[j] = 0.f;
         const long long mrow = (long long)m0 + quarter * 32 + lane;
         bool ok = true;
+        // the scales of chunk c + 1 are loaded while chunk c drains
+        const int *pa = g.expA + (long long)chunk0 * g.expA_ld + mrow;
+        const int *pb = g.expB + (long long)chunk0 * g.expB_ld + n0 + (dt < BN ? dt : 0);
+        int ea_cur = __ldg(pa), eb_cur = __ldg(pb);
         for (int c = 0; c < nchunks; ++c) {
             const int buf = c & 1;
             // column scales of this chunk: 2^e_col, staged once for all drain warps
-            if (dt < BN) {
-                const int eb = g.expB[(long long)c * g.expB_ld + n0 + dt];
-                colsc[buf * BN + dt] = (eb == INT_MIN || eb < -126) ? 0.f : __int_as_float((eb + 127) << 23);
+            if (dt < BN)
+                colsc[buf * BN + dt] = (eb_cur == INT_MIN || eb_cur < -126) ? 0.f : __int_as_float((eb_cur + 127) << 23);
+            int ea_next = 0, eb_next = 0;
+            if (c + 1 < nchunks) {
+                ea_next = __ldg(pa + (long long)(c + 1) * g.expA_ld);
+                eb_next = __ldg(pb + (long long)(c + 1) * g.expB_ld);
             }
             asm volatile("bar.sync 1, %0;" ::"n"(TC_DRAIN) : "memory");
             if (!mbar_wait(&cfull[buf], (uint32_t)(c >> 1) & 1u, abort_flag, g.flags)) {
@@ -315,7 +337,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             __syncwarp();
             tc_fence_after();
-            const int ea = g.expA[(long long)c * g.expA_ld + mrow];
+            const int ea = ea_cur;
+            ea_cur = ea_next;
+            eb_cur = eb_next;
             // row factor 2^(e_row - 18); the column factor comes from shared memory
             const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
             const float *cs = colsc + buf * BN + half * HB;
@@ -338,6 +362,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         if (!ok || *abort_flag) {
             if (lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
+        } else if (g.partial) {
+            // raw partial sums, padded rows and columns included; a warp writes 32 consecutive
+            // floats per column
+            const long long Mpad = g.mtiles * TBM, Npad = (g.tiles / g.mtiles) * BN;
+            float *dst = g.partial + ((long long)split * Npad + n0 + half * HB) * Mpad + mrow;
+#pragma unroll
+            for (int j = 0; j < HB; ++j) dst[(long long)j * Mpad] = acc[j];
         } else if (mrow < g.M) {
             const long long rowoff = mode_off(g.mC, mrow);
 #pragma unroll
@@ -585,9 +616,35 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
         attr_set = true;
     }
+    TcArgs g = t;
+    g.tiles = tiles;
+    if (g.ksplit <= 1) {
+        g.ksplit = 1;
+        g.kper = g.kblocks;
+        g.partial = nullptr;
+    }
+    const long long grid = tiles * g.ksplit;
+    JUES_REQUIRE(grid < (1LL << 31), "too many output tiles");
     Ctx::Scope s(ctx, name);
-    gett_tc_kernel<BN, STAGES, TC_KC><<<(unsigned)tiles, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, t);
+    gett_tc_kernel<BN, STAGES, TC_KC><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
     JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+// Number of K splits for a tile grid that underfills the GPU: the wave count times the stages
+// per split (plus a fixed per-CTA start-up of about five stages) is minimised over splits of
+// at least four stages, and taken when it saves at least 10%.  Grids of two waves or more are
+// left whole.
+static int choose_ksplit(long long tiles, int kblocks) {
+    constexpr long long kSms = 152;
+    if (tiles >= 2 * kSms || kblocks < 8) return 1;
+    auto cost = [&](int ks) {
+        const long long waves = (tiles * ks + kSms - 1) / kSms;
+        return (double)waves * ((kblocks + ks - 1) / ks + 5);
+    };
+    int best = 1;
+    for (int ks = 2; ks <= 256 && ks * 4 <= kblocks; ++ks)
+        if (cost(ks) < cost(best)) best = ks;
+    return cost(best) <= 0.9 * cost(1) ? best : 1;
 }
 
 void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
@@ -653,10 +710,20 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     t.expB_ld = Npad;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
+    const int ks0 = choose_ksplit(tiles, t.kblocks);
+    if (ks0 > 1) {
+        t.kper = (t.kblocks + ks0 - 1) / ks0;
+        t.kper = (t.kper + TC_KC - 1) / TC_KC * TC_KC;
+        t.ksplit = (t.kblocks + t.kper - 1) / t.kper;
+        t.partial = static_cast<float *>(ctx->splitk_scratch((size_t)t.ksplit * Mpad * Npad * sizeof(float)));
+    }
     if (BN == 128)
         launch_tc<128, 3>(ctx, ma, mb, t, tiles, name);
     else
         launch_tc<64, 4>(ctx, ma, mb, t, tiles, name);
+    if (t.ksplit > 1)
+        splitk_reduce(ctx, t.partial, t.ksplit, Mpad * Npad, Mpad, a.M, a.N, a.alpha, a.beta, a.C, t.Cin, a.mC, a.nC,
+                      name);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -240,12 +240,14 @@ __global__ void mp2_gamma_kernel(const double *__restrict__ K, const double *__r
             const double x = K[x_off];
             if (a == b) {
                 acc = fma(x * x, inv, acc);
-                G[x_off] = 2.0 * e_bar * x * inv;
+                if (G) G[x_off] = 2.0 * e_bar * x * inv;
             } else {
                 const double y = K[y_off];
                 acc = fma(x * (2.0 * x - y) + y * (2.0 * y - x), inv, acc);
-                G[x_off] = 2.0 * e_bar * (2.0 * x - y) * inv;
-                G[y_off] = 2.0 * e_bar * (2.0 * y - x) * inv;
+                if (G) {
+                    G[x_off] = 2.0 * e_bar * (2.0 * x - y) * inv;
+                    G[y_off] = 2.0 * e_bar * (2.0 * y - x) * inv;
+                }
             }
         }
     }

@@ -24,6 +24,33 @@ def do_rmp2(refWfn, *, precision: str = "fp64", device: int = 0, doprint: bool =
     return e.value
 
 
+def do_df_rmp2(refWfn, pqP, Jpqh=None, *, precision: str = "fp64", device: int = 0) -> float:
+    """Density-fitted MP2 (src/MollerPlesset/DF-RMP2.jl:1-46).
+
+    ``pqP`` (n x n x naux) and ``Jpqh`` = J^-1/2 (naux x naux) are what ``setup_df``
+    (src/Backend/DF.jl:30-51) returns; the reference builds them from psi4, which this
+    library does not wrap.  With ``Jpqh=None``, ``pqP`` is taken as the fitted b[mu,nu,Q].
+    """
+    b = _lib.f64(pqP)
+    if b.ndim != 3 or b.shape[0] != b.shape[1]:
+        raise ValueError("pqP must be n x n x naux")
+    n, _, naux = b.shape
+    J = None
+    if Jpqh is not None:
+        J = _lib.f64(Jpqh)
+        if J.shape != (naux, naux):
+            raise ValueError("Jpqh must be naux x naux")
+    Co = _lib.f64(refWfn.Cao)
+    Cv = _lib.f64(refWfn.Cav)
+    eps = _lib.f64(refWfn.epsa)
+    e = C.c_double()
+    ctx = _lib.context(device)
+    _lib.check(ctx.lib.jues_df_rmp2(ctx.h, _lib.ptr(b), n, naux, _lib.ptr(J),
+                                    _lib.ptr(Co), Co.shape[1], _lib.ptr(Cv), Cv.shape[1], _lib.ptr(eps),
+                                    _lib.PREC[precision], C.byref(e)))
+    return e.value
+
+
 def rmp2_adjoint(refWfn=None, *, gao=None, C=None, nocc=None, eps=None, e_bar: float = 1.0,
                  want_gao: bool = True, want_C: bool = True, precision: str = "fp64", device: int = 0):
     """(E, dE/dgao * e_bar, dE/dC * e_bar) of the closed-shell MP2 energy.

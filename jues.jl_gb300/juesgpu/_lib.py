@@ -75,6 +75,7 @@ SIGNATURES = {
     "jues_get_eri": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_char_p, C.c_int,
                                C.c_int, C.c_int, DP]),
     "jues_rmp2": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, DP]),
+    "jues_df_rmp2": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP]),
     "jues_rmp2_adjoint": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_double, DP, DP, DP]),
     "jues_batch_rmp2": (C.c_int, [VP, C.c_int, C.POINTER(MP2System), C.c_double, DP, C.POINTER(DP),
                                   C.POINTER(DP), C.POINTER(BatchInfo)]),

@@ -18,4 +18,4 @@ the reference (``RCCD.jl`` einsum vs ``mRCCD.jl`` GEMM, ``RCCSD.jl`` vs
 ``mRCCSD.jl``).
 """
 from .transform import tei_transform, get_eri  # noqa: F401
-from .mp2 import do_rmp2, rmp2_energy  # noqa: F401
+from .mp2 import do_rmp2, rmp2_energy, df_rmp2  # noqa: F401

@@ -38,3 +38,20 @@ def rmp2_energy_loops(K, eps, o):
 def do_rmp2(wfn):
     K = get_eri(wfn, "OOVV")
     return rmp2_energy(K, wfn.epsa, wfn.nalpha)
+
+
+def df_rmp2(wfn, pqP, Jpqh=None):
+    """``do_df_rmp2`` (src/MollerPlesset/DF-RMP2.jl:1-46): b = pqP.Jpqh (:14-16; skipped
+    when Jpqh is None), B_iaQ = Co^T b Cv (:17-22), then per (i, j) the (ia|jb) block and
+    the same pair sum as RMP2 (:23-45)."""
+    o = wfn.nalpha
+    b = pqP if Jpqh is None else np.einsum("pqP,PQ->pqQ", pqP, Jpqh, optimize=True)
+    Bia = np.einsum("mi,mnQ,na->iaQ", wfn.Cao, b, wfn.Cav, optimize=True)
+    eps = wfn.epsa
+    e = 0.0
+    for i in range(o):
+        for j in range(o):
+            bAB = Bia[i] @ Bia[j].T                  # (ia|jb) over a, b
+            D = eps[i] + eps[j] - eps[o:, None] - eps[None, o:]
+            e += float(np.sum(bAB * (2.0 * bAB - bAB.T) / D))
+    return e

@@ -252,3 +252,40 @@ def test_nonfinite_input_is_rejected(jg):
     with pytest.raises(JuESError) as ei:
         mRCCD.do_rccd(w, maxit=3)
     assert ei.value.code == 5
+
+
+# ------------------------------------------------------------------------------ DF-MP2
+def _df_inputs(s, rotate):
+    """pqP, Jpqh for a synthetic system: its integrals are exactly sum_P B_P (x) B_P, so
+    DF-MP2 with the fitted b = B is exact.  ``rotate`` hides b behind an orthogonal Jpqh:
+    pqP = b Q^T and Jpqh = Q give pqP Jpqh = b."""
+    b = np.transpose(s.B, (1, 2, 0))
+    if not rotate:
+        return np.asfortranarray(b), None
+    rng = np.random.default_rng(7)
+    Q, _ = np.linalg.qr(rng.standard_normal((s.naux, s.naux)))
+    return np.asfortranarray(np.einsum("pqQ,PQ->pqP", b, Q)), np.asfortranarray(Q)
+
+
+@pytest.mark.parametrize("name,rotate", [("S25", False), ("S25", True), ("S100", True)])
+def test_df_rmp2_equals_conventional_on_exact_factorisation(jg, name, rotate):
+    # TestMollerPlesset.jl:38-39 checks the DF form against the same molecule's MP2
+    s = make_named(name)
+    pqP, Jpqh = _df_inputs(s, rotate)
+    w = s.wfn()
+    e_df = jg.MollerPlesset.do_df_rmp2(w, pqP, Jpqh)
+    ref = golden()[name]["mp2"]
+    assert abs(e_df - ref) < 1e-10 * max(1.0, abs(ref))
+    if name == "S25":
+        assert abs(e_df - oracle.df_rmp2(w, pqP, Jpqh)) < 1e-12
+    e_split = jg.MollerPlesset.do_df_rmp2(w, pqP, Jpqh, precision="split_bf16")
+    assert abs(e_split - ref) < 1e-6
+
+
+def test_df_rmp2_rejects_bad_shapes(jg):
+    s = make_named("S25")
+    w = s.wfn()
+    with pytest.raises(ValueError):
+        jg.MollerPlesset.do_df_rmp2(w, np.zeros((25, 24, 75)))
+    with pytest.raises(ValueError):
+        jg.MollerPlesset.do_df_rmp2(w, np.zeros((25, 25, 75)), np.zeros((75, 74)))

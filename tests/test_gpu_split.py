@@ -148,3 +148,23 @@ def test_rccsd_split(lib):
     e = RCCSD.do_rccsd(make_named("S25").wfn(), maxit=60, diis=True, r_conv=1e-9,
                        precision="split_bf16", refine=2)
     assert abs(e - ref) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split_bf16"])
+@pytest.mark.parametrize("M,N,K", [(40, 40, 200000), (160, 96, 64000), (300, 200, 4096)])
+def test_gemm_split_k(lib, precision, M, N, K):
+    # small outputs with long contractions (the Fmi / Fae intermediates) are split over K and
+    # reduced in FP64; alpha, beta and a transposed operand go through the reduction epilogue
+    rng = np.random.default_rng(M * N + K)
+    A = rng.normal(size=(K, M))
+    B = rng.normal(size=(K, N))
+    C0 = rng.normal(size=(M, N))
+    got = lib.gemm(A, B, C0, alpha=-0.5, beta=0.25, transA=True, precision=precision)
+    exact = -0.5 * (A.T @ B) + 0.25 * C0
+    if precision == "fp64":
+        assert np.allclose(got, exact, rtol=1e-12, atol=1e-11 * np.sqrt(K))
+    else:
+        rel = np.linalg.norm(got - exact) / np.linalg.norm(0.5 * (A.T @ B))
+        assert rel < 1e-5
+    again = lib.gemm(A, B, C0, alpha=-0.5, beta=0.25, transA=True, precision=precision)
+    assert np.array_equal(got, again)   # the split order is fixed: bitwise reproducible

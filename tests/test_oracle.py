@@ -164,3 +164,16 @@ def test_synthetic_generator_is_deterministic_and_symmetric():
     assert np.allclose(g, np.transpose(g, (2, 3, 0, 1)))
     assert np.allclose(a.C.T @ a.C, np.eye(12), atol=1e-13)
     assert np.all(np.diff(a.eps[:3]) >= 0) and np.all(np.diff(a.eps[3:]) >= 0)
+
+
+def test_df_rmp2_oracle_equals_conventional_on_exact_factorisation():
+    # the synthetic integrals are exactly B^T B, so DF-MP2 (DF-RMP2.jl:1-46) with b = B,
+    # or with b hidden behind an orthogonal J^-1/2, equals conventional MP2
+    s = make_named("S25")
+    w = s.wfn()
+    b = np.transpose(s.B, (1, 2, 0))
+    e = oracle.do_rmp2(w)
+    assert abs(oracle.df_rmp2(w, b) - e) < 1e-12
+    Q, _ = np.linalg.qr(np.random.default_rng(7).standard_normal((s.naux, s.naux)))
+    pqP = np.einsum("pqQ,PQ->pqP", b, Q)
+    assert abs(oracle.df_rmp2(w, pqP, Q) - e) < 1e-12
