@@ -229,6 +229,40 @@ def run_batch_measure(count, local):
             "max_energy_diff_eh": err_e, "max_gao_bar_diff": err_g, "max_C_bar_diff": err_c}
 
 
+def run_pT_measure(shape, local, precisions=("fp64", "split_bf16")):
+    """(T) correction (jues_cc_pT) on a CCSD session's amplitudes after 8 DIIS sweeps."""
+    from juesgpu.CoupledCluster import CCSession
+    from juesgpu.synthetic import make_named
+    import juesgpu
+    w = make_named(shape).wfn()
+    o, v = w.nalpha, w.Cav.shape[1]
+    ses = CCSession(1, w, maxit=8, diis=True, r_conv=0.0, device=local, precision="split_bf16",
+                    transform_precision="fp64")
+    ses.iterate(8)
+    ctx = juesgpu.context(local)
+    flops = 2.0 * v**3 * (v + o) * o * (o + 1) * (o + 2)
+    out = {"workload": f"pT_{shape.lower()}", "nbf": w.Cao.shape[0], "nocc": o, "nvir": v,
+           "flops_algorithmic": flops}
+    for prec in precisions:
+        ses.pT(prec)                       # warm-up (plans, packs, allocations)
+        ctx.set_profiling(True)
+        ctx.profile_reset()
+        t0 = time.perf_counter()
+        e = ses.pT(prec)
+        wall = time.perf_counter() - t0
+        w_ms, w_n = ctx.profile("pt_w")
+        en_ms, _ = ctx.profile("pt_energy")
+        pk_ms, _ = ctx.profile("pack_split")
+        ctx.set_profiling(False)
+        out[prec] = {"energy": e, "wall_s": wall, "gemm_ms": w_ms, "gemm_launches": w_n, "energy_ms": en_ms,
+                     "pack_ms": pk_ms, "tflops_algorithmic_wall": flops / wall / 1e12}
+    if "fp64" in out and "split_bf16" in out:
+        out["split_minus_fp64_eh"] = out["split_bf16"]["energy"] - out["fp64"]["energy"]
+        out["speedup"] = out["fp64"]["wall_s"] / out["split_bf16"]["wall_s"]
+    ses.close()
+    return out
+
+
 def run_gpu(args):
     ws, rank, local, pg = dist_setup(args.gpus)
     import juesgpu
@@ -347,6 +381,7 @@ def run_gpu(args):
                "of the 5 RCCD blocks, sweeps, energy read-back"}
 
     batch = run_batch_measure(args.batch, local) if args.batch > 0 else None
+    pT = run_pT_measure(args.pT_shape, local) if args.pT_shape != "none" else None
     if rank != 0:
         return
     pk, pk_kind = peaks()
@@ -385,7 +420,7 @@ def run_gpu(args):
                      "flops_per_launch": pp_flops_exec, "launch_ms": 1e3 * pp_avg_s if pp_avg_s else None,
                      "traffic": traffic},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
-        "batch": batch,
+        "batch": batch, "pT": pT,
     }
     print(json.dumps(line), flush=True)
 
@@ -401,6 +436,8 @@ def main():
     ap.add_argument("--no-check", dest="check", action="store_false")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=4, help="CPU baseline shares to time")
+    ap.add_argument("--pT-shape", dest="pT_shape", default="S100", choices=["none"] + sorted(SHAPES),
+                    help="(T) correction timing on this synthetic shape (FP64 and split)")
     ap.add_argument("--batch", type=int, default=0,
                     help="also measure the batched MP2 energy+adjoint form on this many systems")
     ap.add_argument("--shape", default="S200", choices=sorted(SHAPES),

@@ -55,6 +55,10 @@ extern "C" {
 #define JUES_GUESS_MP2 1   /* T2 = <ij|ab>/D (mRCCSD.jl:66)                                  */
 #define JUES_GUESS_OVOV 2  /* T2 = (ij|ab)/D (RCCD.jl:145-160)                               */
 
+/* DF-RCCD equation variants */
+#define JUES_DF_REFERENCE 0  /* as DF-RCCD.jl: WmBeJ's last term reads (me|nf) T[n,j,f,b]     */
+#define JUES_DF_RCCD      1  /* as RCCD.jl on the fitted integrals: (ne|mf) T[n,j,f,b]         */
+
 typedef struct jues_ctx jues_ctx;
 typedef struct jues_cc jues_cc;
 
@@ -201,12 +205,40 @@ JUES_API int jues_rccsd(jues_ctx *ctx, const double *gao, int n,
                const jues_cc_opts *opts, double *e_out, double *t1_out, double *t2_out,
                jues_iter_log *log, int log_cap, int *niter);
 
+/* (T) energy correction, PerturbativeTriples.compute_pT (src/CoupledCluster/
+ * PerturbativeTriples.jl:35-138).  Host arrays, column-major, chemists' notation as the
+ * reference takes them: T1[i,a] (o x v), T2[i,j,a,b] (o x o x v x v), Vvvvo[a,b,c,i] = (ab|ci)
+ * (v x v x v x o), Vvooo[a,i,j,k] = (ai|jk) (v x o x o x o), Vvovo[a,i,b,j] = (ai|bj)
+ * (v x o x v x o); fo (o) and fv (v) the Fock diagonals.  precision selects the arithmetic of
+ * the W contractions (the energy sum is FP64). */
+JUES_API int jues_pT(jues_ctx *ctx, const double *T1, const double *T2, const double *Vvvvo,
+               const double *Vvooo, const double *Vvovo, const double *fo, const double *fv, int o,
+               int v, int precision, double *e_out);
+/* (T) on a CCSD session's current amplitudes and resident blocks, with fo, fv = eps
+ * (AutoRCCSD.jl:294-299 with canonical orbitals). */
+JUES_API int jues_cc_pT(jues_cc *cc, int precision, double *e_out);
+
+/* Density-fitted CCD, DFRCCD.do_df_rccd (src/CoupledCluster/DF-RCCD.jl:11-54).  pqP[mu,nu,P]
+ * and Jpqh as for jues_df_rmp2.  The four MO factors (DF-RCCD.jl:78-89) build the five blocks
+ * once; the sweep is jues_rccd's.  The reference's own settings are guess = JUES_GUESS_MP2
+ * (T2 = (ia|jb)/D, DF-RCCD.jl:119-137), diis = 0, r_conv = 0, maxit = 40.  variant selects
+ * DF-RCCD.jl's WmBeJ (JUES_DF_REFERENCE) or RCCD.jl's (JUES_DF_RCCD). */
+JUES_API int jues_df_rccd(jues_ctx *ctx, const double *pqP, int n, int naux, const double *Jpqh,
+               const double *Cocc, int o, const double *Cvir, int v, const double *eps,
+               const jues_cc_opts *opts, int variant, double *e_out, double *t2_out,
+               jues_iter_log *log, int log_cap, int *niter);
+
 /* Resident CC sessions: integrals and amplitudes stay in device memory between calls, so
  * a caller can time single sweeps.  method: 0 = CCD, 1 = CCSD.  gao_is_device != 0 means
  * gao is a device pointer on the context's device. */
 JUES_API int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_device, int n,
                    const double *Cocc, int o, const double *Cvir, int v, const double *eps,
                    const jues_cc_opts *opts, jues_cc **out);
+/* The same session for CCD on density-fitted integrals (DF-RCCD.jl:11-54): pqP and Jpqh as for
+ * jues_df_rmp2 (pqP_is_device != 0: pqP is a device pointer), variant JUES_DF_*. */
+JUES_API int jues_cc_create_df(jues_ctx *ctx, const double *pqP, int pqP_is_device, int n, int naux,
+                   const double *Jpqh, const double *Cocc, int o, const double *Cvir, int v,
+                   const double *eps, const jues_cc_opts *opts, int variant, jues_cc **out);
 /* Run up to nsweeps sweeps (stopping early on convergence); *done = sweeps run,
  * *converged = 1 if the thresholds were met. */
 JUES_API int jues_cc_iterate(jues_cc *cc, int nsweeps, int *done, int *converged);

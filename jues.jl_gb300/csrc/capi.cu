@@ -4,6 +4,8 @@
 #include <string>
 
 #include "cc.cuh"
+#include "df.cuh"
+#include "triples.cuh"
 #include "common.cuh"
 #include "transform.cuh"
 
@@ -76,6 +78,26 @@ struct jues_cc {
     CCState *s = nullptr;
     ~jues_cc() { delete s; }
 };
+
+// the fitted factor b = pqP Jpqh on the device (pqP itself when Jpqh is null), DF.jl:52-57
+static DBuf<double> fitted_factor(Ctx &c, const double *pqP, int pqP_is_device, int n, int naux,
+                                  const double *Jpqh, int precision) {
+    const size_t nb = (size_t)n * n * naux;
+    DBuf<double> host_copy;
+    const double *src = pqP;
+    if (!pqP_is_device) {
+        host_copy = h2d(c, pqP, nb);
+        src = host_copy.p;
+    }
+    if (Jpqh) {
+        DBuf<double> dj = h2d(c, Jpqh, (size_t)naux * naux);
+        return df_fit(&c, precision, src, n, naux, dj.p);
+    }
+    if (!pqP_is_device) return host_copy;
+    DBuf<double> b(&c, nb);
+    JUES_CHECK_CUDA(cudaMemcpyAsync(b.p, pqP, nb * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    return b;
+}
 
 extern "C" {
 
@@ -310,47 +332,14 @@ int jues_df_rmp2(jues_ctx *ctx, const double *pqP, int n, int naux, const double
         if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
-        const long long nn = (long long)n * n, ov = (long long)o * v;
-        DBuf<double> db = h2d(c, pqP, (size_t)(nn * naux));
-        if (Jpqh) {
-            // b[mu,nu,Q] = sum_P pqP[mu,nu,P] Jpqh[P,Q]   (DF.jl:52-57)
-            DBuf<double> dj = h2d(c, Jpqh, (size_t)naux * naux);
-            DBuf<double> fitted(&c, (size_t)(nn * naux));
-            GettArgs a;
-            a.M = nn; a.N = naux; a.K = naux;
-            a.alpha = 1.0; a.beta = 0.0;
-            a.A = db.p; a.mA = plain(1); a.kA = plain(nn);
-            a.B = dj.p; a.kB = plain(1); a.nB = plain(naux);
-            a.C = fitted.p; a.mC = plain(1); a.nC = plain(nn);
-            gett(&c, precision, a, "df_fit");
-            db = std::move(fitted);
-        }
+        const long long ov = (long long)o * v;
+        DBuf<double> b = fitted_factor(c, pqP, 0, n, naux, Jpqh, precision);
         DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
         DBuf<double> de = h2d(c, eps, (size_t)n);
-        // b_inu[i,nu,Q] = sum_mu Cocc[mu,i] b[mu,nu,Q]   (DF-RMP2.jl:17-19)
-        DBuf<double> biv(&c, (size_t)(o * (long long)n * naux));
-        {
-            GettArgs a;
-            a.M = o; a.N = (long long)n * naux; a.K = n;
-            a.alpha = 1.0; a.beta = 0.0;
-            a.A = co.p; a.mA = plain(n); a.kA = plain(1);
-            a.B = db.p; a.kB = plain(1); a.nB = plain(n);
-            a.C = biv.p; a.mC = plain(1); a.nC = plain(o);
-            gett(&c, precision, a, "df_half");
-        }
-        // B[i,a,Q] = sum_nu Cvir[nu,a] b_inu[i,nu,Q]   (DF-RMP2.jl:20-22)
+        // B[i,a,Q] = sum_{mu,nu} Cocc[mu,i] b[mu,nu,Q] Cvir[nu,a]   (DF-RMP2.jl:17-22)
         DBuf<double> bia(&c, (size_t)(ov * naux));
-        {
-            GettArgs a;
-            a.M = (long long)o * naux; a.N = v; a.K = n;
-            a.alpha = 1.0; a.beta = 0.0;
-            a.A = biv.p; a.mA = mode2(o, 1, (long long)o * n); a.kA = plain(o);
-            a.B = cv.p; a.kB = plain(1); a.nB = plain(n);
-            a.C = bia.p; a.mC = mode2(o, 1, ov); a.nC = plain(o);
-            gett(&c, precision, a, "df_half");
-        }
-        biv.reset();
-        db.reset();
+        df_mo_factor(&c, precision, b.p, n, naux, co.p, o, cv.p, v, bia.p);
+        b.reset();
         // (ia|jb) = sum_Q B[(ia),Q] B[(jb),Q], chemists' [i,a,j,b]   (DF-RMP2.jl:28-34)
         DBuf<double> K(&c, (size_t)(ov * ov));
         {
@@ -491,6 +480,30 @@ int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_devi
     });
 }
 
+int jues_cc_create_df(jues_ctx *ctx, const double *pqP, int pqP_is_device, int n, int naux, const double *Jpqh,
+                      const double *Cocc, int o, const double *Cvir, int v, const double *eps,
+                      const jues_cc_opts *opts, int variant, jues_cc **out) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(pqP, "pqP"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(out, "out");
+        *out = nullptr;
+        check_dims(n, o, v);
+        if (naux <= 0) throw Error(JUES_EINVAL, "naux must be positive");
+        if (variant != JUES_DF_REFERENCE && variant != JUES_DF_RCCD) throw Error(JUES_EINVAL, "unknown DF variant");
+        jues_cc_opts op;
+        if (opts) op = *opts; else jues_cc_default_opts(&op);
+        check_opts(op);
+        cudaSetDevice(c.device);
+        const int iprec = op.transform_precision >= 0 ? op.transform_precision : op.precision;
+        DBuf<double> b = fitted_factor(c, pqP, pqP_is_device, n, naux, Jpqh, iprec);
+        DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
+        DBuf<double> de = h2d(c, eps, (size_t)n);
+        std::unique_ptr<jues_cc> cc(new jues_cc());
+        cc->s = cc_create_df(&c, b.p, n, naux, co.p, o, cv.p, v, de.p, op, variant == JUES_DF_REFERENCE);
+        *out = cc.release();
+    });
+}
+
 int jues_cc_iterate(jues_cc *cc, int nsweeps, int *done, int *converged) {
     return guarded([&] {
         need(cc, "cc");
@@ -543,12 +556,10 @@ int jues_cc_destroy(jues_cc *cc) {
     });
 }
 
-static int cc_solve(jues_ctx *ctx, int method, const double *gao, int n, const double *Cocc, int o,
-                    const double *Cvir, int v, const double *eps, const jues_cc_opts *opts, double *e_out,
-                    double *t1_out, double *t2_out, jues_iter_log *log, int log_cap, int *niter) {
-    jues_cc *cc = nullptr;
-    int st = jues_cc_create(ctx, method, gao, 0, n, Cocc, o, Cvir, v, eps, opts, &cc);
-    if (st) return st;
+// runs a created session to completion and fills the outputs
+static int cc_run(jues_cc *cc, const jues_cc_opts *opts, double *e_out, double *t1_out, double *t2_out,
+                  jues_iter_log *log, int log_cap, int *niter) {
+    int st = 0;
     jues_cc_opts op;
     if (opts) op = *opts; else jues_cc_default_opts(&op);
     int done = 0, conv = 0;
@@ -563,6 +574,63 @@ static int cc_solve(jues_ctx *ctx, int method, const double *gao, int n, const d
         st = JUES_ENOTCONV;
     }
     return st;
+}
+
+int jues_pT(jues_ctx *ctx, const double *T1, const double *T2, const double *Vvvvo, const double *Vvooo,
+            const double *Vvovo, const double *fo, const double *fv, int o, int v, int precision, double *e_out) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(T1, "T1"); need(T2, "T2"); need(Vvvvo, "Vvvvo"); need(Vvooo, "Vvooo"); need(Vvovo, "Vvovo");
+        need(fo, "fo"); need(fv, "fv"); need(e_out, "e_out");
+        if (o <= 0 || v <= 0) throw Error(JUES_EINVAL, "need o > 0 and v > 0");
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cudaSetDevice(c.device);
+        const size_t O = (size_t)o, V = (size_t)v;
+        DBuf<double> t1 = h2d(c, T1, O * V), t2 = h2d(c, T2, O * O * V * V);
+        DBuf<double> vv = h2d(c, Vvvvo, V * V * V * O), vo = h2d(c, Vvooo, V * O * O * O);
+        DBuf<double> vvo = h2d(c, Vvovo, V * O * V * O);
+        DBuf<double> dfo = h2d(c, fo, O), dfv = h2d(c, fv, V);
+        *e_out = pT_energy(&c, precision, t1.p, t2.p, col_major(vv.p, v, v, v), col_major(vo.p, v, o, o),
+                           col_major(vvo.p, v, o, v), dfo.p, dfv.p, o, v);
+    });
+}
+
+int jues_cc_pT(jues_cc *cc, int precision, double *e_out) {
+    return guarded([&] {
+        need(cc, "cc"); need(e_out, "e_out");
+        CCState *s = cc->s;
+        if (s->method != 1) throw Error(JUES_EINVAL, "(T) needs a CCSD session");
+        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+            throw Error(JUES_EINVAL, "unknown precision");
+        cudaSetDevice(s->ctx->device);
+        const long long o = s->o, v = s->v, oo = o * o, ov = o * v;
+        // AutoRCCSD.jl:295-297 as strided views of the physicists' blocks:
+        // Vvvvo[a,b,c,i] = ovvv[i,b,c,a], Vvooo[a,j,i,k] = ooov[i,j,k,a], Vvovo[a,i,b,j] = oovv[i,j,a,b]
+        View4 vv, vo, vvo;
+        vv.p = s->ovvv.p; vv.s[0] = ov * v; vv.s[1] = o; vv.s[2] = ov; vv.s[3] = 1;
+        vo.p = s->ooov.p; vo.s[0] = oo * o; vo.s[1] = o; vo.s[2] = 1; vo.s[3] = oo;
+        vvo.p = s->oovv.p; vvo.s[0] = oo; vvo.s[1] = 1; vvo.s[2] = oo * v; vvo.s[3] = o;
+        *e_out = pT_energy(s->ctx, precision, s->t1.p, s->T.p, vv, vo, vvo, s->eps.p, s->eps.p + o, (int)o, (int)v);
+    });
+}
+
+static int cc_solve(jues_ctx *ctx, int method, const double *gao, int n, const double *Cocc, int o,
+                    const double *Cvir, int v, const double *eps, const jues_cc_opts *opts, double *e_out,
+                    double *t1_out, double *t2_out, jues_iter_log *log, int log_cap, int *niter) {
+    jues_cc *cc = nullptr;
+    int st = jues_cc_create(ctx, method, gao, 0, n, Cocc, o, Cvir, v, eps, opts, &cc);
+    if (st) return st;
+    return cc_run(cc, opts, e_out, t1_out, t2_out, log, log_cap, niter);
+}
+
+int jues_df_rccd(jues_ctx *ctx, const double *pqP, int n, int naux, const double *Jpqh, const double *Cocc, int o,
+                 const double *Cvir, int v, const double *eps, const jues_cc_opts *opts, int variant, double *e_out,
+                 double *t2_out, jues_iter_log *log, int log_cap, int *niter) {
+    jues_cc *cc = nullptr;
+    int st = jues_cc_create_df(ctx, pqP, 0, n, naux, Jpqh, Cocc, o, Cvir, v, eps, opts, variant, &cc);
+    if (st) return st;
+    return cc_run(cc, opts, e_out, nullptr, t2_out, log, log_cap, niter);
 }
 
 int jues_rccd(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o, const double *Cvir, int v,

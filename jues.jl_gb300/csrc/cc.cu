@@ -15,6 +15,7 @@
 #include <cstring>
 
 #include "cc.cuh"
+#include "df.cuh"
 #include "transform.cuh"
 
 namespace jues {
@@ -94,8 +95,13 @@ double ccd_sweep(CCState *s, int prec) {
     // WJ = WmBeJ = ovvo + 1/2 oovv[m,n,e,f] T~[n,j,f,b] - 1/2 oovv[n,m,e,f] T[n,j,f,b]  (RCCD.jl:400)
     G(s, prec, "ccd_wj", ov, ov, ov, 0.5, W, mode2(o, 1, oo), mode2(o, o, oov), Tt, mode2(o, 1, oo),
       mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p);
-    G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
-      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
+    if (s->reference_df_wmbej)
+        // DF-RCCD.jl:239-242 reads the last term as oovv[m,n,e,f] T[n,j,f,b] (bov[m,e]bov[n,f])
+        G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, 1, oo), mode2(o, o, oov), T, mode2(o, 1, oo),
+          mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
+    else
+        G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
+          mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
     // WK = WmBEj = -ovov[m,b,j,e] + 1/2 T[j,n,f,b] oovv[n,m,e,f]                  (RCCD.jl:445)
     G(s, prec, "ccd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
       mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p);
@@ -211,8 +217,9 @@ static void diis_step(CCState *s, double *x, const double *xn, size_t len) {
 // ---------------------------------------------------------------------------------------
 // set-up
 // ---------------------------------------------------------------------------------------
-CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *Cocc, int o,
-                   const double *Cvir, int v, const double *eps_dev, const jues_cc_opts &opts) {
+// validated state with its dimensions, options and orbital energies; no blocks yet
+static std::unique_ptr<CCState> cc_begin(Ctx *ctx, int method, int n, int o, int v, const double *eps_dev,
+                                         const jues_cc_opts &opts) {
     JUES_REQUIRE(method == 0 || method == 1, "method must be 0 (CCD) or 1 (CCSD)");
     JUES_REQUIRE(n > 0 && o > 0 && v > 0 && o + v <= n, "need 0 < nocc, 0 < nvir, nocc + nvir <= nbf");
     JUES_REQUIRE(opts.maxit >= 0, "maxit must be >= 0");
@@ -226,30 +233,18 @@ CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *C
     s->n = n; s->o = o; s->v = v;
     s->opts = opts;
     s->precision = opts.precision;
-    const long long oo = (long long)o * o, vv = (long long)v * v, ov = (long long)o * v;
-    const size_t t2n = (size_t)(oo * vv);
     s->eps = DBuf<double>(ctx, n);
     d2d(ctx, s->eps.p, eps_dev, n);
-    // integral blocks (mRCCD.jl:120-127, mRCCSD.jl:102-110), physicists' notation
-    const int iprec = opts.transform_precision >= 0 ? opts.transform_precision : opts.precision;
-    s->oovv = DBuf<double>(ctx, t2n);
-    s->ovov = DBuf<double>(ctx, t2n);
-    s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));
-    s->vvvv = DBuf<double>(ctx, (size_t)(vv * vv));
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOVV", true, 0, s->oovv.p, true);
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVOV", true, 0, s->ovov.p, true);
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOOO", true, 0, s->oooo.p, true);
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "VVVV", true, 0, s->vvvv.p, true);
-    if (method == 0) {
-        s->ovvo = DBuf<double>(ctx, t2n);
-        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVVO", true, 0, s->ovvo.p, true);
-    } else {
-        s->ooov = DBuf<double>(ctx, (size_t)(oo * ov));
-        s->ovvv = DBuf<double>(ctx, (size_t)(ov * vv));
-        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ooov", true, 0, s->ooov.p, true);
-        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ovvv", true, 0, s->ovvv.p, true);
-    }
-    pack_cache_drop(ctx, g);
+    return s;
+}
+
+// ring seeds, work arrays, the initial amplitudes and their energy
+static CCState *cc_finish(std::unique_ptr<CCState> s) {
+    Ctx *ctx = s->ctx;
+    const int method = s->method, o = s->o, v = s->v;
+    const jues_cc_opts &opts = s->opts;
+    const long long oo = (long long)o * o, vv = (long long)v * v, ov = (long long)o * v;
+    const size_t t2n = (size_t)(oo * vv);
     // ring seeds in (me),(bj) layout: ovvoJ[(me),(bj)] = ovvo[m,b,e,j] (CCD) or, for CCSD,
     // the same value read from oovv[m,j,e,b] (= <mj|eb> = (me|jb), as mRCCSD.jl:187 does);
     // ovovK[(me),(bj)] = -ovov[m,b,j,e]
@@ -303,6 +298,57 @@ CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *C
     diis_reset(s.get());
     ctx->check_flags();
     return s.release();
+}
+
+
+CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *Cocc, int o,
+                   const double *Cvir, int v, const double *eps_dev, const jues_cc_opts &opts) {
+    std::unique_ptr<CCState> s = cc_begin(ctx, method, n, o, v, eps_dev, opts);
+    const long long oo = (long long)o * o, vv = (long long)v * v, ov = (long long)o * v;
+    const size_t t2n = (size_t)(oo * vv);
+    // integral blocks (mRCCD.jl:120-127, mRCCSD.jl:102-110), physicists' notation
+    const int iprec = opts.transform_precision >= 0 ? opts.transform_precision : opts.precision;
+    s->oovv = DBuf<double>(ctx, t2n);
+    s->ovov = DBuf<double>(ctx, t2n);
+    s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));
+    s->vvvv = DBuf<double>(ctx, (size_t)(vv * vv));
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOVV", true, 0, s->oovv.p, true);
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVOV", true, 0, s->ovov.p, true);
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOOO", true, 0, s->oooo.p, true);
+    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "VVVV", true, 0, s->vvvv.p, true);
+    if (method == 0) {
+        s->ovvo = DBuf<double>(ctx, t2n);
+        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVVO", true, 0, s->ovvo.p, true);
+    } else {
+        s->ooov = DBuf<double>(ctx, (size_t)(oo * ov));
+        s->ovvv = DBuf<double>(ctx, (size_t)(ov * vv));
+        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ooov", true, 0, s->ooov.p, true);
+        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ovvv", true, 0, s->ovvv.p, true);
+    }
+    pack_cache_drop(ctx, g);
+    return cc_finish(std::move(s));
+}
+
+CCState *cc_create_df(Ctx *ctx, const double *b, int n, int naux, const double *Cocc, int o, const double *Cvir, int v,
+                      const double *eps_dev, const jues_cc_opts &opts, bool reference_wmbej) {
+    JUES_REQUIRE(naux > 0, "naux must be positive");
+    std::unique_ptr<CCState> s = cc_begin(ctx, 0, n, o, v, eps_dev, opts);
+    s->reference_df_wmbej = reference_wmbej;
+    const long long oo = (long long)o * o, vv = (long long)v * v;
+    const size_t t2n = (size_t)(oo * vv);
+    // DF-RCCD.jl:78-89: the four MO factors, then the five blocks the sweep reads, each once
+    const int iprec = opts.transform_precision >= 0 ? opts.transform_precision : opts.precision;
+    {
+        DfFactors f = df_factors(ctx, iprec, b, n, naux, Cocc, o, Cvir, v, true);
+        s->oovv = DBuf<double>(ctx, t2n);
+        s->ovov = DBuf<double>(ctx, t2n);
+        s->ovvo = DBuf<double>(ctx, t2n);
+        s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));
+        s->vvvv = DBuf<double>(ctx, (size_t)(vv * vv));
+        df_blocks(ctx, iprec, f, s->oovv.p, s->ovov.p, s->ovvo.p, s->oooo.p, s->vvvv.p);
+    }
+    pack_cache_clear(ctx);
+    return cc_finish(std::move(s));
 }
 
 // amplitude vector for DIIS: CCD = T2; CCSD = [t1; T2] packed in aux1

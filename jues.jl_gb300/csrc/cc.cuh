@@ -31,12 +31,18 @@ struct CCState {
     int refine_left = -1;
     bool cache_operands = false;   // keep split packs of sweep operands (CCD only)   // split precision: closing FP64 sweeps left (-1 = not started)
     bool converged = false;
+    bool reference_df_wmbej = false;   // DF-RCCD.jl's index order in WmBeJ's last term
     std::vector<jues_iter_log> log;
     double sweep_flops(int prec) const;
 };
 
 CCState *cc_create(Ctx *ctx, int method, const double *gao_dev, int n, const double *Cocc_dev, int o,
                    const double *Cvir_dev, int v, const double *eps_dev, const jues_cc_opts &opts);
+// CCD on density-fitted integrals: b[mu,nu,Q] (device, n x n x naux) is the fitted factor
+// (DF-RCCD.jl:11-54); the five blocks are built from its MO factors and kept resident
+CCState *cc_create_df(Ctx *ctx, const double *b, int n, int naux, const double *Cocc_dev, int o,
+                      const double *Cvir_dev, int v, const double *eps_dev, const jues_cc_opts &opts,
+                      bool reference_wmbej);
 void cc_iterate(CCState *s, int nsweeps, int *done, int *converged);
 void cc_amplitudes(CCState *s, double *t1_host, double *t2_host);
 // one CCD / CCSD sweep: Tn from T (and t1n from t1), returns the squared step norm

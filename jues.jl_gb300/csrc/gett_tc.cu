@@ -140,6 +140,26 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// packed FP32 pairs (sm_100+): two round-to-nearest operations per instruction
+__device__ __forceinline__ uint64_t pk2(uint32_t lo, uint32_t hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(lo), "r"(hi));
+    return r;
+}
+__device__ __forceinline__ uint64_t pk2f(float lo, float hi) { return pk2(__float_as_uint(lo), __float_as_uint(hi)); }
+__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ float lo_f(uint64_t x) { return __uint_as_float((uint32_t)x); }
+__device__ __forceinline__ float hi_f(uint64_t x) { return __uint_as_float((uint32_t)(x >> 32)); }
+
 // UMMA shared-memory descriptor of a K-major tile written by TMA with 128-byte swizzle:
 // start address >> 4, LBO unused (1), SBO = 1024 bytes between 8-row groups, version 1,
 // layout type 2 = SWIZZLE_128B.
@@ -310,9 +330,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int quarter = warp & 3;
         const int half = (warp - 2) >> 2;
         const int dt = threadIdx.x - 64;   // 0..255 among the drain threads
-        float acc[HB];
+        uint64_t acc2[HB / 2];   // FP32 pairs (columns 2j, 2j+1)
 #pragma unroll
-        for (int j = 0; j < HB; ++j) acc[j] = 0.f;
+        for (int j = 0; j < HB / 2; ++j) acc2[j] = 0ull;
         const long long mrow = (long long)m0 + quarter * 32 + lane;
         bool ok = true;
         // the scales of chunk c + 1 are loaded while chunk c drains
@@ -342,19 +362,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             eb_cur = eb_next;
             // row factor 2^(e_row - 18); the column factor comes from shared memory
             const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
-            const float *cs = colsc + buf * BN + half * HB;
+            const float2 *cs = reinterpret_cast<const float2 *>(colsc + buf * BN + half * HB);
+            const uint64_t rs2 = pk2f(rs, rs), k2 = pk2f(0.0009765625f, 0.0009765625f);
+            // 32 columns per round: four TMEM loads in flight, one wait; then per column pair
+            // part = corr 2^-10 + main, acc += part (2^e_row 2^e_col), all round-to-nearest
 #pragma unroll
-            for (int c0 = 0; c0 < HB; c0 += 16) {
-                uint32_t rm[16], rc[16];
+            for (int c0 = 0; c0 < HB; c0 += 32) {
+                uint32_t rm[32], rc[32];
                 const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) +
                                       (uint32_t)(buf * 2 * BN + half * HB + c0);
-                tmem_ld16(base, rm);
-                tmem_ld16(base + (uint32_t)BN, rc);
+                tmem_ld16(base, *reinterpret_cast<uint32_t(*)[16]>(rm));
+                tmem_ld16(base + 16u, *reinterpret_cast<uint32_t(*)[16]>(rm + 16));
+                tmem_ld16(base + (uint32_t)BN, *reinterpret_cast<uint32_t(*)[16]>(rc));
+                tmem_ld16(base + (uint32_t)BN + 16u, *reinterpret_cast<uint32_t(*)[16]>(rc + 16));
                 tmem_ld_wait();
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const float part = __fmaf_rn(__uint_as_float(rc[j]), 0.0009765625f, __uint_as_float(rm[j]));
-                    acc[c0 + j] = __fmaf_rn(part, rs * cs[c0 + j], acc[c0 + j]);
+                for (int j = 0; j < 32; j += 2) {
+                    const float2 c2 = cs[(c0 + j) >> 1];
+                    const uint64_t part = ffma2(pk2(rc[j], rc[j + 1]), k2, pk2(rm[j], rm[j + 1]));
+                    const uint64_t sc = fmul2(rs2, pk2f(c2.x, c2.y));
+                    acc2[(c0 + j) >> 1] = ffma2(part, sc, acc2[(c0 + j) >> 1]);
                 }
             }
             tc_fence_before();
@@ -368,14 +395,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const long long Mpad = g.mtiles * TBM, Npad = (g.tiles / g.mtiles) * BN;
             float *dst = g.partial + ((long long)split * Npad + n0 + half * HB) * Mpad + mrow;
 #pragma unroll
-            for (int j = 0; j < HB; ++j) dst[(long long)j * Mpad] = acc[j];
+            for (int j = 0; j < HB / 2; ++j) {
+                dst[(long long)(2 * j) * Mpad] = lo_f(acc2[j]);
+                dst[(long long)(2 * j + 1) * Mpad] = hi_f(acc2[j]);
+            }
         } else if (mrow < g.M) {
             const long long rowoff = mode_off(g.mC, mrow);
 #pragma unroll
             for (int j = 0; j < HB; ++j) {
                 const long long co = coloff[half * HB + j];
                 if (co >= 0) {
-                    double val = g.alpha * (double)acc[j];
+                    double val = g.alpha * (double)((j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]));
                     if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
                     g.C[rowoff + co] = val;
                 }

@@ -56,6 +56,8 @@ DP = C.POINTER(C.c_double)
 VP = C.c_void_p
 
 # name -> (restype, argtypes)
+DF_VARIANT = {"reference": 0, "rccd": 1}
+
 SIGNATURES = {
     "jues_version": (C.c_int, []),
     "jues_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
@@ -86,6 +88,12 @@ SIGNATURES = {
                              DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
     "jues_cc_create": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, DP, C.c_int, DP, C.c_int, DP,
                                  C.POINTER(CCOpts), C.POINTER(VP)]),
+    "jues_cc_create_df": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, DP, DP, C.c_int, DP, C.c_int, DP,
+                                    C.POINTER(CCOpts), C.c_int, C.POINTER(VP)]),
+    "jues_df_rccd": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts),
+                               C.c_int, DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
+    "jues_pT": (C.c_int, [VP, DP, DP, DP, DP, DP, DP, DP, C.c_int, C.c_int, C.c_int, DP]),
+    "jues_cc_pT": (C.c_int, [VP, C.c_int, DP]),
     "jues_cc_iterate": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "jues_cc_set_precision": (C.c_int, [VP, C.c_int]),
     "jues_cc_energy": (C.c_int, [VP, DP]),

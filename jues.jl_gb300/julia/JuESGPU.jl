@@ -190,4 +190,63 @@ function do_rccsd(refWfn::Wfn; maxit = 40, return_T = false, precision = :fp64, 
     return return_T ? (E, T2) : E
 end
 
+"""
+    do_df_rmp2(refWfn, pqP, Jpqh = nothing; precision = :fp64) -- DF-RMP2.jl:1-46
+
+`pqP` and `Jpqh` are what `DF.setup_df(refWfn)` returns (DF.jl:30-51); with `Jpqh ===
+nothing`, `pqP` is taken as the fitted b[mu,nu,Q].
+"""
+function do_df_rmp2(refWfn::Wfn, pqP::AbstractArray{<:Real,3}, Jpqh = nothing; precision::Symbol = :fp64)
+    b = f64(pqP)
+    J = Jpqh === nothing ? C_NULL : f64(Jpqh)
+    Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
+    e = Ref{Cdouble}(0.0)
+    check(ccall((:jues_df_rmp2, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                 Ptr{Cdouble}, Cint, Ref{Cdouble}),
+                ctx(), b, size(b, 1), size(b, 3), J, Co, size(Co, 2), Cv, size(Cv, 2), f64(refWfn.epsa),
+                PREC[precision], e))
+    return e[]
+end
+
+"""
+    do_df_rccd(refWfn, pqP, Jpqh = nothing; maxit = 40, return_T2 = false) -- DF-RCCD.jl:11-54
+
+The reference's settings by default: T2 = (ia|jb)/D, `maxit` Jacobi sweeps, no DIIS, and
+DF-RCCD.jl's WmBeJ (`variant = :reference`; `:rccd` for RCCD.jl's index order).
+"""
+function do_df_rccd(refWfn::Wfn, pqP::AbstractArray{<:Real,3}, Jpqh = nothing; maxit = 40, doprint = false,
+                    return_T2 = false, precision = :fp64, variant = :reference, diis = false, r_conv = 0.0,
+                    e_conv = 0.0, diis_size = 6, refine = 0)
+    b = f64(pqP)
+    J = Jpqh === nothing ? C_NULL : f64(Jpqh)
+    Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
+    o, v = size(Co, 2), size(Cv, 2)
+    opts = Ref(CCOpts(maxit, e_conv, r_conv, Cint(diis), diis_size, PREC[precision], GUESS[:mp2], refine, Cint(-1)))
+    e = Ref{Cdouble}(0.0)
+    nit = Ref{Cint}(0)
+    T2 = Array{Float64}(undef, o, o, v, v)
+    log = Vector{IterLog}(undef, max(1, maxit))
+    st = ccall((:jues_df_rccd, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                Ptr{Cdouble}, Ref{CCOpts}, Cint, Ref{Cdouble}, Ptr{Cdouble}, Ptr{IterLog}, Cint, Ref{Cint}),
+               ctx(), b, size(b, 1), size(b, 3), J, Co, o, Cv, v, f64(refWfn.epsa), opts,
+               Cint(variant === :reference ? 0 : 1), e, T2, log, length(log), nit)
+    st == ENOTCONV ? @warn(lasterror()) : check(st)
+    doprint && foreach(r -> println(r.iter - 1, " @CCD ", r.energy), log[1:nit[]])
+    return return_T2 ? (e[], T2) : e[]
+end
+
+"compute_pT(; T1, T2, Vvvvo, Vvooo, Vvovo, fo, fv) -- PerturbativeTriples.jl:35-138"
+function compute_pT(; T1, T2, Vvvvo, Vvooo, Vvovo, fo, fv, precision::Symbol = :fp64)
+    o, v = size(T1)
+    e = Ref{Cdouble}(0.0)
+    check(ccall((:jues_pT, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble},
+                 Ptr{Cdouble}, Cint, Cint, Cint, Ref{Cdouble}),
+                ctx(), f64(T1), f64(T2), f64(Vvvvo), f64(Vvooo), f64(Vvovo), f64(fo), f64(fv), o, v,
+                PREC[precision], e))
+    return e[]
+end
+
 end # module

@@ -289,3 +289,67 @@ def test_df_rmp2_rejects_bad_shapes(jg):
         jg.MollerPlesset.do_df_rmp2(w, np.zeros((25, 24, 75)))
     with pytest.raises(ValueError):
         jg.MollerPlesset.do_df_rmp2(w, np.zeros((25, 25, 75)), np.zeros((75, 74)))
+
+
+# ------------------------------------------------------------------------------ DF-CCD
+def test_df_rccd_matches_oracle_sweep_by_sweep(jg):
+    # DF-RCCD.jl as written (its WmBeJ), through an orthogonal Jpqh
+    from oracle import df_rccd
+    from juesgpu.CoupledCluster import solve_df
+    s = make_named("S25")
+    pqP, Jpqh = _df_inputs(s, True)
+    w = s.wfn()
+    e, T2, nit, log = solve_df(w, pqP, Jpqh, maxit=8, guess="mp2", diis=False, r_conv=0.0)
+    ref_log = []
+    e_ref, T_ref = df_rccd.do_df_rccd(w, np.einsum("pqP,PQ->pqQ", pqP, Jpqh), maxit=8, return_T2=True,
+                                      log=ref_log)
+    assert nit == 8
+    for (it, en, *_), (it_r, en_r) in zip(log, ref_log):
+        assert it == it_r and abs(en - en_r) < 1e-10 * max(1.0, abs(en_r))
+    assert abs(e - e_ref) < 1e-10
+    assert np.abs(T2 - T_ref).max() < 1e-9
+    # the mirror's defaults are the reference's: 40 sweeps, MP2 guess, no DIIS
+    e40 = jg.CoupledCluster.DFRCCD.do_df_rccd(w, pqP, Jpqh)
+    assert abs(e40 - df_rccd.do_df_rccd(w, np.transpose(s.B, (1, 2, 0)), maxit=40)) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_df_rccd_rccd_variant_equals_conventional(jg, name):
+    # with RCCD.jl's WmBeJ, CCD on exactly factorised integrals is conventional CCD
+    from juesgpu.CoupledCluster import solve, solve_df
+    s = make_named(name)
+    pqP, _ = _df_inputs(s, False)
+    w = s.wfn()
+    kw = dict(maxit=6, guess="mp2", diis=False, r_conv=0.0)
+    _, T_df, _, log_df = solve_df(w, pqP, None, variant="rccd", **kw)
+    _, _, T_ao, _, log_ao = solve(0, w, **kw)
+    for a, b in zip(log_df, log_ao):
+        assert abs(a[1] - b[1]) < 1e-10 * max(1.0, abs(b[1]))
+    assert np.abs(T_df - T_ao).max() < 1e-9
+
+
+def test_df_rccd_split_precision(jg):
+    from juesgpu.CoupledCluster import solve_df
+    s = make_named("S100")
+    pqP, Jpqh = _df_inputs(s, True)
+    w = s.wfn()
+    kw = dict(maxit=40, guess="mp2", diis=True, r_conv=1e-9)
+    e64 = solve_df(w, pqP, Jpqh, **kw)[0]
+    e_split = solve_df(w, pqP, Jpqh, precision="split_bf16", transform_precision="fp64", refine=2, **kw)[0]
+    assert abs(e_split - e64) < 1e-6
+
+
+def test_df_rccd_session_and_errors(jg):
+    from juesgpu.CoupledCluster import CCSession
+    s = make_named("S25")
+    pqP, _ = _df_inputs(s, False)
+    w = s.wfn()
+    ses = CCSession(0, w, pqP=pqP, guess="mp2", diis=False, r_conv=0.0, maxit=3)
+    ses.iterate(3)
+    e3 = ses.energy()
+    ses.close()
+    assert abs(e3 - jg.CoupledCluster.DFRCCD.do_df_rccd(w, pqP, maxit=3)) < 1e-12
+    with pytest.raises(ValueError):
+        CCSession(1, w, pqP=pqP)
+    with pytest.raises(KeyError):
+        jg.CoupledCluster.DFRCCD.do_df_rccd(w, pqP, variant="nope")

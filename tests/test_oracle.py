@@ -177,3 +177,96 @@ def test_df_rmp2_oracle_equals_conventional_on_exact_factorisation():
     Q, _ = np.linalg.qr(np.random.default_rng(7).standard_normal((s.naux, s.naux)))
     pqP = np.einsum("pqQ,PQ->pqP", b, Q)
     assert abs(oracle.df_rmp2(w, pqP, Q) - e) < 1e-12
+
+
+def test_df_rccd_oracle_forms():
+    # DF-RCCD.jl on exactly factorised integrals: with RCCD.jl's WmBeJ it is the RCCD
+    # iteration itself (MP2 guess, no DIIS), sweep by sweep; DF-RCCD.jl's own WmBeJ (its last
+    # term contracts (me|nf) where RCCD.jl:400 has (ne|mf)) reaches a different fixed point
+    from oracle import df_rccd
+    s = make_named("S25")
+    w = s.wfn()
+    b = np.transpose(s.B, (1, 2, 0))
+    log_df, log_ref, log_q = [], [], []
+    df_rccd.do_df_rccd(w, b, maxit=6, variant="rccd", log=log_df)
+    ccd.do_rccd(w, maxit=6, guess="mp2", diis=False, r_conv=None, log=log_ref)
+    for (i1, e1), (i2, e2, _) in zip(log_df, log_ref):
+        assert i1 == i2 and abs(e1 - e2) < 1e-13
+    e_q = df_rccd.do_df_rccd(w, b, maxit=40, variant="reference", log=log_q)
+    e_r = df_rccd.do_df_rccd(w, b, maxit=40, variant="rccd")
+    assert abs(log_q[-1][1] - log_q[-2][1]) < 1e-10      # both converge within 40 sweeps
+    assert abs(e_q - e_r) > 1e-6
+
+
+def _spin_orbital_pT(w, t1, T2):
+    """Independent spin-orbital (T) (the textbook connected/disconnected triples with
+    antisymmetrised integrals) on converged closed-shell CCSD amplitudes."""
+    from oracle.transform import tei_transform
+    C = w.Ca if hasattr(w, "Ca") else np.hstack([w.Cao, w.Cav])
+    n, o = C.shape[1], w.nalpha
+    mo = tei_transform(w.ao_eri, C)                       # (pq|rs), spatial
+    ns, no = 2 * n, 2 * o
+    # spin orbitals: occupied first (alpha, beta interleaved), then virtuals
+    spat = [p // 2 for p in range(2 * o)] + [o + p // 2 for p in range(2 * (n - o))]
+    spin = [p % 2 for p in range(ns)]
+    sp = np.array(spat)
+    sg = np.array(spin)
+    chem = mo[np.ix_(sp, sp, sp, sp)] * ((sg[:, None] == sg[None, :])[:, :, None, None]
+                                         * (sg[:, None] == sg[None, :])[None, None, :, :])
+    phys = np.transpose(chem, (0, 2, 1, 3))               # <pq|rs> = (pr|qs)
+    anti = phys - np.transpose(phys, (0, 1, 3, 2))
+    eps = np.array([w.epsa[s] for s in spat])
+    nv = ns - no
+    # amplitudes
+    ts1 = np.zeros((no, nv))
+    ts2 = np.zeros((no, no, nv, nv))
+    for I in range(no):
+        for A in range(nv):
+            if sg[I] == sg[no + A]:
+                ts1[I, A] = t1[sp[I], sp[no + A] - o]
+    for I in range(no):
+        for J in range(no):
+            for A in range(nv):
+                for B in range(nv):
+                    i, j, a, b = sp[I], sp[J], sp[no + A] - o, sp[no + B] - o
+                    val = 0.0
+                    if sg[I] == sg[no + A] and sg[J] == sg[no + B]:
+                        val += T2[i, j, a, b]
+                    if sg[I] == sg[no + B] and sg[J] == sg[no + A]:
+                        val -= T2[i, j, b, a]
+                    ts2[I, J, A, B] = val
+    O, V = slice(0, no), slice(no, ns)
+    eo, ev = eps[:no], eps[no:]
+    D = (eo[:, None, None, None, None, None] + eo[None, :, None, None, None, None]
+         + eo[None, None, :, None, None, None] - ev[None, None, None, :, None, None]
+         - ev[None, None, None, None, :, None] - ev[None, None, None, None, None, :])
+    E = np.einsum
+    # t_c without permutation: sum_e t_jk^ae <ei||bc> - sum_m t_im^bc <ma||jk>
+    raw_c = E("jkae,eibc->ijkabc", ts2, anti[V, O, V, V]) - E("imbc,majk->ijkabc", ts2, anti[O, V, O, O])
+    raw_d = E("ia,jkbc->ijkabc", ts1, anti[O, O, V, V])
+
+    def P(x):
+        # P(i/jk) P(a/bc)
+        y = x - np.transpose(x, (1, 0, 2, 3, 4, 5)) - np.transpose(x, (2, 1, 0, 3, 4, 5))
+        return y - np.transpose(y, (0, 1, 2, 4, 3, 5)) - np.transpose(y, (0, 1, 2, 5, 4, 3))
+    tc = P(raw_c) / D
+    td = P(raw_d) / D
+    return float(np.sum(tc * D * (tc + td)) / 36.0)
+
+
+def test_pT_oracle_equals_spin_orbital_triples_on_h2o():
+    # compute_pT (PerturbativeTriples.jl:35-138) has no known answer in the reference's tests;
+    # pin its closed-shell restatement against an independent spin-orbital (T) on the same
+    # converged H2O/STO-3G CCSD amplitudes, and its vectorised energy loop against the scalar one
+    from oracle import triples
+    w = h2o()
+    e, t1, T2, _ = ccsd.do_rccsd(w, return_T=True)
+    assert abs(e - E_CCSD_H2O) < 1e-10
+    oooo, ooov, oovv, ovov, ovvv, vvvv = ccsd.make_rccsd_integrals(w)
+    Vvvvo, Vvooo, Vvovo = triples.integrals_from_cc(ovvv, ooov, oovv)
+    o = w.nalpha
+    args = (t1, T2, Vvvvo, Vvooo, Vvovo, w.epsa[:o], w.epsa[o:])
+    e_t = triples.compute_pT(*args)
+    assert abs(e_t - triples.compute_pT_loops(*args)) < 1e-15
+    e_so = _spin_orbital_pT(w, t1, T2)
+    assert e_t < 0 and abs(e_t - e_so) < 1e-12, (e_t, e_so)
