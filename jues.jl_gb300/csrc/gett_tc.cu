@@ -79,6 +79,19 @@ __device__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_fl
         }
     }
 }
+// bounded wait that ignores the abort flags: used only to let this CTA's own asynchronous
+// copies and MMAs settle before it frees TMEM and exits
+__device__ bool mbar_wait_quiet(uint64_t *bar, uint32_t parity) {
+    unsigned long long t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            unsigned long long t = gtimer();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > WAIT_LIMIT_NS) return false;
+        }
+    }
+}
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
                                             int z) {
     asm volatile(
@@ -126,16 +139,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
           "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
           "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
           "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-}
-// 32 lanes x 16 consecutive 32-bit TMEM columns -> 16 registers per thread
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-          "=r"(r[15])
         : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -215,6 +218,37 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// one work item of the persistent kernel: output tile (m0, n0) over stages [kb0, kb0 + nk)
+struct TcItem {
+    int m0, n0, kb0, nk;
+    long long split;
+};
+__device__ __forceinline__ TcItem tc_item(const TcArgs &g, long long w, int BN) {
+    TcItem I;
+    const long long tile = w % g.tiles;
+    I.split = w / g.tiles;
+    I.m0 = (int)((tile % g.mtiles) * TBM);
+    I.n0 = (int)((tile / g.mtiles) * BN);
+    I.kb0 = (int)I.split * g.kper;
+    I.nk = min(g.kblocks - I.kb0, g.kper);
+    return I;
+}
+
+// barrier over the 256 drain threads (named barrier 1) that returns, uniformly to all of them,
+// whether any thread passed pred = true
+__device__ __forceinline__ bool drain_bar_any(bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "n"(TC_DRAIN)
+        : "memory");
+    return r != 0;
+}
+
 template <int BN, int STAGES, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gett_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs g) {
@@ -226,19 +260,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint64_t *empty = full + STAGES;
     uint64_t *cfull = empty + STAGES;    // [2] chunk accumulated in TMEM buffer
     uint64_t *cempty = cfull + 2;        // [2] chunk drained, buffer reusable
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cempty + 2);
+    uint64_t *fin = cempty + 2;          // the MMA thread's last commit
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     long long *coloff = reinterpret_cast<long long *>(smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES);
     float *colsc = reinterpret_cast<float *>(coloff + BN);   // [2][BN] per-chunk column scales
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long tile = blockIdx.x % g.tiles, split = blockIdx.x / g.tiles;
-    const long long mt = tile % g.mtiles, nt = tile / g.mtiles;
-    const int m0 = (int)(mt * TBM), n0 = (int)(nt * BN);
-    const int kb0 = (int)split * g.kper;                      // first stage of this split
-    const int nk = min(g.kblocks - kb0, g.kper);              // stages of this split (>= 1)
-    const int nchunks = (nk + KC - 1) / KC;
-    const int chunk0 = kb0 / KC;                              // kper is a multiple of KC
+    // persistent: CTA b processes work items b, b + gridDim.x, ...; an item is one output tile
+    // over one K split.  Stage and chunk counters run on across items, so the pipeline and the
+    // TMEM buffers never drain between tiles.
+    const long long nitems = g.tiles * g.ksplit;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -249,6 +281,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&cfull[b], 1);
             mbar_init(&cempty[b], TC_DRAIN);
         }
+        mbar_init(fin, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -256,10 +289,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 1) {
         tmem_alloc(tmem_slot, Cfg::TMEM_COLS);
         tmem_relinquish();
-    }
-    for (int c = threadIdx.x; c < BN; c += blockDim.x) {
-        const long long n = (long long)n0 + c;
-        coloff[c] = n < g.N ? mode_off(g.nC, n) : -1;
     }
     tc_fence_before();
     __syncthreads();
@@ -269,148 +298,200 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {
             // TMA producer
-            for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % STAGES;
-                const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-                if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, g.flags)) {
-                    *abort_flag = 1;
-                    break;
+            long long it = 0;   // stages issued by this CTA
+            bool stop = false;
+            for (long long w = blockIdx.x; w < nitems && !stop; w += gridDim.x) {
+                const TcItem I = tc_item(g, w, BN);
+                for (int kb = 0; kb < I.nk; ++kb, ++it) {
+                    const int s = (int)(it % STAGES);
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, g.flags)) {
+                        *abort_flag = 1;
+                        stop = true;
+                        break;
+                    }
+                    uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+                    const int kx = (I.kb0 + kb) * TBK;
+                    mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
+                    tma_load_3d(st, &mapA, &full[s], kx, I.m0, 0);
+                    tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kx, I.m0, 1);
+                    tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kx, I.n0, 0);
+                    tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kx, I.n0, 1);
                 }
-                uint8_t *st = stages + s * Cfg::STAGE_BYTES;
-                const int kx = (kb0 + kb) * TBK;
-                mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
-                tma_load_3d(st, &mapA, &full[s], kx, m0, 0);
-                tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kx, m0, 1);
-                tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kx, n0, 0);
-                tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kx, n0, 1);
             }
+            // the last load into each slot has landed (immediate unless an abort cut the MMA
+            // thread short), so no copy is in flight when the CTA exits
+            for (int s = 0; s < STAGES; ++s)
+                if (it > s) {
+                    const long long last = s + ((it - 1 - s) / STAGES) * STAGES;
+                    mbar_wait_quiet(&full[s], (uint32_t)(last / STAGES) & 1u);
+                }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // MMA issuer: chunk c accumulates stages [c*KC, c*KC+KC) into TMEM buffer c&1
-            for (int kb = 0; kb < nk; ++kb) {
-                const int chunk = kb / KC, buf = chunk & 1;
-                const bool first = (kb % KC) == 0;
-                if (first && chunk >= 2) {
-                    if (!mbar_wait(&cempty[buf], (uint32_t)((chunk >> 1) - 1) & 1u, abort_flag, g.flags)) {
+            // MMA issuer: chunk gc (counted across items) accumulates into TMEM buffer gc & 1
+            long long it = 0, gc = 0;
+            bool stop = false;
+            for (long long w = blockIdx.x; w < nitems && !stop; w += gridDim.x) {
+                const TcItem I = tc_item(g, w, BN);
+                for (int kb = 0; kb < I.nk; ++kb, ++it) {
+                    const int buf = (int)(gc & 1);
+                    const bool first = (kb % KC) == 0;
+                    if (first && gc >= 2) {
+                        if (!mbar_wait(&cempty[buf], (uint32_t)((gc >> 1) - 1) & 1u, abort_flag, g.flags)) {
+                            *abort_flag = 1;
+                            stop = true;
+                            break;
+                        }
+                        tc_fence_after();
+                    }
+                    const int s = (int)(it % STAGES);
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    if (!mbar_wait(&full[s], ph, abort_flag, g.flags)) {
                         *abort_flag = 1;
+                        stop = true;
                         break;
                     }
                     tc_fence_after();
-                }
-                const int s = kb % STAGES;
-                const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-                if (!mbar_wait(&full[s], ph, abort_flag, g.flags)) {
-                    *abort_flag = 1;
-                    break;
-                }
-                tc_fence_after();
-                uint8_t *st = stages + s * Cfg::STAGE_BYTES;
-                const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
-                const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
-                const uint32_t dmain = tmem + (uint32_t)(buf * 2 * BN);
-                const uint32_t dcorr = dmain + (uint32_t)BN;
-                // B_lo's rows follow B_hi's in shared memory (B_BYTES = BN 128-byte rows, whole
-                // 8-row swizzle groups) and the correction columns follow the main ones in TMEM,
-                // so hi*hi and hi*lo are one N = 2 BN instruction; lo*hi adds to the correction.
+                    uint8_t *st = stages + s * Cfg::STAGE_BYTES;
+                    const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
+                    const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
+                    const uint32_t dmain = tmem + (uint32_t)(buf * 2 * BN);
+                    const uint32_t dcorr = dmain + (uint32_t)BN;
+                    // B_lo's rows follow B_hi's in shared memory (B_BYTES = BN 128-byte rows, whole
+                    // 8-row swizzle groups) and the correction columns follow the main ones in
+                    // TMEM, so hi*hi and hi*lo are one N = 2 BN instruction; lo*hi adds to the
+                    // correction.
 #pragma unroll
-                for (int kk = 0; kk < TBK / 16; ++kk) {
-                    const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
-                    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
-                    umma_bf16(dmain, ah + off, bh + off, Cfg::IDESC2, acc);
-                    umma_bf16(dcorr, al + off, bh + off, Cfg::IDESC, 1u);
+                    for (int kk = 0; kk < TBK / 16; ++kk) {
+                        const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
+                        const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+                        umma_bf16(dmain, ah + off, bh + off, Cfg::IDESC2, acc);
+                        umma_bf16(dcorr, al + off, bh + off, Cfg::IDESC, 1u);
+                    }
+                    umma_commit(&empty[s]);   // stage s free once these complete
+                    if ((kb % KC) == KC - 1 || kb == I.nk - 1) {
+                        umma_commit(&cfull[buf]);   // chunk done
+                        ++gc;
+                    }
                 }
-                umma_commit(&empty[s]);                       // stage s free once these complete
-                if ((kb % KC) == KC - 1 || kb == nk - 1) umma_commit(&cfull[buf]);   // chunk done
             }
+            // every MMA this thread issued has completed before TMEM is freed
+            umma_commit(fin);
+            mbar_wait_quiet(fin, 0u);
         }
     } else {
-        // drain warps 2-9: TMEM lane quarter (warp % 4), one tile row per thread, half the columns
+        // drain warps 2-9: TMEM lane quarter (warp % 4), one tile row per thread, half the columns.
+        // They leave their loops only together: every exit test follows a barrier that ORs the
+        // threads' failure flags, so no drain thread can be left waiting at a barrier.
         constexpr int HB = BN / 2;
         const int quarter = warp & 3;
         const int half = (warp - 2) >> 2;
         const int dt = threadIdx.x - 64;   // 0..255 among the drain threads
-        uint64_t acc2[HB / 2];   // FP32 pairs (columns 2j, 2j+1)
-#pragma unroll
-        for (int j = 0; j < HB / 2; ++j) acc2[j] = 0ull;
-        const long long mrow = (long long)m0 + quarter * 32 + lane;
+        long long gc = 0;
         bool ok = true;
-        // the scales of chunk c + 1 are loaded while chunk c drains
-        const int *pa = g.expA + (long long)chunk0 * g.expA_ld + mrow;
-        const int *pb = g.expB + (long long)chunk0 * g.expB_ld + n0 + (dt < BN ? dt : 0);
-        int ea_cur = __ldg(pa), eb_cur = __ldg(pb);
-        for (int c = 0; c < nchunks; ++c) {
-            const int buf = c & 1;
-            // column scales of this chunk: 2^e_col, staged once for all drain warps
-            if (dt < BN)
-                colsc[buf * BN + dt] = (eb_cur == INT_MIN || eb_cur < -126) ? 0.f : __int_as_float((eb_cur + 127) << 23);
-            int ea_next = 0, eb_next = 0;
-            if (c + 1 < nchunks) {
-                ea_next = __ldg(pa + (long long)(c + 1) * g.expA_ld);
-                eb_next = __ldg(pb + (long long)(c + 1) * g.expB_ld);
-            }
-            asm volatile("bar.sync 1, %0;" ::"n"(TC_DRAIN) : "memory");
-            if (!mbar_wait(&cfull[buf], (uint32_t)(c >> 1) & 1u, abort_flag, g.flags)) {
+        for (long long w = blockIdx.x; w < nitems; w += gridDim.x) {
+            const TcItem I = tc_item(g, w, BN);
+            const int nchunks = (I.nk + KC - 1) / KC;
+            const int chunk0 = I.kb0 / KC;   // kper is a multiple of KC
+            // every drain thread has finished the previous item's epilogue (which reads coloff)
+            if (drain_bar_any(*abort_flag != 0)) {
                 ok = false;
-                *abort_flag = 1;
                 break;
             }
-            __syncwarp();
-            tc_fence_after();
-            const int ea = ea_cur;
-            ea_cur = ea_next;
-            eb_cur = eb_next;
-            // row factor 2^(e_row - 18); the column factor comes from shared memory
-            const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
-            const float2 *cs = reinterpret_cast<const float2 *>(colsc + buf * BN + half * HB);
-            const uint64_t rs2 = pk2f(rs, rs), k2 = pk2f(0.0009765625f, 0.0009765625f);
-            // 32 columns per round: four TMEM loads in flight, one wait; then per column pair
-            // part = corr 2^-10 + main, acc += part (2^e_row 2^e_col), all round-to-nearest
+            if (dt < BN) {
+                const long long n = (long long)I.n0 + dt;
+                coloff[dt] = n < g.N ? mode_off(g.nC, n) : -1;
+            }
+            uint64_t acc2[HB / 2];   // FP32 pairs (columns 2j, 2j+1)
 #pragma unroll
-            for (int c0 = 0; c0 < HB; c0 += 32) {
-                uint32_t rm[32], rc[32];
-                const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) +
-                                      (uint32_t)(buf * 2 * BN + half * HB + c0);
-                tmem_ld16(base, *reinterpret_cast<uint32_t(*)[16]>(rm));
-                tmem_ld16(base + 16u, *reinterpret_cast<uint32_t(*)[16]>(rm + 16));
-                tmem_ld16(base + (uint32_t)BN, *reinterpret_cast<uint32_t(*)[16]>(rc));
-                tmem_ld16(base + (uint32_t)BN + 16u, *reinterpret_cast<uint32_t(*)[16]>(rc + 16));
-                tmem_ld_wait();
+            for (int j = 0; j < HB / 2; ++j) acc2[j] = 0ull;
+            const long long mrow = (long long)I.m0 + quarter * 32 + lane;
+            // the scales of chunk c + 1 are loaded while chunk c drains
+            const int *pa = g.expA + (long long)chunk0 * g.expA_ld + mrow;
+            const int *pb = g.expB + (long long)chunk0 * g.expB_ld + I.n0 + (dt < BN ? dt : 0);
+            int ea_cur = __ldg(pa), eb_cur = __ldg(pb);
+            bool bad = false;
+            for (int c = 0; c < nchunks; ++c, ++gc) {
+                const int buf = (int)(gc & 1);
+                // column scales of this chunk: 2^e_col, staged once for all drain warps
+                if (dt < BN)
+                    colsc[buf * BN + dt] =
+                        (eb_cur == INT_MIN || eb_cur < -126) ? 0.f : __int_as_float((eb_cur + 127) << 23);
+                int ea_next = 0, eb_next = 0;
+                if (c + 1 < nchunks) {
+                    ea_next = __ldg(pa + (long long)(c + 1) * g.expA_ld);
+                    eb_next = __ldg(pb + (long long)(c + 1) * g.expB_ld);
+                }
+                if (drain_bar_any(bad || *abort_flag != 0)) {
+                    bad = true;
+                    break;
+                }
+                // warp-uniform outcome: the TMEM loads below need the whole warp
+                const bool got = mbar_wait(&cfull[buf], (uint32_t)(gc >> 1) & 1u, abort_flag, g.flags);
+                if (!__all_sync(0xffffffffu, got)) {
+                    *abort_flag = 1;
+                    bad = true;   // the next barrier takes every drain thread out
+                    continue;
+                }
+                __syncwarp();
+                tc_fence_after();
+                const int ea = ea_cur;
+                ea_cur = ea_next;
+                eb_cur = eb_next;
+                // row factor 2^(e_row - 18); the column factor comes from shared memory
+                const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
+                const float2 *cs = reinterpret_cast<const float2 *>(colsc + buf * BN + half * HB);
+                const uint64_t rs2 = pk2f(rs, rs), k2 = pk2f(0.0009765625f, 0.0009765625f);
+                // 32 columns per round: two TMEM loads in flight, one wait; then per column pair
+                // part = corr 2^-10 + main, acc += part (2^e_row 2^e_col), all round-to-nearest
 #pragma unroll
-                for (int j = 0; j < 32; j += 2) {
-                    const float2 c2 = cs[(c0 + j) >> 1];
-                    const uint64_t part = ffma2(pk2(rc[j], rc[j + 1]), k2, pk2(rm[j], rm[j + 1]));
-                    const uint64_t sc = fmul2(rs2, pk2f(c2.x, c2.y));
-                    acc2[(c0 + j) >> 1] = ffma2(part, sc, acc2[(c0 + j) >> 1]);
+                for (int c0 = 0; c0 < HB; c0 += 32) {
+                    uint32_t rm[32], rc[32];
+                    const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                          (uint32_t)(buf * 2 * BN + half * HB + c0);
+                    tmem_ld32(base, rm);
+                    tmem_ld32(base + (uint32_t)BN, rc);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; j += 2) {
+                        const float2 c2 = cs[(c0 + j) >> 1];
+                        const uint64_t part = ffma2(pk2(rc[j], rc[j + 1]), k2, pk2(rm[j], rm[j + 1]));
+                        const uint64_t sc = fmul2(rs2, pk2f(c2.x, c2.y));
+                        acc2[(c0 + j) >> 1] = ffma2(part, sc, acc2[(c0 + j) >> 1]);
+                    }
+                }
+                tc_fence_before();
+                mbar_arrive(&cempty[buf]);
+            }
+            if (drain_bar_any(bad)) {   // every drain thread takes part, failed or not
+                ok = false;
+                break;
+            }
+            if (g.partial) {
+                // raw partial sums, padded rows and columns included; a warp writes 32
+                // consecutive floats per column
+                const long long Mpad = g.mtiles * TBM, Npad = (g.tiles / g.mtiles) * BN;
+                float *dst = g.partial + ((long long)I.split * Npad + I.n0 + half * HB) * Mpad + mrow;
+#pragma unroll
+                for (int j = 0; j < HB / 2; ++j) {
+                    dst[(long long)(2 * j) * Mpad] = lo_f(acc2[j]);
+                    dst[(long long)(2 * j + 1) * Mpad] = hi_f(acc2[j]);
+                }
+            } else if (mrow < g.M) {
+                const long long rowoff = mode_off(g.mC, mrow);
+#pragma unroll
+                for (int j = 0; j < HB; ++j) {
+                    const long long co = coloff[half * HB + j];
+                    if (co >= 0) {
+                        double val = g.alpha * (double)((j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]));
+                        if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
+                        g.C[rowoff + co] = val;
+                    }
                 }
             }
-            tc_fence_before();
-            mbar_arrive(&cempty[buf]);
         }
-        if (!ok || *abort_flag) {
-            if (lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
-        } else if (g.partial) {
-            // raw partial sums, padded rows and columns included; a warp writes 32 consecutive
-            // floats per column
-            const long long Mpad = g.mtiles * TBM, Npad = (g.tiles / g.mtiles) * BN;
-            float *dst = g.partial + ((long long)split * Npad + n0 + half * HB) * Mpad + mrow;
-#pragma unroll
-            for (int j = 0; j < HB / 2; ++j) {
-                dst[(long long)(2 * j) * Mpad] = lo_f(acc2[j]);
-                dst[(long long)(2 * j + 1) * Mpad] = hi_f(acc2[j]);
-            }
-        } else if (mrow < g.M) {
-            const long long rowoff = mode_off(g.mC, mrow);
-#pragma unroll
-            for (int j = 0; j < HB; ++j) {
-                const long long co = coloff[half * HB + j];
-                if (co >= 0) {
-                    double val = g.alpha * (double)((j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]));
-                    if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
-                    g.C[rowoff + co] = val;
-                }
-            }
-        }
+        if (!ok && lane == 0) atomicOr(g.flags, FLAG_TIMEOUT);
     }
     tc_fence_before();
     __syncthreads();
@@ -636,6 +717,17 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
 
 constexpr int TC_KC = KCH / TBK;   // stages per accumulation chunk (one scaling chunk)
 
+static int sm_count(int device) {
+    static int cached[64] = {};
+    if (device < 0 || device >= 64) return 148;
+    if (!cached[device]) {
+        int n = 0;
+        JUES_CHECK_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device));
+        cached[device] = n > 0 ? n : 148;
+    }
+    return cached[device];
+}
+
 template <int BN, int STAGES>
 static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
                       const char *name) {
@@ -653,8 +745,10 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
         g.kper = g.kblocks;
         g.partial = nullptr;
     }
-    const long long grid = tiles * g.ksplit;
-    JUES_REQUIRE(grid < (1LL << 31), "too many output tiles");
+    const long long items = tiles * g.ksplit;
+    JUES_REQUIRE(items < (1LL << 31), "too many output tiles");
+    // persistent: one CTA per SM (the stage ring takes most of shared memory)
+    const long long grid = std::min<long long>(items, sm_count(ctx->device));
     Ctx::Scope s(ctx, name);
     gett_tc_kernel<BN, STAGES, TC_KC><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
     JUES_CHECK_CUDA(cudaGetLastError());
@@ -793,7 +887,6 @@ void *noalloc_scratch_address(int device) {
 
 void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
                long long Rpad, long long Kpad, __half *dst, int *ex) {
-    const long long nchunk = (Kpad + KCH - 1) / KCH;
     const long long blocks = (Rpad / PR) * (Kpad / PK);
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
