@@ -205,6 +205,24 @@ JUES_API int jues_rccsd(jues_ctx *ctx, const double *gao, int n,
                const jues_cc_opts *opts, double *e_out, double *t1_out, double *t2_out,
                jues_iter_log *log, int log_cap, int *niter);
 
+/* Fock matrix of a closed-shell determinant, IntegralTransformation.get_fock(wfn)
+ * (src/Backend/IntegralTransformation.jl:119-141): f = C^T (h + 2J - K) C with the density of
+ * the first nocc columns of C.  gao n^4, hao n x n, C n x nmo; f_out nmo x nmo; column-major. */
+JUES_API int jues_get_fock(jues_ctx *ctx, const double *gao, const double *hao, int n, const double *C,
+               int nmo, int nocc, double *f_out);
+
+/* CCSD from a general (non-canonical) Fock matrix, AutoRCCSD.do_rccsd
+ * (src/CoupledCluster/AutoRCCSD.jl:193-300): f = get_fock of C (the first ndocc columns
+ * occupied), fcn frozen core orbitals, T1 = f_ov/d, T2 = <ij|ab>/D, iterations until
+ * |dE| < opts.e_conv and max(||dT1||/len(T1), ||dT2||/len(T2)) < opts.r_conv, at most opts.maxit
+ * (the reference's cc_max_iter = 50, cc_e_conv = cc_max_rms = 1e-10).  With do_pT the (T)
+ * correction follows on the converged amplitudes with fo, fv = the Fock diagonal
+ * (AutoRCCSD.jl:294-299).  Outputs may be NULL. */
+JUES_API int jues_auto_rccsd(jues_ctx *ctx, const double *gao, const double *hao, int n, const double *C,
+               int nmo, int ndocc, int fcn, const jues_cc_opts *opts, int do_pT, double *e_out,
+               double *ept_out, double *t1_out, double *t2_out, jues_iter_log *log, int log_cap,
+               int *niter);
+
 /* (T) energy correction, PerturbativeTriples.compute_pT (src/CoupledCluster/
  * PerturbativeTriples.jl:35-138).  Host arrays, column-major, chemists' notation as the
  * reference takes them: T1[i,a] (o x v), T2[i,j,a,b] (o x o x v x v), Vvvvo[a,b,c,i] = (ab|ci)

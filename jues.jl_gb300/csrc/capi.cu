@@ -5,6 +5,7 @@
 
 #include "cc.cuh"
 #include "df.cuh"
+#include "fock.cuh"
 #include "triples.cuh"
 #include "common.cuh"
 #include "transform.cuh"
@@ -574,6 +575,63 @@ static int cc_run(jues_cc *cc, const jues_cc_opts *opts, double *e_out, double *
         st = JUES_ENOTCONV;
     }
     return st;
+}
+
+int jues_get_fock(jues_ctx *ctx, const double *gao, const double *hao, int n, const double *C, int nmo, int nocc,
+                  double *f_out) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        need(gao, "gao"); need(hao, "hao"); need(C, "C"); need(f_out, "f_out");
+        if (n <= 0 || nmo <= 0 || nmo > n || nocc < 0 || nocc > nmo)
+            throw Error(JUES_EINVAL, "need 0 < nmo <= nbf and 0 <= nocc <= nmo");
+        cudaSetDevice(c.device);
+        const size_t nn = (size_t)n * n;
+        DBuf<double> g = h2d(c, gao, nn * nn), h = h2d(c, hao, nn), cm = h2d(c, C, (size_t)n * nmo);
+        DBuf<double> f(&c, (size_t)nmo * nmo);
+        get_fock(&c, g.p, h.p, n, cm.p, nmo, cm.p, nocc, f.p);
+        d2h(c, f_out, f.p, (size_t)nmo * nmo);
+        c.check_flags();
+    });
+}
+
+int jues_auto_rccsd(jues_ctx *ctx, const double *gao, const double *hao, int n, const double *C, int nmo, int ndocc,
+                    int fcn, const jues_cc_opts *opts, int do_pT, double *e_out, double *ept_out, double *t1_out,
+                    double *t2_out, jues_iter_log *log, int log_cap, int *niter) {
+    jues_cc *cc = nullptr;
+    int st = guarded([&] {
+        Ctx &c = CX(ctx);
+        need(gao, "gao"); need(hao, "hao"); need(C, "C");
+        jues_cc_opts op;
+        if (opts) op = *opts; else jues_cc_default_opts(&op);
+        check_opts(op);
+        cudaSetDevice(c.device);
+        const size_t nn = (size_t)n * n;
+        if (n <= 0 || nmo <= 0 || nmo > n) throw Error(JUES_EINVAL, "need 0 < nmo <= nbf");
+        DBuf<double> g = h2d(c, gao, nn * nn), h = h2d(c, hao, nn), cm = h2d(c, C, (size_t)n * nmo);
+        std::unique_ptr<jues_cc> p(new jues_cc());
+        p->s = cc_create_auto(&c, g.p, h.p, n, cm.p, nmo, ndocc, fcn, op);
+        cc = p.release();
+    });
+    if (st) return st;
+    if (do_pT && ept_out) {
+        // run the iterations, then (T) on the session before it is destroyed
+        jues_cc_opts op;
+        if (opts) op = *opts; else jues_cc_default_opts(&op);
+        int done = 0, conv = 0;
+        st = jues_cc_iterate(cc, op.maxit, &done, &conv);
+        if (!st && e_out) st = jues_cc_energy(cc, e_out);
+        if (!st && (t1_out || t2_out)) st = jues_cc_amplitudes(cc, t1_out, t2_out);
+        if (!st && log) st = jues_cc_log(cc, log, log_cap, nullptr);
+        if (!st) st = jues_cc_pT(cc, op.precision, ept_out);
+        if (niter) *niter = (int)cc->s->iters;
+        jues_cc_destroy(cc);
+        if (!st && !conv && (op.r_conv > 0 || op.e_conv > 0) && op.maxit > 0) {
+            set_last_error("CC iterations did not converge within maxit");
+            st = JUES_ENOTCONV;
+        }
+        return st;
+    }
+    return cc_run(cc, opts, e_out, t1_out, t2_out, log, log_cap, niter);
 }
 
 int jues_pT(jues_ctx *ctx, const double *T1, const double *T2, const double *Vvvvo, const double *Vvooo,

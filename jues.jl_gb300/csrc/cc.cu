@@ -16,6 +16,7 @@
 
 #include "cc.cuh"
 #include "df.cuh"
+#include "fock.cuh"
 #include "transform.cuh"
 
 namespace jues {
@@ -293,7 +294,7 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         permute4(ctx, p, 1.0, s->ovov.p, 0.0, s->Tn.p);
         divide_by_d(ctx, s->Tn.p, s->eps.p, o, v, s->T.p);
     }
-    s->energy = cc_energy(ctx, s->oovv.p, s->T.p, method == 1 ? s->t1.p : nullptr, o, v);
+    s->energy = cc_total_energy(s.get());
     s->e_prev = s->energy;
     diis_reset(s.get());
     ctx->check_flags();
@@ -351,6 +352,63 @@ CCState *cc_create_df(Ctx *ctx, const double *b, int n, int naux, const double *
     return cc_finish(std::move(s));
 }
 
+double cc_total_energy(CCState *s) {
+    double e = cc_energy(s->ctx, s->oovv.p, s->T.p, s->method == 1 ? s->t1.p : nullptr, s->o, s->v);
+    if (s->fock && s->method == 1) e += 2.0 * dot(s->ctx, (size_t)s->o * s->v, s->fOV.p, s->t1.p);   // AutoRCCSD.jl:43
+    return e;
+}
+
+CCState *cc_create_auto(Ctx *ctx, const double *g, const double *h, int n, const double *C, int nmo, int ndocc,
+                        int fcn, const jues_cc_opts &opts) {
+    JUES_REQUIRE(n > 0 && nmo > 0 && nmo <= n, "need 0 < nmo <= nbf");
+    JUES_REQUIRE(ndocc > 0 && ndocc < nmo, "need 0 < ndocc < nmo");
+    JUES_REQUIRE(fcn >= 0 && fcn < ndocc, "need 0 <= fcn < ndocc");
+    const int o = ndocc - fcn, v = nmo - ndocc;
+    // Fock matrix of the orbitals (all ndocc occupied define the density), AutoRCCSD.jl:218-233
+    DBuf<double> f(ctx, (size_t)nmo * nmo);
+    get_fock(ctx, g, h, n, C, nmo, C, ndocc, f.p);
+    std::vector<double> hf((size_t)nmo * nmo);
+    JUES_CHECK_CUDA(cudaMemcpyAsync(hf.data(), f.p, hf.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    JUES_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    auto F = [&](int p, int q) { return hf[(size_t)p + (size_t)nmo * q]; };
+    // eps has nbf entries like the orbital energies it replaces (the sweeps read the first o + v)
+    std::vector<double> eps((size_t)n, 0.0), foo((size_t)o * o), fov((size_t)o * v), fvv((size_t)v * v);
+    for (int i = 0; i < o; ++i) eps[i] = F(fcn + i, fcn + i);
+    for (int a = 0; a < v; ++a) eps[o + a] = F(ndocc + a, ndocc + a);
+    for (int i = 0; i < o; ++i)
+        for (int j = 0; j < o; ++j) foo[i + (size_t)o * j] = i == j ? 0.0 : F(fcn + i, fcn + j);
+    for (int i = 0; i < o; ++i)
+        for (int a = 0; a < v; ++a) fov[i + (size_t)o * a] = F(fcn + i, ndocc + a);
+    for (int a = 0; a < v; ++a)
+        for (int b = 0; b < v; ++b) fvv[a + (size_t)v * b] = a == b ? 0.0 : F(ndocc + a, ndocc + b);
+    DBuf<double> deps(ctx, eps.size());
+    JUES_CHECK_CUDA(cudaMemcpyAsync(deps.p, eps.data(), eps.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                    ctx->stream));
+    // the active orbitals are column ranges of C: occupied fcn..ndocc-1, virtual ndocc..nmo-1
+    jues_cc_opts op = opts;
+    op.guess = JUES_GUESS_MP2;
+    std::unique_ptr<CCState> s(cc_create(ctx, 1, g, n, C + (size_t)n * fcn, o, C + (size_t)n * ndocc, v, deps.p, op));
+    auto up = [&](DBuf<double> &d, const std::vector<double> &hsrc) {
+        d = DBuf<double>(ctx, hsrc.size());
+        JUES_CHECK_CUDA(cudaMemcpyAsync(d.p, hsrc.data(), hsrc.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                        ctx->stream));
+    };
+    up(s->fOO, foo);
+    up(s->fOV, fov);
+    up(s->fVV, fvv);
+    s->fock = true;
+    s->auto_rms = true;
+    // T1 = f_ov / d (AutoRCCSD.jl:253), T2 = <ij|ab>/D already set
+    d2d(ctx, s->t1n.p, s->fOV.p, (size_t)o * v);
+    fill(ctx, s->t1.p, (size_t)o * v, 0.0);
+    t1_finalize(ctx, s->t1n.p, s->eps.p, o, v, s->t1.p);
+    std::swap(s->t1, s->t1n);
+    s->energy = cc_total_energy(s.get());
+    s->e_prev = s->energy;
+    ctx->check_flags();
+    return s.release();
+}
+
 // amplitude vector for DIIS: CCD = T2; CCSD = [t1; T2] packed in aux1
 static void cc_one(CCState *s, int prec) {
     Ctx *ctx = s->ctx;
@@ -387,7 +445,11 @@ static void cc_one(CCState *s, int prec) {
         if (s->method == 1) std::swap(s->t1, s->t1n);
     }
     s->e_prev = s->energy;
-    s->energy = cc_energy(ctx, s->oovv.p, s->T.p, s->method == 1 ? s->t1.p : nullptr, s->o, s->v);
+    s->energy = cc_total_energy(s);
+    if (s->auto_rms) {
+        const double n1 = (double)s->o * s->v, n2 = n1 * n1;
+        rn = std::max(std::sqrt(s->r1sq) / n1, std::sqrt(s->r2sq) / n2);
+    }
     JUES_CHECK_CUDA(cudaEventRecord(e1, ctx->stream));
     JUES_CHECK_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -517,6 +579,17 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(0), 0.0, s->Fme.p, plain(1), plain(0));
     G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, -1.0, W, mode2(o, o, oo), mode2(o, 1, oov), t1, plain(1),
       plain(0), 1.0, s->Fme.p, plain(1), plain(0));
+    if (s->fock) {
+        // non-canonical Fock terms: Fae += f_ae - 1/2 f_me t1[m,a], Fmi += f_mi + 1/2 t1[i,e] f_me,
+        // Fme += f_me (the diagonals of f_oo and f_vv are zero; they sit in the resolvents)
+        axpby(ctx, (size_t)vv, 1.0, s->fVV.p, 1.0, s->Fae.p, s->Fae.p);
+        G(s, JUES_PREC_FP64, "ccsd_fock", v, v, o, -0.5, t1, plain(o), plain(1), s->fOV.p, plain(1), plain(o),
+          1.0, s->Fae.p, plain(1), plain(v));
+        axpby(ctx, (size_t)oo, 1.0, s->fOO.p, 1.0, s->Fmi.p, s->Fmi.p);
+        G(s, JUES_PREC_FP64, "ccsd_fock", o, o, v, 0.5, s->fOV.p, plain(1), plain(o), t1, plain(o), plain(1),
+          1.0, s->Fmi.p, plain(1), plain(o));
+        axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, s->Fme.p, s->Fme.p);
+    }
 
     // W' = oooo + t1[j,e] ooov[m,n,i,e] + t1[i,e] ooov[n,m,j,e] + sum_ef oovv[mn,ef] (T2+tau)[ij,ef]
     G(s, JUES_PREC_FP64, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
@@ -615,10 +688,13 @@ double ccsd_sweep(CCState *s, int prec) {
     G(s, JUES_PREC_FP64, "ccsd_z_ooov", oov, v, o, -1.0, ooov, mode3(o, o, oo, o, ooo), plain(1), t1,
       plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
 
+    if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia
     double r2 = t2_finalize(ctx, s->L.p, Z, s->eps.p, (int)o, (int)v, T, s->Tn.p);
     // t1n = R1 / D_ia and its step norm
-    r2 += t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, t1);
-    return r2;
+    const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, t1);
+    s->r1sq = r1;
+    s->r2sq = r2;
+    return r2 + r1;
 }
 
 }  // namespace jues

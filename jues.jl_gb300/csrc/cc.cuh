@@ -32,6 +32,12 @@ struct CCState {
     bool cache_operands = false;   // keep split packs of sweep operands (CCD only)   // split precision: closing FP64 sweeps left (-1 = not started)
     bool converged = false;
     bool reference_df_wmbej = false;   // DF-RCCD.jl's index order in WmBeJ's last term
+    // general (non-canonical) Fock matrix, AutoRCCSD.jl: off-diagonal occupied and virtual
+    // blocks and the occupied-virtual block; eps then holds the Fock diagonal
+    bool fock = false;
+    DBuf<double> fOO, fOV, fVV;
+    bool auto_rms = false;       // rnorm = max(||dT1||/len(T1), ||dT2||/len(T2)) (AutoRCCSD.jl:172-174)
+    double r1sq = 0.0, r2sq = 0.0;   // squared step norms of the last sweep
     std::vector<jues_iter_log> log;
     double sweep_flops(int prec) const;
 };
@@ -43,6 +49,12 @@ CCState *cc_create(Ctx *ctx, int method, const double *gao_dev, int n, const dou
 CCState *cc_create_df(Ctx *ctx, const double *b, int n, int naux, const double *Cocc_dev, int o,
                       const double *Cvir_dev, int v, const double *eps_dev, const jues_cc_opts &opts,
                       bool reference_wmbej);
+// CCSD from a general Fock matrix, AutoRCCSD.do_rccsd (AutoRCCSD.jl:193-300): f = get_fock of
+// the orbitals C (n x nmo; the first ndocc occupied), fcn frozen core orbitals, T1 = f_ov/d,
+// T2 = <ij|ab>/D, per-element rms convergence
+CCState *cc_create_auto(Ctx *ctx, const double *gao_dev, const double *hao_dev, int n, const double *C_dev, int nmo,
+                        int ndocc, int fcn, const jues_cc_opts &opts);
+double cc_total_energy(CCState *s);   // CC energy including 2 f_ov . t1 when a Fock matrix is set
 void cc_iterate(CCState *s, int nsweeps, int *done, int *converged);
 void cc_amplitudes(CCState *s, double *t1_host, double *t2_host);
 // one CCD / CCSD sweep: Tn from T (and t1n from t1), returns the squared step norm

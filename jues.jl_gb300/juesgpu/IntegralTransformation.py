@@ -37,3 +37,25 @@ def get_eri(wfn, eri_string: str, notation: str = "phys", fcn: int = 0, *,
                                     Cv.shape[1], eri_string.encode(), 1 if notation == "phys" else 0,
                                     fcn, _lib.PREC[precision], _lib.ptr(out)))
     return out
+
+
+def get_fock(wfn, spin: str = "alpha", *, device: int = 0) -> np.ndarray:
+    """``get_fock(wfn; spin)`` (src/Backend/IntegralTransformation.jl:119-141): the Fock matrix
+    of the determinant in the basis of ``wfn.Ca`` (``Cb`` for beta), built on the device."""
+    import ctypes as C
+    sp = spin.lower()
+    if sp in ("alpha", "up", "a"):
+        Cm, Co = wfn.Ca, wfn.Cao
+    elif sp in ("beta", "down", "b"):
+        Cm, Co = wfn.Cb, wfn.Cbo
+    else:
+        raise ValueError(f"Invalid Spin option given to get_fock: {spin}")
+    g = _lib.f64(wfn.ao_eri)
+    h = _lib.f64(wfn.hao)
+    Cm = _lib.f64(Cm)
+    n, nmo = Cm.shape
+    f = np.empty((nmo, nmo), order="F")
+    ctx = _lib.context(device)
+    _lib.check(ctx.lib.jues_get_fock(ctx.h, _lib.ptr(g), _lib.ptr(h), n, _lib.ptr(Cm), nmo,
+                                     int(np.asarray(Co).shape[1]), _lib.ptr(f)))
+    return f

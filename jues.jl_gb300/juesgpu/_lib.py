@@ -93,6 +93,9 @@ SIGNATURES = {
     "jues_df_rccd": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts),
                                C.c_int, DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
     "jues_pT": (C.c_int, [VP, DP, DP, DP, DP, DP, DP, DP, C.c_int, C.c_int, C.c_int, DP]),
+    "jues_get_fock": (C.c_int, [VP, DP, DP, C.c_int, DP, C.c_int, C.c_int, DP]),
+    "jues_auto_rccsd": (C.c_int, [VP, DP, DP, C.c_int, DP, C.c_int, C.c_int, C.c_int, C.POINTER(CCOpts), C.c_int,
+                                  DP, DP, DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
     "jues_cc_pT": (C.c_int, [VP, C.c_int, DP]),
     "jues_cc_iterate": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "jues_cc_set_precision": (C.c_int, [VP, C.c_int]),

@@ -249,4 +249,44 @@ function compute_pT(; T1, T2, Vvvvo, Vvooo, Vvovo, fo, fv, precision::Symbol = :
     return e[]
 end
 
+"get_fock(wfn; spin = \"alpha\") -- IntegralTransformation.jl:119-141"
+function get_fock(wfn::Wfn; spin = "alpha")
+    sp = lowercase(spin)
+    C, Co = sp in ("alpha", "up", "a") ? (wfn.Ca, wfn.Cao) :
+            sp in ("beta", "down", "b") ? (wfn.Cb, wfn.Cbo) :
+            error("Invalid Spin option given to JuES.IntegralTransformation.get_fock: $spin")
+    Cm = f64(C)
+    n, nmo = size(Cm)
+    f = Array{Float64}(undef, nmo, nmo)
+    check(ccall((:jues_get_fock, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Cint, Ptr{Cdouble}),
+                ctx(), f64(wfn.ao_eri), f64(wfn.hao), n, Cm, nmo, size(Co, 2), f))
+    return f
+end
+
+"""
+    auto_rccsd(wfn; cc_max_iter = 50, cc_max_rms = 1e-10, cc_e_conv = 1e-10, diis = false,
+               do_pT = false, fcn = 0, precision = :fp64) -- AutoRCCSD.jl:193-300
+
+CCSD from the Fock matrix of the orbitals (non-canonical and non-HF references); returns the
+correlation energy, or `(E, E_T)` with `do_pT`.
+"""
+function auto_rccsd(wfn::Wfn; cc_max_iter = 50, cc_max_rms = 1e-10, cc_e_conv = 1e-10, diis = false,
+                    do_pT = false, fcn = 0, precision::Symbol = :fp64)
+    Cm = f64(wfn.Ca)
+    n, nmo = size(Cm)
+    ndocc = (wfn.nalpha + wfn.nbeta) ÷ 2
+    opts = Ref(CCOpts(cc_max_iter, cc_e_conv, cc_max_rms, Cint(diis), 6, PREC[precision], GUESS[:mp2], 0, Cint(-1)))
+    e = Ref{Cdouble}(0.0)
+    ept = Ref{Cdouble}(0.0)
+    nit = Ref{Cint}(0)
+    st = ccall((:jues_auto_rccsd, LIB), Cint,
+               (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Cint, Cint, Ref{CCOpts}, Cint,
+                Ref{Cdouble}, Ref{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{IterLog}, Cint, Ref{Cint}),
+               ctx(), f64(wfn.ao_eri), f64(wfn.hao), n, Cm, nmo, ndocc, fcn, opts, Cint(do_pT), e, ept,
+               C_NULL, C_NULL, C_NULL, 0, nit)
+    st == ENOTCONV ? @warn(lasterror()) : check(st)
+    return do_pT ? (e[], ept[]) : e[]
+end
+
 end # module

@@ -270,3 +270,40 @@ def test_pT_oracle_equals_spin_orbital_triples_on_h2o():
     assert abs(e_t - triples.compute_pT_loops(*args)) < 1e-15
     e_so = _spin_orbital_pT(w, t1, T2)
     assert e_t < 0 and abs(e_t - e_so) < 1e-12, (e_t, e_so)
+
+
+def _h2o_rotated(scale, seed=3):
+    """H2O/STO-3G with its occupied and virtual orbitals each mixed by exp(scale * A), A
+    antisymmetric: a non-canonical but equivalent reference."""
+    from scipy.linalg import expm
+    d = np.load(os.path.join(GOLDEN, "h2o_sto3g.npz"))
+    o, n = int(d["nocc"]), d["C"].shape[1]
+    rng = np.random.default_rng(seed)
+    Ao = rng.standard_normal((o, o))
+    Av = rng.standard_normal((n - o, n - o))
+    C = d["C"].copy()
+    C[:, :o] = C[:, :o] @ expm(scale * (Ao - Ao.T))
+    C[:, o:] = C[:, o:] @ expm(scale * (Av - Av.T))
+    return wfn_from_rhf(C, d["eps"], d["ao_eri"], o, hao=d["H"])
+
+
+def test_auto_rccsd_oracle_pins():
+    # AutoRCCSD.jl restated: the canonical H2O energy is the reference's CCSD known answer, the
+    # Fock matrix of the RHF orbitals is diagonal with the orbital energies, a rotation of the
+    # occupied and of the virtual orbitals leaves the energy unchanged, and with one frozen
+    # core orbital it equals the canonical CCSD of the active space
+    from oracle import auto_rccsd
+    w = _h2o_rotated(0.0)
+    f = auto_rccsd.get_fock(w.Ca, w.Cao, w.ao_eri, w.hao)
+    assert np.abs(np.diag(f) - w.epsa).max() < 1e-10
+    assert np.abs(f - np.diag(np.diag(f))).max() < 1e-10
+    e = auto_rccsd.do_rccsd(w)
+    assert abs(e - E_CCSD_H2O) < 1e-9
+    e_rot = auto_rccsd.do_rccsd(_h2o_rotated(0.1))
+    assert abs(e_rot - e) < 1e-9
+    e_fc = auto_rccsd.do_rccsd(w, fcn=1)
+    import dataclasses
+    act = dataclasses.replace(w, nalpha=w.nalpha - 1, nbeta=w.nalpha - 1, Cao=w.Cao[:, 1:], Cbo=w.Cao[:, 1:],
+                              epsa=w.epsa[1:], epsb=w.epsa[1:])
+    assert abs(e_fc - ccsd.do_rccsd(act, maxit=80, diis=True)) < 1e-9
+    assert abs(e_fc - e) > 1e-5
