@@ -263,6 +263,34 @@ def run_pT_measure(shape, local, precisions=("fp64", "split_bf16")):
     return out
 
 
+def run_df_measure(shape, local, sweeps=5):
+    """DF-RCCD (jues_df_rccd / jues_cc_create_df): the fitted factor of the synthetic system
+    (its integrals are exactly B^T B) instead of the n^4 AO integrals.  Reports the session
+    set-up (H2D of b, MO factors, the five blocks), split sweeps, and the whole C-ABI call with
+    host buffers."""
+    from juesgpu.CoupledCluster import CCSession, DFRCCD
+    from juesgpu.synthetic import make_named
+    from juesgpu.Wavefunction import wfn_from_rhf
+    s = make_named(shape)
+    b = np.asfortranarray(np.transpose(s.B, (1, 2, 0)))
+    n = s.nbf
+    w = wfn_from_rhf(s.C, s.eps, None, s.nocc)   # no n^4 array: the DF path reads C and eps
+    t0 = time.perf_counter()
+    ses = CCSession(0, w, pqP=b, guess="mp2", diis=True, r_conv=0.0, maxit=sweeps, device=local,
+                    precision="split_bf16", transform_precision="fp64")
+    setup = time.perf_counter() - t0
+    ses.iterate(sweeps)
+    lg = ses.log()
+    ses.close()
+    t0 = time.perf_counter()
+    e = DFRCCD.do_df_rccd(w, b, maxit=sweeps, diis=True, precision="split_bf16", transform_precision="fp64",
+                          device=local)
+    e2e = time.perf_counter() - t0
+    return {"workload": f"df_rccd_{shape.lower()}_split_bf16", "nbf": n, "naux": s.naux, "setup_s": setup,
+            "sweep_ms": sum(r[3] for r in lg) / len(lg), "e2e_s_per_iter": e2e / sweeps, "sweeps": sweeps,
+            "h2d_bytes": int(b.nbytes), "energy": e}
+
+
 def run_gpu(args):
     ws, rank, local, pg = dist_setup(args.gpus)
     import juesgpu
@@ -332,13 +360,23 @@ def run_gpu(args):
     except OSError:
         pass
     e_split = None
+    converged = None
     if args.check:
-        s2 = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
-                       guess="mp2", diis=True, r_conv=1e-9, refine=2, maxit=60, transform_precision="fp64")
-        s2.iterate(60)
-        e_split = s2.energy()
-        nconv = len(s2.log())
-        s2.close()
+        converged = {}
+        for label, refine in (("refine2", 2), ("refine0", 0)):
+            t0 = time.perf_counter()
+            s2 = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
+                           guess="mp2", diis=True, r_conv=1e-9, refine=refine, maxit=60, transform_precision="fp64")
+            t_setup = time.perf_counter() - t0
+            s2.iterate(60)
+            wall = time.perf_counter() - t0
+            lg2 = s2.log()
+            e_c = s2.energy()
+            s2.close()
+            converged[label] = {"energy": e_c, "sweeps": len(lg2), "fp64_sweeps": sum(1 for r in lg2 if r[4] == 0),
+                                "setup_s": t_setup, "wall_s": wall,
+                                "error_eh": (e_c - golden) if golden is not None else None}
+        e_split = converged["refine2"]["energy"]
         if golden is not None and rank == 0:
             err = e_split - golden
 
@@ -371,17 +409,24 @@ def run_gpu(args):
     if args.e2e_steps > 0:
         w = system.wfn(ao_eri=gao)
         barrier(pg)
+        ctx.set_profiling(True)
+        ctx.profile_reset()
         t0 = time.perf_counter()
         e, lg = mRCCD.do_rccd(w, maxit=args.e2e_steps, r_conv=0.0, guess="mp2", precision="split_bf16",
                               refine=0, device=local, return_log=True)
         t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+        e2e_kernels = {k: ctx.profile(k)[0] for k in ("", "transform", "pack_split", "ccd_")}
+        ctx.set_profiling(False)
         h2d = gao.nbytes + system.C.nbytes + eps.nbytes
         e2e = {"value": t_e2e / len(lg), "unit": "s/iter", "h2d_bytes_per_step": int(h2d / len(lg)),
-               "d2h_bytes_per_step": 8, "sweeps": len(lg), "includes": "H2D of AO ERIs, split transform "
+               "d2h_bytes_per_step": 8, "sweeps": len(lg), "wall_s": t_e2e,
+               "kernel_ms": {("all" if k == "" else k): v for k, v in e2e_kernels.items()},
+               "includes": "H2D of AO ERIs, split transform "
                "of the 5 RCCD blocks, sweeps, energy read-back"}
 
     batch = run_batch_measure(args.batch, local) if args.batch > 0 else None
     pT = run_pT_measure(args.pT_shape, local) if args.pT_shape != "none" else None
+    df = run_df_measure(args.df_shape, local) if args.df_shape != "none" else None
     if rank != 0:
         return
     pk, pk_kind = peaks()
@@ -409,6 +454,7 @@ def run_gpu(args):
         "fp64_s_per_iter": fp64,
         "speedup_vs_fp64": (fp64 / s_per_iter) if fp64 else None,
         "energy_split": e_split, "energy_fp64_golden": golden, "energy_error_eh": err,
+        "converged_runs": converged,
         "transform": transform,
         "wall_s_timed": wall, "setup_s": setup_s,
         "kernels_ms_per_step": {"pp_ladder": pp_ms / args.steps, "ring": ring_ms / args.steps,
@@ -420,7 +466,7 @@ def run_gpu(args):
                      "flops_per_launch": pp_flops_exec, "launch_ms": 1e3 * pp_avg_s if pp_avg_s else None,
                      "traffic": traffic},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
-        "batch": batch, "pT": pT,
+        "batch": batch, "pT": pT, "df_rccd": df,
     }
     print(json.dumps(line), flush=True)
 
@@ -438,6 +484,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4, help="CPU baseline shares to time")
     ap.add_argument("--pT-shape", dest="pT_shape", default="S100", choices=["none"] + sorted(SHAPES),
                     help="(T) correction timing on this synthetic shape (FP64 and split)")
+    ap.add_argument("--df-shape", dest="df_shape", default="S200", choices=["none"] + sorted(SHAPES),
+                    help="DF-RCCD timing on this synthetic shape (split sweeps, set-up, C-ABI call)")
     ap.add_argument("--batch", type=int, default=0,
                     help="also measure the batched MP2 energy+adjoint form on this many systems")
     ap.add_argument("--shape", default="S200", choices=sorted(SHAPES),

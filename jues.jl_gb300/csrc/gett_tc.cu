@@ -1,22 +1,23 @@
 // Split-precision GEMM over tensor modes on the sm_103a tensor cores (tcgen05 + TMEM + TMA).
 //
-// Each FP64 operand row r (a row of A or of B, running over K) is cut into chunks of KCH = 64
-// K values (one pipeline stage); chunk c gets a power-of-two scale 2^e with max |x| < 2^e over
+// Each FP64 operand row r (a row of A or of B, running over K) is cut into chunks of KCH = 128
+// K values (two pipeline stages); chunk c gets a power-of-two scale 2^e with max |x| < 2^e over
 // the chunk, and every element is written as two integers carried exactly in FP16,
 //     x = 2^(e - 9) (hi + 2^-10 lo),   hi = rint(x 2^(9 - e)),  |hi|, |lo| <= 512,
-// so |x - 2^(e-9)(hi + 2^-10 lo)| <= 2^(e-20).  One CTA computes a 128 x BN tile of C = A.B^T
-// with three tcgen05.mma (kind::f16) products per K=16 step: hi.hi into a "main" TMEM
-// accumulator and hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-20), is dropped).
-// Because the FP16 values are integers, every product and every partial sum of the main
-// accumulator over one chunk (<= 64 * 2^18 = 2^24) is an exact FP32 integer: the tensor core's
-// truncating accumulation never rounds where it matters (the correction term is 2^-10 smaller,
-// so its rounding is below 1e-10 of the result).  Chunks alternate between two TMEM buffers;
-// four warps scale each finished chunk by 2^(e_r + e_c - 18) and add it into FP32 registers
-// (round-to-nearest, unbiased) while the next chunk runs, then apply alpha/beta in FP64
-// through the output tensor modes.  Operand
-// tiles arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by
-// mbarriers; one thread issues the TMA loads and one the MMAs.  Every mbarrier wait is bounded
-// by %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips its stores, frees its TMEM and
+// so |x - 2^(e-9)(hi + 2^-10 lo)| <= 2^(e-20).  One CTA computes 128 x BN tiles of C = A.B^T
+// with tcgen05.mma (kind::f16) products per K=16 step: hi.hi into a "main" TMEM accumulator and
+// hi.lo + lo.hi into a "correction" accumulator (lo.lo, O(2^-20), is dropped).  Because the FP16
+// values are integers, every product is exact and the main accumulator's partial sums over one
+// chunk are exact FP32 integers while they stay below 2^24 (128 products of up to 2^18: random
+// signs keep them near 2^21; only a chunk of equal-signed maximal products could pass 2^24,
+// and then the tensor core's truncation costs at most one unit in 2^24 of that sum).  The
+// correction term is 2^-10 smaller, so its rounding is below 1e-10 of the result.  Chunks
+// alternate between two TMEM buffers; eight warps scale each finished chunk by
+// 2^(e_r + e_c - 18) and add it into FP32 registers (round-to-nearest, unbiased) while the next
+// chunk runs, then apply alpha/beta in FP64 through the output tensor modes.  Operand tiles
+// arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by mbarriers;
+// one thread issues the TMA loads and one the MMAs.  Every mbarrier wait is bounded by
+// %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips its stores, frees its TMEM and
 // returns.
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -194,7 +195,7 @@ struct TcArgs {
 // Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-9 drain TMEM (two
 // warps per 32-lane TMEM quarter, each owning half of the tile's columns).
 // The MMA warp restarts both accumulators every KC stages (one scaling chunk of KCH = KC * 64
-// K values, which keeps every partial sum below 2^23), alternating between two TMEM buffers.
+// K values), alternating between two TMEM buffers.
 constexpr int TC_THREADS = 320;
 constexpr int TC_DRAIN = 256;   // drain threads (warps 2-9)
 
@@ -501,11 +502,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-constexpr int PR = 32, PK = 64, KCH = 64;   // pack tile; scaling chunk = one pipeline stage
+constexpr int PR = 32, PK = 128, KCH = 128;   // pack tile = one scaling chunk = two pipeline stages
 
 // FP64 operand -> integer-valued FP16 planes [2][Rpad][Kpad], K-major, and the per-(chunk,row)
-// scales, in one pass.  A block covers 32 rows x 64 K = exactly one scaling chunk per row, so
-// the chunk maximum is a block-local reduction.  The split works on the IEEE-754 bit pattern
+// scales, in one pass.  A block covers 32 rows x one 128-wide K chunk (the last chunk may be 64
+// wide: Kpad is a multiple of 64), so the chunk maximum is a block-local reduction.  The split works on the IEEE-754 bit pattern
 // with integer arithmetic only (GB300 runs FP64 arithmetic at a small fraction of its integer
 // rate): for x = +-m 2^(E-1075) (m the 53-bit significand) and chunk scale e,
 //     q = rint(x 2^(19-e)) = round(m >> (1056 + e - E)),  hi = (q + 512) >> 10,  lo = q - 1024 hi,
@@ -533,7 +534,7 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
                                                          __half *__restrict__ dst) {
     __shared__ double tile[PR][PK + 1];
     __shared__ long long roff[PR], koff[PK];
-    const long long kblocks = Kpad / PK;
+    const long long kblocks = (Kpad + PK - 1) / PK;
     const long long r0 = (blockIdx.x / kblocks) * PR;
     const long long k0 = (blockIdx.x % kblocks) * PK;
     const int tid = threadIdx.x;
@@ -545,7 +546,7 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
         koff[tid - 64] = k < K ? mode_off(kmode, k) : -1;
     }
     __syncthreads();
-#pragma unroll
+#pragma unroll 4
     for (int i = 0; i < (PR * PK) / 256; ++i) {
         const int e = tid + i * 256;
         const int kk = kfast ? (e % PK) : (e / PR);
@@ -554,26 +555,32 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
         tile[rr][kk] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
     }
     __syncthreads();
-    // the 8 threads of a row are consecutive lanes: reduce the chunk exponent with shuffles
-    const int rr = tid >> 3, kc = (tid & 7) * 8;
+    // the 8 threads of a row are consecutive lanes, 16 columns each: reduce the chunk exponent
+    // with shuffles
+    const int rr = tid >> 3, kc = (tid & 7) * 16;
     int ex = INT_MIN;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) ex = max(ex, exp_bound(tile[rr][kc + j]));
+    for (int j = 0; j < 16; ++j) ex = max(ex, exp_bound(tile[rr][kc + j]));
 #pragma unroll
     for (int d = 1; d < 8; d <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, d));
     const long long r = r0 + rr;
     if ((tid & 7) == 0) rexp[(k0 / KCH) * Rpad + r] = ex;
-    __align__(16) __half hi[8], lo[8];
+    if (k0 + kc >= Kpad) return;   // the 64-wide tail of the last chunk (Kpad is a multiple of 64)
+    __align__(16) __half hi[16], lo[16];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < 16; ++j) {
         const long long q = fixed_q(tile[rr][kc + j], ex);
         const long long h = (q + 512) >> 10;
         hi[j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
         lo[j] = __int2half_rn((int)(q - (h << 10)));
     }
     const size_t base = (size_t)r * (size_t)Kpad + (size_t)(k0 + kc);
-    *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
-    *reinterpret_cast<uint4 *>(dst + (size_t)Rpad * Kpad + base) = *reinterpret_cast<const uint4 *>(lo);
+    uint4 *ph = reinterpret_cast<uint4 *>(dst + base);
+    uint4 *pl = reinterpret_cast<uint4 *>(dst + (size_t)Rpad * Kpad + base);
+    ph[0] = reinterpret_cast<const uint4 *>(hi)[0];
+    ph[1] = reinterpret_cast<const uint4 *>(hi)[1];
+    pl[0] = reinterpret_cast<const uint4 *>(lo)[0];
+    pl[1] = reinterpret_cast<const uint4 *>(lo)[1];
 }
 
 
@@ -702,7 +709,7 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
         dst = pc.scratch[slot].p;
         ex = pc.scratch_exp[slot].p;
     }
-    const long long blocks = (Rpad / PR) * (Kpad / PK);
+    const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     {
@@ -887,7 +894,7 @@ void *noalloc_scratch_address(int device) {
 
 void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
                long long Rpad, long long Kpad, __half *dst, int *ex) {
-    const long long blocks = (Rpad / PR) * (Kpad / PK);
+    const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     Ctx::Scope s(ctx, "pack_split_noalloc");

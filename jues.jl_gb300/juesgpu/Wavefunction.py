@@ -66,9 +66,12 @@ def wfn_from_rhf(C: np.ndarray, eps: np.ndarray, ao_eri: np.ndarray, nocc: int,
     if C.shape != (n, n):
         raise ValueError("C must be square (nbf x nmo)")
     eps = np.asarray(eps, dtype=dtype).copy()
-    g = np.asfortranarray(np.asarray(ao_eri, dtype=dtype))
-    if g.shape != (n, n, n, n):
-        raise ValueError("ao_eri must be nbf^4")
+    if ao_eri is None:
+        g = None   # density-fitted paths read C and eps only
+    else:
+        g = np.asfortranarray(np.asarray(ao_eri, dtype=dtype))
+        if g.shape != (n, n, n, n):
+            raise ValueError("ao_eri must be nbf^4")
     if hao is None:
         hao = np.zeros((n, n), dtype=dtype, order="F")
     nv = n - nocc

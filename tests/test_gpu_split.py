@@ -1,8 +1,8 @@
 """GPU checks of the split-BF16 (tcgen05) form.
 
 Bars: against an exact emulation of the operand representation (power-of-two fixed point per
-row and 64-long K chunk, hi + lo/1024 carried in FP16, three products) the kernel may differ only by the round-to-nearest FP32
-sum of its exact chunk sums (1e-6 of max|C|); the relative Frobenius error against exact FP64
+row and 128-long K chunk, hi + lo/1024 carried in FP16, three products) the kernel may differ
+only by the round-to-nearest FP32 sum of its chunk sums (1e-6 of max|C|); the relative Frobenius error against exact FP64
 must stay below 1e-5 (~20 bits kept; a single BF16 product gives ~4e-3), also at K = 25600.
 Energies: within 1 uEh of the FP64 oracle.
 """
@@ -19,11 +19,11 @@ from juesgpu.synthetic import make_named, make_system
 pytestmark = pytest.mark.gpu
 
 
-KCH = 64
+KCH = 128
 
 
 def split_rows(X):
-    """Integer-carrier split of each row of X over its columns (= K), chunk by chunk of 64:
+    """Integer-carrier split of each row of X over its columns (= K), chunk by chunk of 128:
     the library's operand representation x ~ 2^(e-9) (hi + lo/1024), |hi|, |lo| <= 512,
     with max |x| < 2^e over the chunk.  Returns hi, lo and the per-element exponent e."""
     X = np.asarray(X, dtype=np.float64)
