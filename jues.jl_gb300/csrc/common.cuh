@@ -86,6 +86,7 @@ struct Ctx {
     BatchCache *batch = nullptr;       // owned; destroyed by batch_cache_destroy
     void *splitk_ws = nullptr;         // split-K partial sums, grown on demand
     size_t splitk_bytes = 0;
+    cudaMemPool_t pool = nullptr;      // stream-ordered pool behind alloc/free (keeps freed memory)
     Ctx();
     ~Ctx();
 

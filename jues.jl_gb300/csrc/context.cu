@@ -1,6 +1,7 @@
 // Context: stream, memory accounting, per-kernel event timing, error flags.
 #include <nvtx3/nvToolsExt.h>
 
+#include <cstdint>
 #include <cstring>
 
 #include <algorithm>
@@ -25,7 +26,10 @@ Ctx::~Ctx() {
         for (auto &e : kv.second.pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto &e : kv.second.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
     }
-    if (splitk_ws) cudaFree(splitk_ws);
+    if (splitk_ws) free(splitk_ws, splitk_bytes);
+    splitk_ws = nullptr;
+    if (stream) cudaStreamSynchronize(stream);
+    if (pool) cudaMemPoolDestroy(pool);   // returns everything the pool still holds
     if (d_flags) cudaFree(d_flags);
     if (d_red) cudaFree(d_red);
     if (stream) cudaStreamDestroy(stream);
@@ -38,11 +42,33 @@ void *Ctx::alloc(size_t bytes) {
                                      " bytes exceeds the context memory limit (" +
                                      std::to_string(mem_limit) + " bytes, " +
                                      std::to_string(mem_used) + " in use)");
+    // Stream-ordered allocation from the context's own pool.  Freed blocks stay in the pool
+    // (release threshold = unlimited) and are handed out again in stream order, so the large
+    // per-call buffers (AO integrals, packed operands, transform scratch) cost no
+    // cudaMalloc/cudaFree round trips and no implicit device synchronisation after warm-up.
+    if (!pool) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        JUES_CHECK_CUDA(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = UINT64_MAX;
+        JUES_CHECK_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
     void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, stream);
+    if (e != cudaSuccess) {
+        // give the pool's idle blocks back and try once more (fragmentation)
+        cudaGetLastError();
+        cudaStreamSynchronize(stream);
+        cudaMemPoolTrimTo(pool, 0);
+        e = cudaMallocFromPoolAsync(&p, bytes, pool, stream);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
-        throw Error(JUES_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+        throw Error(JUES_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: " +
                                      cudaGetErrorString(e));
     }
     mem_used += bytes;
@@ -51,13 +77,13 @@ void *Ctx::alloc(size_t bytes) {
 
 void Ctx::free(void *p, size_t bytes) {
     if (!p) return;
-    cudaFree(p);
+    cudaFreeAsync(p, stream);   // reusable by later work on this stream once its readers are done
     mem_used -= bytes;
 }
 
 void *Ctx::splitk_scratch(size_t bytes) {
     if (bytes > splitk_bytes) {
-        // cudaFree waits for the device, so no launch still reads the old buffer
+        // stream-ordered: launches queued before still read the old buffer before it is reused
         free(splitk_ws, splitk_bytes);
         splitk_ws = nullptr;
         splitk_bytes = 0;

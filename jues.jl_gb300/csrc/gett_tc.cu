@@ -502,11 +502,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-constexpr int PR = 32, PK = 128, KCH = 128;   // pack tile = one scaling chunk = two pipeline stages
+constexpr int PR = 16, PK = 128, KCH = 128;   // pack tile = one scaling chunk = two pipeline stages
 
 // FP64 operand -> integer-valued FP16 planes [2][Rpad][Kpad], K-major, and the per-(chunk,row)
-// scales, in one pass.  A block covers 32 rows x one 128-wide K chunk (the last chunk may be 64
-// wide: Kpad is a multiple of 64), so the chunk maximum is a block-local reduction.  The split works on the IEEE-754 bit pattern
+// scales, in one pass.  A block covers 16 rows x one 128-wide K chunk (the last chunk may be 64
+// wide: Kpad is a multiple of 64), so the chunk maximum is a block-local reduction.  Each row
+// is handled by 16 consecutive lanes taking every 16th column (conflict-free shared-memory
+// reads); the FP16 planes are staged in shared memory and written as 16-byte rows.  The split works on the IEEE-754 bit pattern
 // with integer arithmetic only (GB300 runs FP64 arithmetic at a small fraction of its integer
 // rate): for x = +-m 2^(E-1075) (m the 53-bit significand) and chunk scale e,
 //     q = rint(x 2^(19-e)) = round(m >> (1056 + e - E)),  hi = (q + 512) >> 10,  lo = q - 1024 hi,
@@ -533,6 +535,7 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
                                                          long long Kpad, int kfast, int *__restrict__ rexp,
                                                          __half *__restrict__ dst) {
     __shared__ double tile[PR][PK + 1];
+    __shared__ __align__(16) __half outp[2][PR][PK];
     __shared__ long long roff[PR], koff[PK];
     const long long kblocks = (Kpad + PK - 1) / PK;
     const long long r0 = (blockIdx.x / kblocks) * PR;
@@ -546,7 +549,7 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
         koff[tid - 64] = k < K ? mode_off(kmode, k) : -1;
     }
     __syncthreads();
-#pragma unroll 4
+#pragma unroll
     for (int i = 0; i < (PR * PK) / 256; ++i) {
         const int e = tid + i * 256;
         const int kk = kfast ? (e % PK) : (e / PR);
@@ -555,32 +558,32 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
         tile[rr][kk] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
     }
     __syncthreads();
-    // the 8 threads of a row are consecutive lanes, 16 columns each: reduce the chunk exponent
-    // with shuffles
-    const int rr = tid >> 3, kc = (tid & 7) * 16;
+    // 16 lanes per row, lane t owns columns t, t + 16, ..., t + 112
+    const int rr = tid >> 4, t = tid & 15;
     int ex = INT_MIN;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) ex = max(ex, exp_bound(tile[rr][kc + j]));
+    for (int j = 0; j < PK / 16; ++j) ex = max(ex, exp_bound(tile[rr][t + 16 * j]));
 #pragma unroll
-    for (int d = 1; d < 8; d <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, d));
-    const long long r = r0 + rr;
-    if ((tid & 7) == 0) rexp[(k0 / KCH) * Rpad + r] = ex;
-    if (k0 + kc >= Kpad) return;   // the 64-wide tail of the last chunk (Kpad is a multiple of 64)
-    __align__(16) __half hi[16], lo[16];
+    for (int d = 1; d < 16; d <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, d));
+    if (t == 0) rexp[(k0 / KCH) * Rpad + r0 + rr] = ex;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const long long q = fixed_q(tile[rr][kc + j], ex);
+    for (int j = 0; j < PK / 16; ++j) {
+        const long long q = fixed_q(tile[rr][t + 16 * j], ex);
         const long long h = (q + 512) >> 10;
-        hi[j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
-        lo[j] = __int2half_rn((int)(q - (h << 10)));
+        outp[0][rr][t + 16 * j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
+        outp[1][rr][t + 16 * j] = __int2half_rn((int)(q - (h << 10)));
     }
-    const size_t base = (size_t)r * (size_t)Kpad + (size_t)(k0 + kc);
-    uint4 *ph = reinterpret_cast<uint4 *>(dst + base);
-    uint4 *pl = reinterpret_cast<uint4 *>(dst + (size_t)Rpad * Kpad + base);
-    ph[0] = reinterpret_cast<const uint4 *>(hi)[0];
-    ph[1] = reinterpret_cast<const uint4 *>(hi)[1];
-    pl[0] = reinterpret_cast<const uint4 *>(lo)[0];
-    pl[1] = reinterpret_cast<const uint4 *>(lo)[1];
+    __syncthreads();
+    // 2 planes x PR rows x 16 segments of 8 halves
+#pragma unroll
+    for (int i = 0; i < (2 * PR * (PK / 8)) / 256; ++i) {
+        const int idx = tid + 256 * i;
+        const int seg = idx & 15, row = (idx >> 4) % PR, plane = idx / (16 * PR);
+        const long long k = k0 + 8 * seg;
+        if (k >= Kpad) continue;   // the 64-wide tail of the last chunk (Kpad is a multiple of 64)
+        *reinterpret_cast<uint4 *>(dst + (size_t)plane * Rpad * Kpad + (size_t)(r0 + row) * Kpad + k) =
+            *reinterpret_cast<const uint4 *>(&outp[plane][row][8 * seg]);
+    }
 }
 
 
