@@ -363,10 +363,13 @@ def run_gpu(args):
     converged = None
     if args.check:
         converged = {}
-        for label, refine in (("refine2", 2), ("refine0", 0)):
+        # FP64 integrals with two closing FP64 sweeps; FP64 integrals, split sweeps only; the
+        # three-plane split integrals with split sweeps only (no FP64 arithmetic at all)
+        for label, refine, tprec, rconv in (("refine2", 2, "fp64", 1e-9), ("refine0", 0, "fp64", 1e-8),
+                                            ("split3_integrals", 0, "split3", 1e-8)):
             t0 = time.perf_counter()
             s2 = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
-                           guess="mp2", diis=True, r_conv=1e-9, refine=refine, maxit=60, transform_precision="fp64")
+                           guess="mp2", diis=True, r_conv=rconv, refine=refine, maxit=60, transform_precision=tprec)
             t_setup = time.perf_counter() - t0
             s2.iterate(60)
             wall = time.perf_counter() - t0
@@ -384,7 +387,7 @@ def run_gpu(args):
     from juesgpu import MollerPlesset
     wt = system.wfn(ao_eri=gao)
     tr = {}
-    for prec in ("fp64", "split_bf16"):
+    for prec in ("fp64", "split_bf16", "split3"):
         ctx.set_profiling(True)
         ctx.profile_reset()
         e_mp2 = MollerPlesset.do_rmp2(wt, precision=prec, device=local)
@@ -402,6 +405,8 @@ def run_gpu(args):
                  "speedup": tr["fp64"]["ms"] / max(tr["split_bf16"]["ms"], 1e-9),
                  "mp2_fp64": tr["fp64"]["mp2"], "mp2_split": tr["split_bf16"]["mp2"],
                  "mp2_split_error_eh": tr["split_bf16"]["mp2"] - tr["fp64"]["mp2"],
+                 "split3_ms": tr["split3"]["ms"], "mp2_split3": tr["split3"]["mp2"],
+                 "mp2_split3_error_eh": tr["split3"]["mp2"] - tr["fp64"]["mp2"],
                  "mp2_fp64_vs_oracle_eh": (tr["fp64"]["mp2"] - mp2_golden) if mp2_golden else None}
 
     # ---------------- e2e through the C ABI with host buffers ----------------
@@ -416,11 +421,15 @@ def run_gpu(args):
                               refine=0, device=local, return_log=True)
         t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
         e2e_kernels = {k: ctx.profile(k)[0] for k in ("", "transform", "pack_split", "ccd_")}
+        e2e_host = {k: ctx.profile("host:" + k)[0] for k in ("h2d_ao_eri", "cc_create", "integral_blocks",
+                                                             "release_ao_eri")}
+        e2e_kernels[""] -= ctx.profile("host:")[0]   # kernel events only
         ctx.set_profiling(False)
         h2d = gao.nbytes + system.C.nbytes + eps.nbytes
         e2e = {"value": t_e2e / len(lg), "unit": "s/iter", "h2d_bytes_per_step": int(h2d / len(lg)),
                "d2h_bytes_per_step": 8, "sweeps": len(lg), "wall_s": t_e2e,
                "kernel_ms": {("all" if k == "" else k): v for k, v in e2e_kernels.items()},
+               "host_phase_ms": e2e_host,
                "includes": "H2D of AO ERIs, split transform "
                "of the 5 RCCD blocks, sweeps, energy read-back"}
 

@@ -48,7 +48,10 @@ extern "C" {
 
 /* arithmetic used for the bulk of the contractions */
 #define JUES_PREC_FP64 0       /* plain FP64 (the drop-in form)                          */
-#define JUES_PREC_SPLIT_BF16 1 /* tcgen05 BF16 hi+lo, three products, FP32 accumulation  */
+#define JUES_PREC_SPLIT_BF16 1 /* tcgen05, operands as hi + lo 10-bit integers carried in
+                                  FP16, three products, ~2^-20 relative                  */
+#define JUES_PREC_SPLIT3 2     /* tcgen05, hi + mid + lo (30 bits), six products,
+                                  ~2^-24 relative (FP32 chunk sums)                      */
 
 /* CC initial amplitudes */
 #define JUES_GUESS_ZERO 0  /* T2 = 0 (mRCCD.jl:239-256); first sweep gives MP2 amplitudes   */

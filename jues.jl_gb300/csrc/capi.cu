@@ -65,11 +65,11 @@ void check_dims(int n, int o, int v) {
 void check_opts(const jues_cc_opts &o) {
     if (o.maxit < 0) throw Error(JUES_EINVAL, "maxit must be >= 0");
     if (o.diis && (o.diis_size < 2 || o.diis_size > 16)) throw Error(JUES_EINVAL, "diis_size must be in 2..16");
-    if (o.precision != JUES_PREC_FP64 && o.precision != JUES_PREC_SPLIT_BF16)
+    if (!valid_precision(o.precision))
         throw Error(JUES_EINVAL, "unknown precision");
     if (o.guess < 0 || o.guess > 2) throw Error(JUES_EINVAL, "unknown guess");
     if (o.refine < 0) throw Error(JUES_EINVAL, "refine must be >= 0");
-    if (o.transform_precision < -1 || o.transform_precision > 1)
+    if (o.transform_precision != -1 && !valid_precision(o.transform_precision))
         throw Error(JUES_EINVAL, "unknown transform_precision");
 }
 
@@ -199,7 +199,7 @@ int jues_gemm(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double
         const int ar = transA ? K : M, br = transB ? N : K;
         if (lda < std::max(1, ar) || ldb < std::max(1, br) || ldc < std::max(1, M))
             throw Error(JUES_EINVAL, "leading dimension too small");
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         if (M == 0 || N == 0) return;
         cudaSetDevice(c.device);
@@ -251,7 +251,7 @@ int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1
         need(out, "out");
         if (n <= 0) throw Error(JUES_EINVAL, "nbf must be positive");
         if (d1 < 0 || d2 < 0 || d3 < 0 || d4 < 0) throw Error(JUES_EINVAL, "negative MO dimension");
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
         const size_t n4 = (size_t)n * n * n * n;
@@ -277,7 +277,7 @@ int jues_get_eri(jues_ctx *ctx, const double *gao, int n, const double *Cocc, in
         if (std::strlen(spec) != 4)
             throw Error(JUES_EINVAL, std::string("Invalid string given to get_eri: ") + spec);
         check_dims(n, o, v);
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         size_t no = 1;
         for (int q = 0; q < 4; ++q) {
@@ -307,7 +307,7 @@ int jues_rmp2(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o
         Ctx &c = CX(ctx);
         need(gao, "gao"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(e_out, "e_out");
         check_dims(n, o, v);
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
         DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
@@ -330,7 +330,7 @@ int jues_df_rmp2(jues_ctx *ctx, const double *pqP, int n, int naux, const double
         need(pqP, "pqP"); need(Cocc, "Cocc"); need(Cvir, "Cvir"); need(eps, "eps"); need(e_out, "e_out");
         check_dims(n, o, v);
         if (naux <= 0) throw Error(JUES_EINVAL, "naux must be positive");
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
         const long long ov = (long long)o * v;
@@ -364,7 +364,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
         need(gao, "gao"); need(C, "C"); need(eps, "eps"); need(e_out, "e_out");
         const int v = n - o;
         check_dims(n, o, v);
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
         DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
@@ -470,13 +470,19 @@ int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_devi
         DBuf<double> g;
         const double *gp = gao;
         if (!gao_is_device) {
+            Ctx::HostPhase ph(&c, "host:h2d_ao_eri");
             g = h2d(c, gao, (size_t)n * n * n * n);
             gp = g.p;
         }
         DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
         DBuf<double> de = h2d(c, eps, (size_t)n);
         std::unique_ptr<jues_cc> cc(new jues_cc());
-        cc->s = cc_create(&c, method, gp, n, co.p, o, cv.p, v, de.p, op);
+        {
+            Ctx::HostPhase ph(&c, "host:cc_create");
+            cc->s = cc_create(&c, method, gp, n, co.p, o, cv.p, v, de.p, op);
+        }
+        Ctx::HostPhase ph(&c, "host:release_ao_eri");
+        g.reset();
         *out = cc.release();
     });
 }
@@ -517,7 +523,7 @@ int jues_cc_iterate(jues_cc *cc, int nsweeps, int *done, int *converged) {
 int jues_cc_set_precision(jues_cc *cc, int precision) {
     return guarded([&] {
         need(cc, "cc");
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cc->s->precision = precision;
         cc->s->refine_left = -1;
@@ -641,7 +647,7 @@ int jues_pT(jues_ctx *ctx, const double *T1, const double *T2, const double *Vvv
         need(T1, "T1"); need(T2, "T2"); need(Vvvvo, "Vvvvo"); need(Vvooo, "Vvooo"); need(Vvovo, "Vvovo");
         need(fo, "fo"); need(fv, "fv"); need(e_out, "e_out");
         if (o <= 0 || v <= 0) throw Error(JUES_EINVAL, "need o > 0 and v > 0");
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
         const size_t O = (size_t)o, V = (size_t)v;
@@ -659,7 +665,7 @@ int jues_cc_pT(jues_cc *cc, int precision, double *e_out) {
         need(cc, "cc"); need(e_out, "e_out");
         CCState *s = cc->s;
         if (s->method != 1) throw Error(JUES_EINVAL, "(T) needs a CCSD session");
-        if (precision != JUES_PREC_FP64 && precision != JUES_PREC_SPLIT_BF16)
+        if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(s->ctx->device);
         const long long o = s->o, v = s->v, oo = o * o, ov = o * v;

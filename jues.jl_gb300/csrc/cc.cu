@@ -71,7 +71,7 @@ double ccd_sweep(CCState *s, int prec) {
     // their packs here (the integrals keep theirs).
     for (const double *p : {s->T.p, s->Tn.p, s->Tt.p, s->Wp.p, s->WJ.p, s->WK.p, s->W12.p, s->Fae.p, s->Fmi.p})
         pack_cache_drop(ctx, p);
-    s->cache_operands = (prec == JUES_PREC_SPLIT_BF16);
+    s->cache_operands = is_split(prec);
     // T~[i,j,a,b] = 2T[i,j,a,b] - T[j,i,a,b]
     t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
     const double *Tt = s->Tt.p;
@@ -225,8 +225,7 @@ static std::unique_ptr<CCState> cc_begin(Ctx *ctx, int method, int n, int o, int
     JUES_REQUIRE(n > 0 && o > 0 && v > 0 && o + v <= n, "need 0 < nocc, 0 < nvir, nocc + nvir <= nbf");
     JUES_REQUIRE(opts.maxit >= 0, "maxit must be >= 0");
     JUES_REQUIRE(opts.diis_size >= 2 && opts.diis_size <= 16 || !opts.diis, "diis_size must be in 2..16");
-    JUES_REQUIRE(opts.precision == JUES_PREC_FP64 || opts.precision == JUES_PREC_SPLIT_BF16,
-                 "unknown precision");
+    JUES_REQUIRE(valid_precision(opts.precision), "unknown precision");
     JUES_REQUIRE(opts.guess >= 0 && opts.guess <= 2, "unknown guess");
     std::unique_ptr<CCState> s(new CCState());
     s->ctx = ctx;
@@ -313,6 +312,7 @@ CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *C
     s->ovov = DBuf<double>(ctx, t2n);
     s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));
     s->vvvv = DBuf<double>(ctx, (size_t)(vv * vv));
+    Ctx::HostPhase ph_blocks(ctx, "host:integral_blocks");
     get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOVV", true, 0, s->oovv.p, true);
     get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVOV", true, 0, s->ovov.p, true);
     get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOOO", true, 0, s->oooo.p, true);
@@ -490,7 +490,7 @@ static bool at_noise_floor(const CCState *s) {
 void cc_iterate(CCState *s, int nsweeps, int *done, int *converged) {
     int k = 0;
     bool conv = false;
-    const bool split = s->precision == JUES_PREC_SPLIT_BF16;
+    const bool split = is_split(s->precision);
     while (k < nsweeps) {
         const int prec = (split && s->refine_left >= 0) ? JUES_PREC_FP64 : s->precision;
         cc_one(s, prec);

@@ -104,6 +104,15 @@ struct Ctx {
     };
     void flush_profile();
     void count_launch() { ++launches; }
+    // host wall time of a phase ("host:..." entries of the profile), recorded when profiling is
+    // on; the stream is synchronised at both ends so device work is attributed to its phase
+    struct HostPhase {
+        Ctx *c;
+        const char *name;
+        double t0 = 0.0;
+        HostPhase(Ctx *c, const char *name);
+        ~HostPhase();
+    };
     void check_flags();   // reads d_flags after a sync; throws on a set flag
 };
 
@@ -156,7 +165,11 @@ struct GettArgs {
 };
 
 void gett_f64(Ctx *ctx, const GettArgs &g, const char *name);
-void gett_tc(Ctx *ctx, const GettArgs &g, const char *name);   // split BF16 on tcgen05
+// split precision on tcgen05: np = 2 operand planes (hi, lo; JUES_PREC_SPLIT_BF16) or 3 (hi,
+// mid, lo; JUES_PREC_SPLIT3)
+void gett_tc(Ctx *ctx, const GettArgs &g, const char *name, int np = 2);
+inline bool is_split(int precision) { return precision == JUES_PREC_SPLIT_BF16 || precision == JUES_PREC_SPLIT3; }
+inline bool valid_precision(int precision) { return precision == JUES_PREC_FP64 || is_split(precision); }
 // split-K epilogue: C[mC(m) + nC(n)] = alpha sum_s ws[s sstride + n ld + m] + beta Cin[...],
 // the partials summed in FP64 in split order (deterministic)
 void splitk_reduce(Ctx *ctx, const float *ws, int ks, long long sstride, long long ld, long long M, long long N,

@@ -1,6 +1,7 @@
 // Context: stream, memory accounting, per-kernel event timing, error flags.
 #include <nvtx3/nvToolsExt.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 
@@ -115,6 +116,24 @@ Ctx::Scope::~Scope() {
     cudaEventRecord(ev.second, c->stream);
     r->pending.push_back(ev);
     r->launches += 1;
+}
+
+static double wall_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+Ctx::HostPhase::HostPhase(Ctx *c_, const char *n) : c(c_), name(n) {
+    if (!c->profiling) return;
+    cudaStreamSynchronize(c->stream);
+    t0 = wall_ms();
+}
+
+Ctx::HostPhase::~HostPhase() {
+    if (!c->profiling) return;
+    cudaStreamSynchronize(c->stream);
+    ProfRec &r = c->prof[name];
+    r.total_ms += wall_ms() - t0;
+    r.launches += 1;
 }
 
 void Ctx::flush_profile() {

@@ -199,20 +199,26 @@ struct TcArgs {
 constexpr int TC_THREADS = 320;
 constexpr int TC_DRAIN = 256;   // drain threads (warps 2-9)
 
-template <int BN, int STAGES, int KC>
+__host__ __device__ constexpr uint32_t pow2_at_least(uint32_t x) {
+    return x <= 32 ? 32u : (x <= 64 ? 64u : (x <= 128 ? 128u : (x <= 256 ? 256u : 512u)));
+}
+// instruction descriptor: FP32 accumulate, FP16 A and B (format 0), both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t tc_idesc(int n) {
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+}
+
+// NP = operand planes: 2 (hi, lo) or 3 (hi, mid, lo)
+template <int BN, int STAGES, int KC, int NP>
 struct TcCfg {
-    static constexpr int A_BYTES = TBM * TBK * 2;
+    static constexpr int A_BYTES = TBM * TBK * 2;   // one plane
     static constexpr int B_BYTES = BN * TBK * 2;
-    static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+    static constexpr int STAGE_BYTES = NP * A_BYTES + NP * B_BYTES;
     static constexpr int BAR_BYTES = 256;
     static constexpr int SMEM = STAGES * STAGE_BYTES + BAR_BYTES + BN * 8 + 2 * BN * 4 + 1024;
-    static constexpr uint32_t TMEM_COLS = 4 * BN;   // 2 buffers x (main, correction)
-    // instruction descriptor: FP32 accumulate, FP16 A and B (format 0), both K-major,
-    // M = 128, N = BN
-    static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
-    // the same with N = 2 BN: A_hi against the stacked [B_hi; B_lo] rows, writing the main and
-    // correction accumulators (adjacent TMEM columns) in one instruction
-    static constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(2 * BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+    static constexpr int BUF_COLS = NP * BN;   // one chunk buffer: NP accumulators of BN columns
+    static constexpr uint32_t TMEM_COLS = pow2_at_least(2 * BUF_COLS);   // two chunk buffers
+    static_assert(2 * BUF_COLS <= 512, "TMEM holds 512 columns");
+    static_assert(NP * BN <= 256, "one MMA instruction spans at most N = 256");
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -250,10 +256,10 @@ __device__ __forceinline__ bool drain_bar_any(bool pred) {
     return r != 0;
 }
 
-template <int BN, int STAGES, int KC>
+template <int BN, int STAGES, int KC, int NP>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gett_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs g) {
-    using Cfg = TcCfg<BN, STAGES, KC>;
+    using Cfg = TcCfg<BN, STAGES, KC, NP>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *stages = smem;
@@ -314,10 +320,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     uint8_t *st = stages + s * Cfg::STAGE_BYTES;
                     const int kx = (I.kb0 + kb) * TBK;
                     mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
-                    tma_load_3d(st, &mapA, &full[s], kx, I.m0, 0);
-                    tma_load_3d(st + Cfg::A_BYTES, &mapA, &full[s], kx, I.m0, 1);
-                    tma_load_3d(st + 2 * Cfg::A_BYTES, &mapB, &full[s], kx, I.n0, 0);
-                    tma_load_3d(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES, &mapB, &full[s], kx, I.n0, 1);
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) tma_load_3d(st + p * Cfg::A_BYTES, &mapA, &full[s], kx, I.m0, p);
+#pragma unroll
+                    for (int p = 0; p < NP; ++p)
+                        tma_load_3d(st + NP * Cfg::A_BYTES + p * Cfg::B_BYTES, &mapB, &full[s], kx, I.n0, p);
                 }
             }
             // the last load into each slot has landed (immediate unless an abort cut the MMA
@@ -355,20 +362,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                     tc_fence_after();
                     uint8_t *st = stages + s * Cfg::STAGE_BYTES;
-                    const uint64_t ah = sw128_desc(st), al = sw128_desc(st + Cfg::A_BYTES);
-                    const uint64_t bh = sw128_desc(st + 2 * Cfg::A_BYTES);
-                    const uint32_t dmain = tmem + (uint32_t)(buf * 2 * BN);
-                    const uint32_t dcorr = dmain + (uint32_t)BN;
-                    // B_lo's rows follow B_hi's in shared memory (B_BYTES = BN 128-byte rows, whole
-                    // 8-row swizzle groups) and the correction columns follow the main ones in
-                    // TMEM, so hi*hi and hi*lo are one N = 2 BN instruction; lo*hi adds to the
-                    // correction.
+                    const uint64_t b0 = sw128_desc(st + NP * Cfg::A_BYTES);
+                    const uint32_t dbuf = tmem + (uint32_t)(buf * Cfg::BUF_COLS);
+                    // The B planes' rows are stacked in shared memory (B_BYTES = BN 128-byte rows,
+                    // whole 8-row swizzle groups) and the NP accumulators of a buffer are adjacent
+                    // TMEM column ranges, so plane p of A against B planes 0..NP-1-p is one
+                    // instruction with N = (NP - p) BN writing accumulators p..NP-1: accumulator
+                    // j collects every product A_p B_q with p + q = j (j < NP), and the products
+                    // with p + q >= NP (lo.lo, 2^-20 or 2^-30 smaller) are left out.
 #pragma unroll
                     for (int kk = 0; kk < TBK / 16; ++kk) {
                         const uint64_t off = (uint64_t)((kk * 16 * 2) >> 4);   // 32 bytes per K=16 step
                         const uint32_t acc = (first && kk == 0) ? 0u : 1u;
-                        umma_bf16(dmain, ah + off, bh + off, Cfg::IDESC2, acc);
-                        umma_bf16(dcorr, al + off, bh + off, Cfg::IDESC, 1u);
+#pragma unroll
+                        for (int p = 0; p < NP; ++p)
+                            umma_bf16(dbuf + (uint32_t)(p * BN), sw128_desc(st + p * Cfg::A_BYTES) + off, b0 + off,
+                                      tc_idesc((NP - p) * BN), p == 0 ? acc : 1u);
                     }
                     umma_commit(&empty[s]);   // stage s free once these complete
                     if ((kb % KC) == KC - 1 || kb == I.nk - 1) {
@@ -444,20 +453,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
                 const float2 *cs = reinterpret_cast<const float2 *>(colsc + buf * BN + half * HB);
                 const uint64_t rs2 = pk2f(rs, rs), k2 = pk2f(0.0009765625f, 0.0009765625f);
-                // 32 columns per round: two TMEM loads in flight, one wait; then per column pair
-                // part = corr 2^-10 + main, acc += part (2^e_row 2^e_col), all round-to-nearest
+                // 32 columns per round: the NP accumulator loads in flight, one wait; then per
+                // column pair part = main + 2^-10 (corr + 2^-10 corr2), acc += part (2^e_row 2^e_col),
+                // all round-to-nearest
 #pragma unroll
                 for (int c0 = 0; c0 < HB; c0 += 32) {
-                    uint32_t rm[32], rc[32];
+                    uint32_t r0[32], r1[32], r2[NP > 2 ? 32 : 1];
                     const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) +
-                                          (uint32_t)(buf * 2 * BN + half * HB + c0);
-                    tmem_ld32(base, rm);
-                    tmem_ld32(base + (uint32_t)BN, rc);
+                                          (uint32_t)(buf * Cfg::BUF_COLS + half * HB + c0);
+                    tmem_ld32(base, r0);
+                    tmem_ld32(base + (uint32_t)BN, r1);
+                    if constexpr (NP > 2) tmem_ld32(base + (uint32_t)(2 * BN), *reinterpret_cast<uint32_t(*)[32]>(r2));
                     tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 32; j += 2) {
                         const float2 c2 = cs[(c0 + j) >> 1];
-                        const uint64_t part = ffma2(pk2(rc[j], rc[j + 1]), k2, pk2(rm[j], rm[j + 1]));
+                        uint64_t corr = pk2(r1[j], r1[j + 1]);
+                        if constexpr (NP > 2) corr = ffma2(pk2(r2[j], r2[j + 1]), k2, corr);
+                        const uint64_t part = ffma2(corr, k2, pk2(r0[j], r0[j + 1]));
                         const uint64_t sc = fmul2(rs2, pk2f(c2.x, c2.y));
                         acc2[(c0 + j) >> 1] = ffma2(part, sc, acc2[(c0 + j) >> 1]);
                     }
@@ -512,7 +525,9 @@ constexpr int PR = 16, PK = 128, KCH = 128;   // pack tile = one scaling chunk =
 // with integer arithmetic only (GB300 runs FP64 arithmetic at a small fraction of its integer
 // rate): for x = +-m 2^(E-1075) (m the 53-bit significand) and chunk scale e,
 //     q = rint(x 2^(19-e)) = round(m >> (1056 + e - E)),  hi = (q + 512) >> 10,  lo = q - 1024 hi,
-// so x ~ 2^(e-19) q = 2^(e-9) (hi + 2^-10 lo) with |hi| <= 512, |lo| <= 512.  Every element
+// so x ~ 2^(e-19) q = 2^(e-9) (hi + 2^-10 lo) with |hi| <= 512, |lo| <= 512.  The three-plane
+// form keeps 29 bits: q = rint(x 2^(29-e)) = 2^20 hi + 2^10 mid + lo, x ~ 2^(e-9) (hi + 2^-10 mid
+// + 2^-20 lo), |x - that| <= 2^(e-30).  Every element
 // of the padded tile and every scale is written, so nothing has to be cleared beforehand.
 __device__ __forceinline__ int exp_bound(double x) {
     // smallest e with |x| < 2^e (INT_MIN for zero and subnormals, which are flushed)
@@ -520,22 +535,25 @@ __device__ __forceinline__ int exp_bound(double x) {
     const int E = (int)((b >> 52) & 0x7FF);
     return E == 0 ? INT_MIN : E - 1022;
 }
-__device__ __forceinline__ long long fixed_q(double x, int e) {
+// q = rint(x 2^(bits - e)), ties away from zero, for |x| < 2^e: bits = 19 (two planes) or 29
+// (three planes)
+__device__ __forceinline__ long long fixed_q(double x, int e, int bits) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const int E = (int)((b >> 52) & 0x7FF);
     if (E == 0 || e == INT_MIN) return 0;
     const unsigned long long m = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    const int r = 1056 + e - E;   // >= 34 because |x| < 2^e
+    const int r = 1075 - bits + e - E;   // >= 54 - bits because |x| < 2^e
     const unsigned long long q = r > 60 ? 0ull : ((m + (1ull << (r - 1))) >> r);
     return (b >> 63) ? -(long long)q : (long long)q;
 }
 
+template <int NP>
 __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
                                                          long long Kpad, int kfast, int *__restrict__ rexp,
                                                          __half *__restrict__ dst) {
     __shared__ double tile[PR][PK + 1];
-    __shared__ __align__(16) __half outp[2][PR][PK];
+    __shared__ __align__(16) __half outp[NP][PR][PK];
     __shared__ long long roff[PR], koff[PK];
     const long long kblocks = (Kpad + PK - 1) / PK;
     const long long r0 = (blockIdx.x / kblocks) * PR;
@@ -568,15 +586,25 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
     if (t == 0) rexp[(k0 / KCH) * Rpad + r0 + rr] = ex;
 #pragma unroll
     for (int j = 0; j < PK / 16; ++j) {
-        const long long q = fixed_q(tile[rr][t + 16 * j], ex);
-        const long long h = (q + 512) >> 10;
-        outp[0][rr][t + 16 * j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
-        outp[1][rr][t + 16 * j] = __int2half_rn((int)(q - (h << 10)));
+        const long long q = fixed_q(tile[rr][t + 16 * j], ex, 10 * NP - 1);
+        if constexpr (NP == 2) {
+            const long long h = (q + 512) >> 10;
+            outp[0][rr][t + 16 * j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
+            outp[1][rr][t + 16 * j] = __int2half_rn((int)(q - (h << 10)));
+        } else {
+            // q = 2^20 hi + 2^10 mid + lo, each in [-512, 512]
+            const long long h = (q + (1LL << 19)) >> 20;
+            const long long rem = q - (h << 20);
+            const long long m = (rem + 512) >> 10;
+            outp[0][rr][t + 16 * j] = __int2half_rn((int)h);
+            outp[1][rr][t + 16 * j] = __int2half_rn((int)m);
+            outp[2][rr][t + 16 * j] = __int2half_rn((int)(rem - (m << 10)));
+        }
     }
     __syncthreads();
-    // 2 planes x PR rows x 16 segments of 8 halves
+    // NP planes x PR rows x 16 segments of 8 halves
 #pragma unroll
-    for (int i = 0; i < (2 * PR * (PK / 8)) / 256; ++i) {
+    for (int i = 0; i < (NP * PR * (PK / 8)) / 256; ++i) {
         const int idx = tid + 256 * i;
         const int seg = idx & 15, row = (idx >> 4) % PR, plane = idx / (16 * PR);
         const long long k = k0 + 8 * seg;
@@ -600,10 +628,10 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     return fn;
 }
 
-CUtensorMap make_map(const __half *base, long long rows_pad, long long kpad, int box_rows) {
+CUtensorMap make_map(const __half *base, long long rows_pad, long long kpad, int box_rows, int np) {
     CUtensorMap m;
     std::memset(&m, 0, sizeof(m));
-    cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, 2};
+    cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)np};
     cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
     cuuint32_t box[3] = {(cuuint32_t)TBK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
@@ -630,6 +658,7 @@ struct PackEntry {
     const double *src;
     Mode r, k;
     long long R, K, Rpad, Kpad;
+    int np;
     DBuf<__half> buf;
     DBuf<int> exps;
 };
@@ -681,22 +710,22 @@ void pack_cache_drop(Ctx *ctx, const void *ptr) {
 }
 
 static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm, const Mode &km, long long R,
-                           long long K, long long Rpad, long long Kpad, bool cache) {
+                           long long K, long long Rpad, long long Kpad, bool cache, int np) {
     if (!ctx->pack) ctx->pack = new PackCache();
     PackCache &pc = *ctx->pack;
     if (cache) {
         for (auto &e : pc.cached)
-            if (e->src == src && e->R == R && e->K == K && e->Rpad == Rpad && e->Kpad == Kpad &&
+            if (e->src == src && e->R == R && e->K == K && e->Rpad == Rpad && e->Kpad == Kpad && e->np == np &&
                 same_mode(e->r, rm) && same_mode(e->k, km))
                 return Packed{e->buf.p, e->exps.p};
     }
-    const size_t need = (size_t)2 * Rpad * Kpad;
+    const size_t need = (size_t)np * Rpad * Kpad;
     const long long nchunk = (Kpad + KCH - 1) / KCH;
     __half *dst;
     int *ex;
     std::unique_ptr<PackEntry> ent;
     if (cache) {
-        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, take_buffer(ctx, pc.free_planes, need),
+        ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, np, take_buffer(ctx, pc.free_planes, need),
                                 take_buffer(ctx, pc.free_exps, (size_t)nchunk * Rpad)});
         dst = ent->buf.p;
         ex = ent->exps.p;
@@ -717,8 +746,12 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     {
         Ctx::Scope s(ctx, "pack_split");
-        pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
-                                                                     dst);
+        if (np == 3)
+            pack_split_kernel<3><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
+                                                                            dst);
+        else
+            pack_split_kernel<2><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
+                                                                            dst);
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     if (cache) pc.cached.push_back(std::move(ent));
@@ -738,13 +771,13 @@ static int sm_count(int device) {
     return cached[device];
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int NP>
 static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
                       const char *name) {
-    using Cfg = TcCfg<BN, STAGES, TC_KC>;
+    using Cfg = TcCfg<BN, STAGES, TC_KC, NP>;
     static bool attr_set = false;
     if (!attr_set) {
-        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES, TC_KC>,
+        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES, TC_KC, NP>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
         attr_set = true;
     }
@@ -760,7 +793,7 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
     // persistent: one CTA per SM (the stage ring takes most of shared memory)
     const long long grid = std::min<long long>(items, sm_count(ctx->device));
     Ctx::Scope s(ctx, name);
-    gett_tc_kernel<BN, STAGES, TC_KC><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
+    gett_tc_kernel<BN, STAGES, TC_KC, NP><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -781,15 +814,18 @@ static int choose_ksplit(long long tiles, int kblocks) {
     return cost(best) <= 0.9 * cost(1) ? best : 1;
 }
 
-void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
+void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name, int np) {
     if (a0.M <= 0 || a0.N <= 0) return;
+    JUES_REQUIRE(np == 2 || np == 3, "operand planes must be 2 or 3");
     GettArgs a = a0;
+    // three planes fit TMEM and shared memory only with BN = 64
+    const std::vector<int> widths = np == 3 ? std::vector<int>{64} : std::vector<int>{128, 64};
     // Orientation: the output's unit-stride mode on the row (TMEM lane) side lets each warp
     // store 32 consecutive doubles per column; weigh that against the padding of both tile
     // grids (rows pad to 128, columns to the chosen BN).
-    auto pad_cost = [](long long M, long long N, bool unit_rows) {
+    auto pad_cost = [&](long long M, long long N, bool unit_rows) {
         long long best = -1;
-        for (int cand : {128, 64}) {
+        for (int cand : widths) {
             long long p = roundup(N, cand);
             if (best < 0 || p < best) best = p;
         }
@@ -811,10 +847,10 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
         return;
     }
     // tile width: smallest padded N, preferring wider tiles on ties
-    int BN = 128;
+    int BN = widths[0];
     {
         long long best = -1;
-        for (int cand : {128, 64}) {
+        for (int cand : widths) {
             long long p = roundup(a.N, cand);
             if (best < 0 || p < best) { best = p; BN = cand; }
         }
@@ -822,10 +858,10 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
     const long long Mpad = roundup(a.M, TBM), Npad = roundup(a.N, BN), Kpad = roundup(a.K, TBK);
     JUES_REQUIRE(Mpad < (1LL << 31) && Npad < (1LL << 31) && Kpad / TBK < (1LL << 30),
                  "GEMM extent exceeds the TMA coordinate range");
-    const Packed pa = pack_operand(ctx, 0, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, a.a_const);
-    const Packed pb = pack_operand(ctx, 1, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, a.b_const);
-    const CUtensorMap ma = make_map(pa.planes, Mpad, Kpad, TBM);
-    const CUtensorMap mb = make_map(pb.planes, Npad, Kpad, BN);
+    const Packed pa = pack_operand(ctx, 0, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, a.a_const, np);
+    const Packed pb = pack_operand(ctx, 1, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, a.b_const, np);
+    const CUtensorMap ma = make_map(pa.planes, Mpad, Kpad, TBM, np);
+    const CUtensorMap mb = make_map(pb.planes, Npad, Kpad, BN, np);
     TcArgs t;
     t.M = a.M;
     t.N = a.N;
@@ -851,10 +887,12 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name) {
         t.ksplit = (t.kblocks + t.kper - 1) / t.kper;
         t.partial = static_cast<float *>(ctx->splitk_scratch((size_t)t.ksplit * Mpad * Npad * sizeof(float)));
     }
-    if (BN == 128)
-        launch_tc<128, 3>(ctx, ma, mb, t, tiles, name);
+    if (np == 3)
+        launch_tc<64, 3, 3>(ctx, ma, mb, t, tiles, name);
+    else if (BN == 128)
+        launch_tc<128, 3, 2>(ctx, ma, mb, t, tiles, name);
     else
-        launch_tc<64, 4>(ctx, ma, mb, t, tiles, name);
+        launch_tc<64, 4, 2>(ctx, ma, mb, t, tiles, name);
     if (t.ksplit > 1)
         splitk_reduce(ctx, t.partial, t.ksplit, Mpad * Npad, Mpad, a.M, a.N, a.alpha, a.beta, a.C, t.Cin, a.mC, a.nC,
                       name);
@@ -901,7 +939,7 @@ void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     Ctx::Scope s(ctx, "pack_split_noalloc");
-    pack_split_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex, dst);
+    pack_split_kernel<2><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex, dst);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 }  // namespace
@@ -933,8 +971,8 @@ void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
     // every (chunk,row) scale
     pack_into(ctx, a.A, a.mA, a.kA, a.M, a.K, Mpad, Kpad, pa, ea);
     pack_into(ctx, a.B, a.nB, a.kB, a.N, a.K, Npad, Kpad, pb, eb);
-    const CUtensorMap ma = make_map(pa, Mpad, Kpad, TBM);
-    const CUtensorMap mb = make_map(pb, Npad, Kpad, BN);
+    const CUtensorMap ma = make_map(pa, Mpad, Kpad, TBM, 2);
+    const CUtensorMap mb = make_map(pb, Npad, Kpad, BN, 2);
     TcArgs t;
     t.M = a.M;
     t.N = a.N;
@@ -953,7 +991,7 @@ void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
     t.expB_ld = Npad;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
-    launch_tc<BN, 3>(ctx, ma, mb, t, tiles, "gemm_noalloc");
+    launch_tc<BN, 3, 2>(ctx, ma, mb, t, tiles, "gemm_noalloc");
 }
 
 }  // namespace jues

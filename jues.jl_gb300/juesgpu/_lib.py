@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libjuesgpu.so")
 
 OK, EINVAL, ENOMEM, ECUDA, ENOTCONV, ENONFINITE, ETIMEOUT, ENODEV = range(8)
-PREC = {"fp64": 0, "split_bf16": 1}
+PREC = {"fp64": 0, "split_bf16": 1, "split3": 2}
 GUESS = {"zero": 0, "mp2": 1, "ovov": 2}
 
 

@@ -16,7 +16,7 @@ module JuESGPU
 using JuES.Wavefunction
 
 const LIB = get(ENV, "JUESGPU_LIB", joinpath(@__DIR__, "..", "lib", "libjuesgpu.so"))
-const PREC = Dict(:fp64 => Cint(0), :split_bf16 => Cint(1))
+const PREC = Dict(:fp64 => Cint(0), :split_bf16 => Cint(1), :split3 => Cint(2))
 const GUESS = Dict(:zero => Cint(0), :mp2 => Cint(1), :ovov => Cint(2))
 const ENOTCONV = 4
 

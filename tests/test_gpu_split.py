@@ -168,3 +168,82 @@ def test_gemm_split_k(lib, precision, M, N, K):
         assert rel < 1e-5
     again = lib.gemm(A, B, C0, alpha=-0.5, beta=0.25, transA=True, precision=precision)
     assert np.array_equal(got, again)   # the split order is fixed: bitwise reproducible
+
+
+# ------------------------------------------------------------------------------ three planes
+def split3_rows(X):
+    """The three-plane operand representation: q = rint(x 2^(29-e)) (ties away from zero) =
+    2^20 hi + 2^10 mid + lo, each in [-512, 512], per row and 128-long K chunk."""
+    X = np.asarray(X, dtype=np.float64)
+    R, K = X.shape
+    e = np.zeros_like(X, dtype=np.int64)
+    for c0 in range(0, K, KCH):
+        mx = np.abs(X[:, c0:c0 + KCH]).max(axis=1)
+        e[:, c0:c0 + KCH] = np.where(mx > 0, np.frexp(mx)[1], 0)[:, None]
+    t = np.ldexp(np.abs(X), 29 - e)
+    q = np.sign(X) * np.floor(t + 0.5)
+    h = np.floor((q + 2.0**19) / 2.0**20)
+    rem = q - 2.0**20 * h
+    m = np.floor((rem + 512.0) / 1024.0)
+    lo = rem - 1024.0 * m
+    return h, m, lo, e
+
+
+def emulate3(A, B):
+    """What the three-plane kernel computes, with its FP32 roundings: per chunk the exact
+    integer accumulators main = hh, c1 = hm + mh, c2 = hl + mm + lh, then in FP32
+    part = (c2 2^-10 + c1) 2^-10 + main and acc += part 2^(e_A + e_B - 18)."""
+    ha, ma, la, ea = split3_rows(A)
+    hb, mb, lb, eb = split3_rows(B.T)
+    K = A.shape[1]
+    f32 = np.float32
+    acc = np.zeros((A.shape[0], B.shape[1]), dtype=f32)
+    for c0 in range(0, K, KCH):
+        s = slice(c0, c0 + KCH)
+        main = ha[:, s] @ hb[:, s].T
+        c1 = ha[:, s] @ mb[:, s].T + ma[:, s] @ hb[:, s].T
+        c2 = ha[:, s] @ lb[:, s].T + ma[:, s] @ mb[:, s].T + la[:, s] @ hb[:, s].T
+        corr = f32(c2 / 1024.0 + c1)
+        part = f32(corr.astype(np.float64) / 1024.0 + main)
+        sc = np.ldexp(1.0, ea[:, c0][:, None] + eb[:, c0][None, :] - 18)
+        acc = f32(part.astype(np.float64) * sc + acc.astype(np.float64))
+    return acc.astype(np.float64)
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb", SHAPES[:6])
+def test_gemm_split3(lib, M, N, K, ta, tb):
+    rng = np.random.default_rng(11 * M + N + K)
+    A = rng.normal(size=(K, M) if ta else (M, K))
+    B = rng.normal(size=(N, K) if tb else (K, N))
+    got = lib.gemm(A, B, transA=ta, transB=tb, precision="split3")
+    Aop, Bop = (A.T if ta else A), (B.T if tb else B)
+    exact = Aop @ Bop
+    emu = emulate3(Aop, Bop)
+    # the FP32 roundings dominate: ~2^-24 per chunk sum, growing like sqrt(chunks)
+    assert np.abs(got - emu).max() < 1e-6 * np.abs(exact).max()
+    rel = np.linalg.norm(got - exact) / np.linalg.norm(exact)
+    assert rel < (3e-7 if K <= 640 else 1e-6), rel
+    # and far better than the two-plane form
+    two = lib.gemm(A, B, transA=ta, transB=tb, precision="split_bf16")
+    assert rel < 0.2 * np.linalg.norm(two - exact) / np.linalg.norm(exact)
+
+
+@pytest.mark.parametrize("name,bar", [("S25", 1e-10), ("S100", 3e-8)])
+def test_rmp2_split3(lib, name, bar):
+    from juesgpu import MollerPlesset
+    with open(os.path.join(GOLDEN, "synthetic_golden.json")) as f:
+        ref = json.load(f)[name]["mp2"]
+    e = MollerPlesset.do_rmp2(make_named(name).wfn(), precision="split3")
+    assert abs(e - ref) < bar, (e, ref)
+
+
+def test_rccd_split3_transform_within_one_microhartree(lib):
+    # the microhartree setting without FP64 arithmetic: split3 integrals, split sweeps
+    from juesgpu.CoupledCluster import mRCCD
+    with open(os.path.join(GOLDEN, "synthetic_golden.json")) as f:
+        ref = json.load(f)["S100"]["ccd_mp2guess_diis"]["energy"]
+    w = make_named("S100").wfn()
+    e, log = mRCCD.do_rccd(w, maxit=40, r_conv=1e-8, guess="mp2", precision="split_bf16", refine=0,
+                           transform_precision="split3", return_log=True)
+    assert abs(e - ref) < 1e-6, (e, ref)
+    assert all(r[4] == 1 for r in log)
