@@ -429,7 +429,7 @@ def run_gpu(args):
         e2e = {"value": t_e2e / len(lg), "unit": "s/iter", "h2d_bytes_per_step": int(h2d / len(lg)),
                "d2h_bytes_per_step": 8, "sweeps": len(lg), "wall_s": t_e2e,
                "kernel_ms": {("all" if k == "" else k): v for k, v in e2e_kernels.items()},
-               "host_phase_ms": e2e_host,
+               "host_phase_ms": e2e_host, "ao_direct": ctx.set_ao_direct(True),
                "includes": "H2D of AO ERIs, split transform "
                "of the 5 RCCD blocks, sweeps, energy read-back"}
 

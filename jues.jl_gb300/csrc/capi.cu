@@ -1,5 +1,6 @@
 // extern "C" entry points of libjuesgpu.so (declared in include/jues_gpu.h).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -45,10 +46,22 @@ void need(const void *p, const char *what) {
 }
 
 // copy a host array to a new context buffer
+// The AO integrals of a transform in precision prec.  Where the device reads pageable host
+// memory through the host page tables, the split forms pack them straight from the caller's
+// array (one pass over the NVLink-C2C link, no n^4 device copy); otherwise they are copied.
+static const double *ao_operand(Ctx &c, const double *gao, size_t n4, int prec, DBuf<double> &hold);
+
 DBuf<double> h2d(Ctx &ctx, const double *h, size_t n) {
     DBuf<double> d(&ctx, n);
     if (n) JUES_CHECK_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
     return d;
+}
+
+static const double *ao_operand(Ctx &c, const double *gao, size_t n4, int prec, DBuf<double> &hold) {
+    if (is_split(prec) && c.ao_direct) return gao;
+    Ctx::HostPhase ph(&c, "host:h2d_ao_eri");
+    hold = h2d(c, gao, n4);
+    return hold.p;
 }
 
 void d2h(Ctx &ctx, double *h, const double *d, size_t n) {
@@ -138,7 +151,24 @@ int jues_ctx_create(int device, jues_ctx **out) {
         JUES_CHECK_CUDA(cudaMalloc(&x.d_flags, 4 * sizeof(unsigned)));
         JUES_CHECK_CUDA(cudaMemset(x.d_flags, 0, 4 * sizeof(unsigned)));
         JUES_CHECK_CUDA(cudaMalloc(&x.d_red, 65536 * sizeof(double)));
+        int pageable = 0, host_tables = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) pageable = 0;
+        if (cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) !=
+            cudaSuccess)
+            host_tables = 0;
+        cudaGetLastError();
+        const char *env = std::getenv("JUES_AO_DIRECT");
+        x.ao_direct_supported = pageable == 1 && host_tables == 1;
+        x.ao_direct = x.ao_direct_supported && !(env && env[0] == '0');
         *out = c.release();
+    });
+}
+
+int jues_ctx_set_ao_direct(jues_ctx *ctx, int enable, int *active) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        c.ao_direct = enable && c.ao_direct_supported;
+        if (active) *active = c.ao_direct ? 1 : 0;
     });
 }
 
@@ -255,7 +285,8 @@ int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
         const size_t n4 = (size_t)n * n * n * n;
-        DBuf<double> g = h2d(c, gao, n4);
+        DBuf<double> g;
+        const double *gp = ao_operand(c, gao, n4, precision, g);
         DBuf<double> c1 = h2d(c, C1, (size_t)n * d1), c2 = h2d(c, C2, (size_t)n * d2),
                      c3 = h2d(c, C3, (size_t)n * d3), c4 = h2d(c, C4, (size_t)n * d4);
         const size_t no = (size_t)d1 * d2 * d3 * d4;
@@ -263,7 +294,7 @@ int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1
         const double *Cs[4] = {c1.p, c2.p, c3.p, c4.p};
         int d[4] = {d1, d2, d3, d4};
         long long ostr[4] = {1, d1, (long long)d1 * d2, (long long)d1 * d2 * d3};
-        transform4(&c, precision, g.p, n, Cs, d, dout.p, ostr, false);
+        transform4(&c, precision, gp, n, Cs, d, dout.p, ostr, false);
         d2h(c, out, dout.p, no);
         c.check_flags();
     });
@@ -292,10 +323,11 @@ int jues_get_eri(jues_ctx *ctx, const double *gao, int n, const double *Cocc, in
             }
         }
         cudaSetDevice(c.device);
-        DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
+        DBuf<double> g;
+        const double *gp = ao_operand(c, gao, (size_t)n * n * n * n, precision, g);
         DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
         DBuf<double> dout(&c, no);
-        get_eri_block(&c, precision, g.p, n, co.p, o, cv.p, v, spec, phys != 0, fcn, dout.p, false);
+        get_eri_block(&c, precision, gp, n, co.p, o, cv.p, v, spec, phys != 0, fcn, dout.p, false);
         d2h(c, out, dout.p, no);
         c.check_flags();
     });
@@ -310,12 +342,13 @@ int jues_rmp2(jues_ctx *ctx, const double *gao, int n, const double *Cocc, int o
         if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
-        DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
+        DBuf<double> g;
+        const double *gp = ao_operand(c, gao, (size_t)n * n * n * n, precision, g);
         DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
         DBuf<double> de = h2d(c, eps, (size_t)n);
         const size_t nk = (size_t)o * o * v * v;
         DBuf<double> K(&c, nk);
-        get_eri_block(&c, precision, g.p, n, co.p, o, cv.p, v, "OOVV", true, 0, K.p, false);
+        get_eri_block(&c, precision, gp, n, co.p, o, cv.p, v, "OOVV", true, 0, K.p, false);
         g.reset();
         *e_out = mp2_energy(&c, K.p, de.p, o, v);
         if (k_out) d2h(c, k_out, K.p, nk);
@@ -367,7 +400,8 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
         if (!valid_precision(precision))
             throw Error(JUES_EINVAL, "unknown precision");
         cudaSetDevice(c.device);
-        DBuf<double> g = h2d(c, gao, (size_t)n * n * n * n);
+        DBuf<double> gbuf;
+        const double *gp = ao_operand(c, gao, (size_t)n * n * n * n, precision, gbuf);
         DBuf<double> dC = h2d(c, C, (size_t)n * n);
         DBuf<double> de = h2d(c, eps, (size_t)n);
         const double *Co = dC.p, *Cv = dC.p + (size_t)n * o;
@@ -379,7 +413,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
             const double *Cs[4] = {Co, Cv, Co, Cv};
             int d[4] = {o, v, o, v};
             long long ostr[4] = {1, o, ov, ov * o};
-            transform4(&c, precision, g.p, n, Cs, d, K.p, ostr, true);
+            transform4(&c, precision, gp, n, Cs, d, K.p, ostr, true);
         }
         *e_out = mp2_gamma(&c, K.p, de.p, o, v, e_bar, G.p);
         K.reset();
@@ -398,7 +432,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
                 int d[4] = {n, v, o, v};
                 long long ostr[4] = {1, n, (long long)n * v, (long long)n * v * o};
                 DBuf<double> H(&c, (size_t)n * v * o * v);
-                transform4(&c, precision, g.p, n, Cs, d, H.p, ostr, true);
+                transform4(&c, precision, gp, n, Cs, d, H.p, ostr, true);
                 GettArgs a;
                 a.M = n; a.N = o; a.K = ov * v;
                 a.alpha = 2.0; a.beta = 0.0;
@@ -413,7 +447,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
                 int d[4] = {o, n, o, v};
                 long long ostr[4] = {1, o, (long long)o * n, (long long)o * n * o};
                 DBuf<double> H(&c, (size_t)o * n * o * v);
-                transform4(&c, precision, g.p, n, Cs, d, H.p, ostr, true);
+                transform4(&c, precision, gp, n, Cs, d, H.p, ostr, true);
                 GettArgs a;
                 a.M = n; a.N = v; a.K = (long long)o * o * v;
                 a.alpha = 2.0; a.beta = 0.0;
@@ -424,7 +458,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
             }
             d2h(c, C_bar, cb.p, cb.n);
         }
-        pack_cache_drop(&c, g.p);
+        pack_cache_drop(&c, gp);
         c.check_flags();
     });
 }
@@ -469,11 +503,9 @@ int jues_cc_create(jues_ctx *ctx, int method, const double *gao, int gao_is_devi
         cudaSetDevice(c.device);
         DBuf<double> g;
         const double *gp = gao;
-        if (!gao_is_device) {
-            Ctx::HostPhase ph(&c, "host:h2d_ao_eri");
-            g = h2d(c, gao, (size_t)n * n * n * n);
-            gp = g.p;
-        }
+        if (!gao_is_device)
+            gp = ao_operand(c, gao, (size_t)n * n * n * n,
+                            op.transform_precision >= 0 ? op.transform_precision : op.precision, g);
         DBuf<double> co = h2d(c, Cocc, (size_t)n * o), cv = h2d(c, Cvir, (size_t)n * v);
         DBuf<double> de = h2d(c, eps, (size_t)n);
         std::unique_ptr<jues_cc> cc(new jues_cc());

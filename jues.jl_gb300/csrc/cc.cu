@@ -128,7 +128,7 @@ double ccd_sweep(CCState *s, int prec) {
       plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
 
     s->cache_operands = false;
-    return t2_finalize(ctx, s->L.p, Z, s->eps.p, (int)o, (int)v, T, s->Tn.p);
+    return t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -264,6 +264,8 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         Perm4 q{{o, v, v, o}, {1, ov * o, o, ov}, {1, o, ov, ov * v}};
         permute4(ctx, q, -1.0, s->ovov.p, 0.0, s->ovovK.p);
     }
+    s->invD = DBuf<double>(ctx, t2n);
+    inv_denominators(ctx, s->eps.p, o, v, s->invD.p);
     s->T = DBuf<double>(ctx, t2n);
     s->Tn = DBuf<double>(ctx, t2n);
     s->Tt = DBuf<double>(ctx, t2n);
@@ -689,7 +691,7 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
 
     if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia
-    double r2 = t2_finalize(ctx, s->L.p, Z, s->eps.p, (int)o, (int)v, T, s->Tn.p);
+    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p);
     // t1n = R1 / D_ia and its step norm
     const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, t1);
     s->r1sq = r1;

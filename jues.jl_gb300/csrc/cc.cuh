@@ -14,6 +14,7 @@ struct CCState {
     int precision = JUES_PREC_FP64;
     // integrals, physicists' notation, column-major as the reference's get_eri blocks
     DBuf<double> eps, oovv, ovov, ovvo, oooo, vvvv, ooov, ovvv;
+    DBuf<double> invD;           // 1 / D[i,j,a,b], formed once
     DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;

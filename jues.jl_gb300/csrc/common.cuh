@@ -87,6 +87,10 @@ struct Ctx {
     void *splitk_ws = nullptr;         // split-K partial sums, grown on demand
     size_t splitk_bytes = 0;
     cudaMemPool_t pool = nullptr;      // stream-ordered pool behind alloc/free (keeps freed memory)
+    // the device reads pageable host memory through the host page tables (ATS, e.g. Grace), so
+    // the split forms can pack host operands without a device copy (jues_ctx_set_ao_direct)
+    bool ao_direct = false;
+    bool ao_direct_supported = false;
     Ctx();
     ~Ctx();
 
@@ -211,10 +215,12 @@ double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v);
 double mp2_gamma(Ctx *ctx, const double *K, const double *eps, int o, int v, double e_bar, double *G);
 // CC energy: sum oovv[i,j,a,b] (2 X[i,j,a,b] - X[j,i,a,b]) with X = T2 (+ t1 t1 when t1)
 double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t1, int o, int v);
-// T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a]) / D ; returns ||Tn - Told||^2
+// T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a]) invD ; returns ||Tn - Told||^2
 // if Told != nullptr.  Writes Tn.
-double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *eps, int o, int v,
+double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
                    const double *Told, double *Tn);
+// invD[i,j,a,b] = 1 / (e_i + e_j - e_a - e_b)
+void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out);
 // t1n[i,a] /= (e_i - e_a) in place; returns ||t1n - t1old||^2
 double t1_finalize(Ctx *ctx, double *t1n, const double *eps, int o, int v, const double *t1old);
 // X[i,j,a,b] = (L[...]) / D in place variants used for guesses

@@ -143,9 +143,22 @@ __global__ void ccenergy_kernel(const double *__restrict__ W, const double *__re
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// 1 / D[i,j,a,b] = 1 / (e_i + e_j - e_a - e_b), formed once per CC problem: GB300 runs FP64 at a
+// few operations per clock per SM, so an FP64 division per element would dominate the sweep's
+// finalisation; the sweeps then multiply.
+__global__ void inv_denominators_kernel(const double *__restrict__ eps, int o, int v, double *__restrict__ out) {
+    const long long oo = (long long)o * o, n = oo * v * v;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long ij = x % oo, ab = x / oo;
+        int i = (int)(ij % o), j = (int)(ij / o), a = (int)(ab % v), b = (int)(ab / v);
+        out[x] = 1.0 / (eps[i] + eps[j] - eps[o + a] - eps[o + b]);
+    }
+}
+
 // Tn[i,j,a,b] = (L[i,j,a,b] + Z[i,j,a,b] + Z[j,i,b,a]) / D, and the squared step norm.
 __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *__restrict__ Z,
-                                   const double *__restrict__ eps, int o, int v,
+                                   const double *__restrict__ invD, int o, int v,
                                    const double *__restrict__ Told, double *__restrict__ Tn,
                                    double *part) {
     const long long oo = (long long)o * o;
@@ -154,12 +167,11 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
     for (long long p = blockIdx.x; p < npair; p += gridDim.x) {
         int a, b;
         pair_ab(p, a, b);
-        const double ea = eps[o + a], eb = eps[o + b];
         const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
         for (long long ij = threadIdx.x; ij < oo; ij += blockDim.x) {
             int i = (int)(ij % o), j = (int)(ij / o);
             long long ji = j + (long long)o * i;
-            double inv = 1.0 / (eps[i] + eps[j] - ea - eb);
+            const double inv = invD[ab + ij];   // D is symmetric in (a, b)
             double x = (L[ab + ij] + Z[ab + ij] + Z[ba + ji]) * inv;
             Tn[ab + ij] = x;
             if (Told) { double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
@@ -355,13 +367,20 @@ double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t
     return finish_reduce(ctx, nb);
 }
 
-double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *eps, int o, int v,
+void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out) {
+    long long n = (long long)o * o * v * v;
+    Ctx::Scope s(ctx, "inv_denominators");
+    inv_denominators_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(eps, o, v, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
                    const double *Told, double *Tn) {
     long long npair = (long long)v * (v + 1) / 2;
     int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
     {
         Ctx::Scope s(ctx, "t2_finalize");
-        t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, eps, o, v, Told, Tn, ctx->d_red);
+        t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     return Told ? finish_reduce(ctx, nb) : 0.0;

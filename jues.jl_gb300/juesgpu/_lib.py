@@ -97,6 +97,7 @@ SIGNATURES = {
     "jues_auto_rccsd": (C.c_int, [VP, DP, DP, C.c_int, DP, C.c_int, C.c_int, C.c_int, C.POINTER(CCOpts), C.c_int,
                                   DP, DP, DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
     "jues_cc_pT": (C.c_int, [VP, C.c_int, DP]),
+    "jues_ctx_set_ao_direct": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "jues_cc_iterate": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "jues_cc_set_precision": (C.c_int, [VP, C.c_int]),
     "jues_cc_energy": (C.c_int, [VP, DP]),
@@ -181,6 +182,12 @@ class Context:
 
     def profile_reset(self):
         check(self.lib.jues_ctx_profile_reset(self.h))
+
+    def set_ao_direct(self, enable: bool) -> bool:
+        """Read host AO integrals in place where the device supports it; returns whether on."""
+        a = C.c_int()
+        check(self.lib.jues_ctx_set_ao_direct(self.h, 1 if enable else 0, C.byref(a)))
+        return bool(a.value)
 
     def launches(self) -> int:
         return int(self.lib.jues_ctx_launch_count(self.h))

@@ -247,3 +247,22 @@ def test_rccd_split3_transform_within_one_microhartree(lib):
                            transform_precision="split3", return_log=True)
     assert abs(e - ref) < 1e-6, (e, ref)
     assert all(r[4] == 1 for r in log)
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_ao_direct_matches_device_copy(lib, name):
+    # split forms pack the host AO array in place where the device reads pageable memory through
+    # the host page tables; the packed values, hence the results, are the same bits as after a
+    # device copy
+    from juesgpu import MollerPlesset
+    from juesgpu.CoupledCluster import mRCCD
+    ctx = lib.context(0)
+    w = make_named(name).wfn()
+    on = ctx.set_ao_direct(True)
+    e1 = MollerPlesset.do_rmp2(w, precision="split_bf16")
+    c1 = mRCCD.do_rccd(w, maxit=3, r_conv=0.0, guess="mp2", precision="split_bf16", refine=0)
+    ctx.set_ao_direct(False)
+    e2 = MollerPlesset.do_rmp2(w, precision="split_bf16")
+    c2 = mRCCD.do_rccd(w, maxit=3, r_conv=0.0, guess="mp2", precision="split_bf16", refine=0)
+    ctx.set_ao_direct(on)
+    assert e1 == e2 and c1 == c2, (on, e1, e2, c1, c2)
