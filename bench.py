@@ -429,7 +429,7 @@ def run_gpu(args):
         e2e = {"value": t_e2e / len(lg), "unit": "s/iter", "h2d_bytes_per_step": int(h2d / len(lg)),
                "d2h_bytes_per_step": 8, "sweeps": len(lg), "wall_s": t_e2e,
                "kernel_ms": {("all" if k == "" else k): v for k, v in e2e_kernels.items()},
-               "host_phase_ms": e2e_host, "ao_direct": ctx.set_ao_direct(True),
+               "host_phase_ms": e2e_host,
                "includes": "H2D of AO ERIs, split transform "
                "of the 5 RCCD blocks, sweeps, energy read-back"}
 
@@ -480,6 +480,31 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gemm(args):
+    """One jues_gemm call repeated (--warmup untimed, --steps timed with the library's events):
+    a small standalone case for profiler captures of the operand pack and the GEMM kernel."""
+    from juesgpu import _lib
+    M, N, K = args.gemm
+    rng = np.random.default_rng(0)
+    A = np.asfortranarray(rng.standard_normal((M, K)))
+    B = np.asfortranarray(rng.standard_normal((K, N)))
+    ctx = _lib.context(0)
+    for _ in range(args.warmup):
+        _lib.gemm(A, B, precision=args.gemm_precision)
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    for _ in range(args.steps):
+        _lib.gemm(A, B, precision=args.gemm_precision)
+    g_ms, g_n = ctx.profile("gemm")
+    p_ms, p_n = ctx.profile("pack_split")
+    ctx.set_profiling(False)
+    flops = 2.0 * M * N * K * (3 if args.gemm_precision == "split_bf16" else 6)
+    print(json.dumps({"gemm": [M, N, K], "precision": args.gemm_precision, "steps": args.steps,
+                      "gemm_ms": g_ms / max(args.steps, 1), "pack_ms": p_ms / max(args.steps, 1),
+                      "pack_launches": p_n, "tflops_executed": flops / (g_ms / args.steps * 1e-3) / 1e12
+                      if g_ms > 0 else None}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -499,7 +524,14 @@ def main():
                     help="also measure the batched MP2 energy+adjoint form on this many systems")
     ap.add_argument("--shape", default="S200", choices=sorted(SHAPES),
                     help="S200 is the benchmark; S100 is the small case used for profiler captures")
+    ap.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"), default=None,
+                    help="instead: time one split GEMM C = A B (A M x K, B K x N, FP64 host arrays "
+                         "through jues_gemm) -- the profiler case for the pack and GEMM kernels")
+    ap.add_argument("--gemm-precision", default="split_bf16", choices=["split_bf16", "split3", "fp64"])
     args = ap.parse_args()
+    if args.gemm:
+        run_gemm(args)
+        return
     global SHAPE
     SHAPE = SHAPES[args.shape]
     if args.warmup < 3 and args.impl == "gb300":

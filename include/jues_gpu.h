@@ -92,8 +92,9 @@ JUES_API int jues_ctx_create(int device, jues_ctx **out);
 /* AO integrals read in place (no reference counterpart).  Where the device reads pageable host
  * memory through the host page tables (ATS, e.g. Grace-Blackwell over NVLink-C2C), the split
  * forms pack the caller's n^4 AO array straight from host memory instead of copying it to the
- * device first.  On by default where supported (environment JUES_AO_DIRECT=0 turns the
- * default off); enable = 0 forces the copy.  *active (may be NULL) tells whether it is on. */
+ * device first.  Off by default (environment JUES_AO_DIRECT=1 turns the default on): on GB300
+ * with Grace the in-place reads measured ~8 GB/s, below the page-locked copy the library uses
+ * otherwise (~200 GB/s).  *active (may be NULL) tells whether it is on. */
 JUES_API int jues_ctx_set_ao_direct(jues_ctx *ctx, int enable, int *active);
 JUES_API int jues_ctx_destroy(jues_ctx *ctx);
 /* Cap the device memory the context may hold (bytes, 0 = no cap); used to exercise the
