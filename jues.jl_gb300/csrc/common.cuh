@@ -54,9 +54,26 @@ inline Mode mode2(long long d0, long long s0, long long s1) { return Mode{d0, MO
 inline Mode mode3(long long d0, long long d1, long long s0, long long s1, long long s2) {
     return Mode{d0, d1, s0, s1, s2};
 }
+// 64-bit integer division is a long instruction sequence on the GPU; plain modes need none, and
+// indices and extents below 2^32 divide in 32 bits
+__host__ __device__ inline void divmod_ll(long long r, long long d, long long &q, long long &rem) {
+    if ((unsigned long long)r < (1ull << 32) && (unsigned long long)d < (1ull << 32)) {
+        const unsigned rr = (unsigned)r, dd = (unsigned)d, qq = rr / dd;
+        q = qq;
+        rem = (long long)(rr - qq * dd);
+    } else {
+        q = r / d;
+        rem = r - q * d;
+    }
+}
 __host__ __device__ inline long long mode_off(const Mode &m, long long r) {
-    long long q = r / m.d0;
-    return (r - q * m.d0) * m.s0 + (q % m.d1) * m.s1 + (q / m.d1) * m.s2;
+    if (m.d0 == MODE_BIG) return r * m.s0;
+    long long q, i0;
+    divmod_ll(r, m.d0, q, i0);
+    if (m.d1 == MODE_BIG) return i0 * m.s0 + q * m.s1;
+    long long q2, i1;
+    divmod_ll(q, m.d1, q2, i1);
+    return i0 * m.s0 + i1 * m.s1 + q2 * m.s2;
 }
 
 // ---------------------------------------------------------------------------------------

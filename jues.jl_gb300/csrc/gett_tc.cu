@@ -54,14 +54,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
+// try_wait with a suspend-time hint: a waiting thread sleeps until the phase completes (or up to
+// 20 us) instead of polling, which keeps the spinning warps off the shared-memory pipe the
+// tensor cores read their operands through
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
         : "memory");
     return ok != 0;
 }
@@ -72,7 +75,7 @@ __device__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_fl
     unsigned long long t0 = 0;
     for (uint32_t it = 0;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u) {
+        if ((it & 15u) == 15u) {
             if (*abort_flag || (*gflags & FLAG_TIMEOUT)) return false;
             unsigned long long t = gtimer();
             if (t0 == 0) t0 = t;
@@ -86,7 +89,7 @@ __device__ bool mbar_wait_quiet(uint64_t *bar, uint32_t parity) {
     unsigned long long t0 = 0;
     for (uint32_t it = 0;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u) {
+        if ((it & 15u) == 15u) {
             unsigned long long t = gtimer();
             if (t0 == 0) t0 = t;
             else if (t - t0 > WAIT_LIMIT_NS) return false;
