@@ -424,6 +424,7 @@ def run_gpu(args):
         e2e_host = {k: ctx.profile("host:" + k)[0] for k in ("h2d_ao_eri", "cc_create", "integral_blocks",
                                                              "release_ao_eri")}
         e2e_kernels[""] -= ctx.profile("host:")[0]   # kernel events only
+        e2e_host["register_failures"] = ctx.profile("host:register_failed")[1]
         ctx.set_profiling(False)
         h2d = gao.nbytes + system.C.nbytes + eps.nbytes
         e2e = {"value": t_e2e / len(lg), "unit": "s/iter", "h2d_bytes_per_step": int(h2d / len(lg)),

@@ -62,10 +62,13 @@ DBuf<double> h2d(Ctx &ctx, const double *h, size_t n) {
     const size_t bytes = n * sizeof(double);
     bool registered = false;
     if (bytes >= (size_t(64) << 20)) {
-        if (cudaHostRegister(const_cast<double *>(h), bytes, cudaHostRegisterDefault) == cudaSuccess)
+        const cudaError_t e = cudaHostRegister(const_cast<double *>(h), bytes, cudaHostRegisterDefault);
+        if (e == cudaSuccess) {
             registered = true;
-        else
+        } else {
             cudaGetLastError();   // already page-locked by the caller, or not registrable: plain copy
+            if (ctx.profiling) ctx.prof["host:register_failed_" + std::to_string((int)e)].launches += 1;
+        }
     }
     JUES_CHECK_CUDA(cudaMemcpyAsync(d.p, h, bytes, cudaMemcpyHostToDevice, ctx.stream));
     if (registered) {

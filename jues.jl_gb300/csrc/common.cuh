@@ -209,6 +209,7 @@ void batch_cache_destroy(BatchCache *p);
 void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, double *e_out, double **gao_bar,
                 double **C_bar, jues_batch_info *info);
 void pack_cache_drop(Ctx *ctx, const void *ptr);
+void pack_cache_forget(Ctx *ctx, const void *p, size_t bytes);   // on every free of device memory
 
 // ---------------------------------------------------------------------------------------
 // bandwidth kernels (kernels.cu)

@@ -19,8 +19,9 @@ Ctx::Ctx() {}
 
 Ctx::~Ctx() {
     if (stream) cudaStreamSynchronize(stream);
-    pack_cache_destroy(pack);
-    pack = nullptr;
+    PackCache *pk = pack;
+    pack = nullptr;   // the cache's own buffers are freed below; no lookups into it meanwhile
+    pack_cache_destroy(pk);
     batch_cache_destroy(batch);
     batch = nullptr;
     for (auto &kv : prof) {
@@ -78,6 +79,7 @@ void *Ctx::alloc(size_t bytes) {
 
 void Ctx::free(void *p, size_t bytes) {
     if (!p) return;
+    pack_cache_forget(this, p, bytes);
     cudaFreeAsync(p, stream);   // reusable by later work on this stream once its readers are done
     mem_used -= bytes;
 }

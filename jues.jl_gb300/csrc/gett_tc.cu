@@ -558,9 +558,11 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
     __shared__ double tile[PR][PK + 1];
     __shared__ __align__(16) __half outp[NP][PR][PK];
     __shared__ long long roff[PR], koff[PK];
-    const long long kblocks = (Kpad + PK - 1) / PK;
-    const long long r0 = (blockIdx.x / kblocks) * PR;
-    const long long k0 = (blockIdx.x % kblocks) * PK;
+    // consecutive blocks follow the source's unit-stride index (K when kfast, rows otherwise),
+    // so the blocks resident at one time read long contiguous runs of it
+    const long long kblocks = (Kpad + PK - 1) / PK, rblocks = Rpad / PR;
+    const long long r0 = (kfast ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
+    const long long k0 = (kfast ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
     const int tid = threadIdx.x;
     if (tid < PR) {
         const long long r = r0 + tid;
@@ -666,6 +668,7 @@ struct PackEntry {
     DBuf<int> exps;
 };
 struct PackCache {
+    bool busy = false;   // inside a cache operation: frees of the cache's own buffers are not lookups
     std::vector<std::unique_ptr<PackEntry>> cached;
     DBuf<__half> scratch[2];
     DBuf<int> scratch_exp[2];
@@ -691,13 +694,41 @@ struct Packed {
     const int *exps;
 };
 
-void pack_cache_destroy(PackCache *p) { delete p; }
+void pack_cache_destroy(PackCache *p) {
+    if (p) p->busy = true;
+    delete p;
+}
 void pack_cache_clear(Ctx *ctx) {
     if (ctx->pack) {
+        ctx->pack->busy = true;
         ctx->pack->cached.clear();
         ctx->pack->free_planes.clear();
         ctx->pack->free_exps.clear();
+        ctx->pack->busy = false;
     }
+}
+// Entries are keyed by their source address.  Device memory is reused quickly (the context's
+// pool hands freed blocks out again), so every free of device memory forgets the entries whose
+// source lay in the freed range: a later array at the same address can never hit a stale pack.
+void pack_cache_forget(Ctx *ctx, const void *p, size_t bytes) {
+    if (!ctx->pack || ctx->pack->busy || !p) return;
+    PackCache &pc = *ctx->pack;
+    const char *b = static_cast<const char *>(p), *e = b + bytes;
+    auto inside = [&](const std::unique_ptr<PackEntry> &x) {
+        const char *q = reinterpret_cast<const char *>(x->src);
+        return q >= b && q < e;
+    };
+    bool any = false;
+    for (auto &x : pc.cached) any = any || inside(x);
+    if (!any) return;
+    pc.busy = true;
+    for (auto &x : pc.cached)
+        if (inside(x)) {
+            pc.free_planes.push_back(std::move(x->buf));
+            pc.free_exps.push_back(std::move(x->exps));
+        }
+    pc.cached.erase(std::remove_if(pc.cached.begin(), pc.cached.end(), inside), pc.cached.end());
+    pc.busy = false;
 }
 void pack_cache_drop(Ctx *ctx, const void *ptr) {
     if (!ctx->pack) return;
@@ -727,6 +758,11 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
     __half *dst;
     int *ex;
     std::unique_ptr<PackEntry> ent;
+    struct Busy {
+        PackCache &c;
+        explicit Busy(PackCache &x) : c(x) { c.busy = true; }
+        ~Busy() { c.busy = false; }
+    } busy(pc);
     if (cache) {
         ent.reset(new PackEntry{src, rm, km, R, K, Rpad, Kpad, np, take_buffer(ctx, pc.free_planes, need),
                                 take_buffer(ctx, pc.free_exps, (size_t)nchunk * Rpad)});

@@ -266,3 +266,24 @@ def test_ao_direct_matches_device_copy(lib, name):
     c2 = mRCCD.do_rccd(w, maxit=3, r_conv=0.0, guess="mp2", precision="split_bf16", refine=0)
     ctx.set_ao_direct(on)
     assert e1 == e2 and c1 == c2, (on, e1, e2, c1, c2)
+
+
+def test_pack_cache_never_serves_a_freed_address(lib):
+    # split operands are cached by source address and device memory is reused at once by the
+    # context's pool: a session after another in the same context must give the bits of a
+    # session in a fresh context
+    from juesgpu import _lib
+    from juesgpu.CoupledCluster import mRCCD
+    w = make_named("S100").wfn()
+    kw = dict(maxit=4, r_conv=0.0, guess="mp2", precision="split_bf16", refine=0)
+    mRCCD.do_rccd(w, transform_precision="fp64", **kw)
+    e_after = mRCCD.do_rccd(w, transform_precision="split3", **kw)
+    saved = _lib._ctxs.get(0)
+    fresh = _lib.Context(0)
+    _lib._ctxs[0] = fresh
+    try:
+        e_fresh = mRCCD.do_rccd(w, transform_precision="split3", **kw)
+    finally:
+        _lib._ctxs[0] = saved
+        fresh.close()
+    assert e_after == e_fresh, (e_after, e_fresh)
