@@ -365,11 +365,15 @@ def run_gpu(args):
         converged = {}
         # FP64 integrals with two closing FP64 sweeps; FP64 integrals, split sweeps only; the
         # three-plane split integrals with split sweeps only (no FP64 arithmetic at all)
-        for label, refine, tprec, rconv in (("refine2", 2, "fp64", 1e-9), ("refine0", 0, "fp64", 1e-8),
-                                            ("split3_integrals", 0, "split3", 1e-8)):
+        # (split-only runs stop when the energy changes by less than 0.1 uEh: their step norm and
+        # energy level off at the split noise floor, ~1e-7 and ~1e-8 Eh)
+        for label, refine, tprec, rconv, econv in (("refine2", 2, "fp64", 1e-9, 0.0),
+                                                   ("refine0", 0, "fp64", 0.0, 1e-7),
+                                                   ("split3_integrals", 0, "split3", 0.0, 1e-7)):
             t0 = time.perf_counter()
             s2 = CCSession(0, gao=gao, Cocc=Cocc, Cvir=Cvir, eps=eps, device=local, precision="split_bf16",
-                           guess="mp2", diis=True, r_conv=rconv, refine=refine, maxit=60, transform_precision=tprec)
+                           guess="mp2", diis=True, r_conv=rconv, e_conv=econv, refine=refine, maxit=60,
+                           transform_precision=tprec)
             t_setup = time.perf_counter() - t0
             s2.iterate(60)
             wall = time.perf_counter() - t0

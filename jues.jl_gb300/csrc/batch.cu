@@ -297,6 +297,12 @@ void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, do
     JUES_CHECK_CUDA(cudaEventCreate(&t3));
     JUES_CHECK_CUDA(cudaEventRecord(t0, ctx->stream));
     double *A = bp.arena.p;
+    HostPins pins;   // the systems' AO arrays and adjoint outputs, page-locked for this call
+    for (int s = 0; s < nsys; ++s) {
+        const size_t n = (size_t)sys[s].n;
+        pins.pin(sys[s].gao, n * n * n * n * sizeof(double));
+        if (want_gb && gao_bar && gao_bar[s]) pins.pin(gao_bar[s], n * n * n * n * sizeof(double));
+    }
     for (int s = 0; s < nsys; ++s) {
         const size_t n = (size_t)sys[s].n;
         JUES_CHECK_CUDA(cudaMemcpyAsync(A + bp.off_g[s], sys[s].gao, n * n * n * n * sizeof(double),

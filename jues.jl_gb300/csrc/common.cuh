@@ -137,6 +137,19 @@ struct Ctx {
     void check_flags();   // reads d_flags after a sync; throws on a set flag
 };
 
+// Page-locks caller-owned host ranges for the copies of one call and releases them at scope
+// exit (after the caller has synchronised).  A pageable copy is staged through the driver's
+// bounce buffers at a few GB/s; a registered one runs at link speed.  Ranges below min_bytes,
+// and ranges that cannot be registered (e.g. already page-locked), are copied as they are.
+struct HostPins {
+    std::vector<void *> regs;
+    void pin(const void *p, size_t bytes, size_t min_bytes = size_t(4) << 20);
+    HostPins() = default;
+    HostPins(const HostPins &) = delete;
+    HostPins &operator=(const HostPins &) = delete;
+    ~HostPins();
+};
+
 // device buffer owned by a context
 template <class T>
 struct DBuf {

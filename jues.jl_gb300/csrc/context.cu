@@ -77,6 +77,18 @@ void *Ctx::alloc(size_t bytes) {
     return p;
 }
 
+void HostPins::pin(const void *p, size_t bytes, size_t min_bytes) {
+    if (!p || bytes < min_bytes) return;
+    if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterDefault) == cudaSuccess)
+        regs.push_back(const_cast<void *>(p));
+    else
+        cudaGetLastError();
+}
+
+HostPins::~HostPins() {
+    for (void *p : regs) cudaHostUnregister(p);
+}
+
 void Ctx::free(void *p, size_t bytes) {
     if (!p) return;
     pack_cache_forget(this, p, bytes);

@@ -94,14 +94,18 @@ __global__ void pt_zero(double *p, int n) {
 }
 
 // one W term: W[(rows),(cols)] (+)= alpha sum_x A[(rows),x] B[x,(cols)]
+// A operands that are the same slice for every pair sharing i (or j) are kept packed
+// (a_const) and dropped at the end
 void term(Ctx *ctx, int prec, long long M, long long N, long long K, double alpha, const double *A, Mode mA, Mode kA,
-          const double *B, Mode kB, Mode nB, double beta, double *W, Mode mC, Mode nC, const char *name) {
+          const double *B, Mode kB, Mode nB, double beta, double *W, Mode mC, Mode nC, const char *name,
+          bool a_const = false) {
     GettArgs g;
     g.M = M; g.N = N; g.K = K;
     g.alpha = alpha; g.beta = beta;
     g.A = A; g.mA = mA; g.kA = kA;
     g.B = B; g.kB = kB; g.nB = nB;
     g.C = W; g.mC = mC; g.nC = nC;
+    g.a_const = a_const;
     gett(ctx, prec, g, name);
 }
 
@@ -146,16 +150,16 @@ double pT_energy(Ctx *ctx, int prec, const double *T1, const double *T2, const V
             // PerturbativeTriples.jl:104-111; each line below is one term (ijk, ikj, kij, kji, jki, jik)
             // Vvvvo[b,d,a,i] T2[k,j,c,d] -> rows (a,b), cols (c,k)
             term(ctx, prec, v2, v * nk, v, 1.0, Vi, mode2(v, V0[2], V0[0]), plain(V0[1]), T2 + (long long)o * j,
-                 plain(oov), mode2(v, oo, 1), 0.0, w, ab, ck, "pt_w");
+                 plain(oov), mode2(v, oo, 1), 0.0, w, ab, ck, "pt_w", true);
             // - Vvooo[c,k,j,l] T2[i,l,a,b] -> rows (a,b), cols (c,k)
             term(ctx, prec, v2, v * nk, o, -1.0, T2 + i, mode2(v, oo, oov), plain(o), Vo.p + j * O0[2],
-                 plain(O0[3]), mode2(v, O0[0], O0[1]), 1.0, w, ab, ck, "pt_w");
+                 plain(O0[3]), mode2(v, O0[0], O0[1]), 1.0, w, ab, ck, "pt_w", true);
             // Vvvvo[c,d,a,i] T2[j,k,b,d] -> rows (a,c), cols (b,k)
             term(ctx, prec, v2, v * nk, v, 1.0, Vi, mode2(v, V0[2], V0[0]), plain(V0[1]), T2 + j, plain(oov),
-                 mode2(v, oo, o), 1.0, w, ac, bk, "pt_w");
+                 mode2(v, oo, o), 1.0, w, ac, bk, "pt_w", true);
             // - Vvooo[b,j,k,l] T2[i,l,a,c] -> rows (a,c), cols (b,k)
             term(ctx, prec, v2, v * nk, o, -1.0, T2 + i, mode2(v, oo, oov), plain(o), Vo.p + j * O0[1],
-                 plain(O0[3]), mode2(v, O0[0], O0[2]), 1.0, w, ac, bk, "pt_w");
+                 plain(O0[3]), mode2(v, O0[0], O0[2]), 1.0, w, ac, bk, "pt_w", true);
             // Vvvvo[a,d,c,k] T2[j,i,b,d] -> rows (a,c,k), cols b
             term(ctx, prec, v2 * nk, v, v, 1.0, Vv.p, mode3(v, v, V0[0], V0[2], V0[3]), plain(V0[1]),
                  T2 + j + (long long)o * i, plain(oov), plain(oo), 1.0, w, ack, plain(v), "pt_w");
@@ -170,16 +174,16 @@ double pT_energy(Ctx *ctx, int prec, const double *T1, const double *T2, const V
                  plain(O0[3]), plain(O0[0]), 1.0, w, bck, plain(1), "pt_w");
             // Vvvvo[c,d,b,j] T2[i,k,a,d] -> rows (b,c), cols (a,k)
             term(ctx, prec, v2, v * nk, v, 1.0, Vj, mode2(v, V0[2], V0[0]), plain(V0[1]), T2 + i, plain(oov),
-                 mode2(v, oo, o), 1.0, w, bc, ak, "pt_w");
+                 mode2(v, oo, o), 1.0, w, bc, ak, "pt_w", true);
             // - Vvooo[a,i,k,l] T2[j,l,b,c] -> rows (b,c), cols (a,k)
             term(ctx, prec, v2, v * nk, o, -1.0, T2 + j, mode2(v, oo, oov), plain(o), Vo.p + i * O0[1],
-                 plain(O0[3]), mode2(v, O0[0], O0[2]), 1.0, w, bc, ak, "pt_w");
+                 plain(O0[3]), mode2(v, O0[0], O0[2]), 1.0, w, bc, ak, "pt_w", true);
             // Vvvvo[a,d,b,j] T2[k,i,c,d] -> rows (a,b), cols (c,k)
             term(ctx, prec, v2, v * nk, v, 1.0, Vj, mode2(v, V0[0], V0[2]), plain(V0[1]), T2 + (long long)o * i,
-                 plain(oov), mode2(v, oo, 1), 1.0, w, ab, ck, "pt_w");
+                 plain(oov), mode2(v, oo, 1), 1.0, w, ab, ck, "pt_w", true);
             // - Vvooo[c,k,i,l] T2[j,l,b,a] -> rows (a,b), cols (c,k)
             term(ctx, prec, v2, v * nk, o, -1.0, T2 + j, mode2(v, oov, oo), plain(o), Vo.p + i * O0[2],
-                 plain(O0[3]), mode2(v, O0[0], O0[1]), 1.0, w, ab, ck, "pt_w");
+                 plain(O0[3]), mode2(v, O0[0], O0[1]), 1.0, w, ab, ck, "pt_w", true);
             {
                 Ctx::Scope s(ctx, "pt_energy");
                 const long long work = ntri * nk;
@@ -189,6 +193,10 @@ double pT_energy(Ctx *ctx, int prec, const double *T1, const double *T2, const V
                 JUES_CHECK_CUDA(cudaGetLastError());
             }
         }
+    }
+    for (int i = 0; i < o; ++i) {   // the kept slices
+        pack_cache_drop(ctx, Vv.p + i * V0[3]);
+        pack_cache_drop(ctx, T2 + i);
     }
     pt_sum_slots<<<1, 1024, 0, ctx->stream>>>(slots.p, PT_BLOCKS, slots.p + PT_BLOCKS);
     JUES_CHECK_CUDA(cudaGetLastError());
