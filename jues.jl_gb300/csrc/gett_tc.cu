@@ -534,20 +534,22 @@ constexpr int PR = 16, PK = 128, KCH = 128;   // pack tile = one scaling chunk =
 // of the padded tile and every scale is written, so nothing has to be cleared beforehand.
 __device__ __forceinline__ int exp_bound(double x) {
     // smallest e with |x| < 2^e (INT_MIN for zero and subnormals, which are flushed)
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int E = (int)((b >> 52) & 0x7FF);
+    const int E = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7FFu);
     return E == 0 ? INT_MIN : E - 1022;
 }
 // q = rint(x 2^(bits - e)), ties away from zero, for |x| < 2^e: bits = 19 (two planes) or 29
-// (three planes)
-__device__ __forceinline__ long long fixed_q(double x, int e, int bits) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int E = (int)((b >> 52) & 0x7FF);
+// (three planes).  With x = +-m 2^(E-1075), q = floor((m + 2^(r-1)) / 2^r), r = 1075 - bits + e - E
+// >= 54 - bits, which equals floor((floor(m / 2^(r-1)) + 1) / 2) and needs only the top 32
+// bits of m (m >> 21), so the whole split runs in 32-bit integer arithmetic.
+__device__ __forceinline__ int fixed_q(double x, int e, int bits) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int E = (int)((hi >> 20) & 0x7FFu);
     if (E == 0 || e == INT_MIN) return 0;
-    const unsigned long long m = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    const int r = 1075 - bits + e - E;   // >= 54 - bits because |x| < 2^e
-    const unsigned long long q = r > 60 ? 0ull : ((m + (1ull << (r - 1))) >> r);
-    return (b >> 63) ? -(long long)q : (long long)q;
+    const int sh = 1075 - bits + e - E - 22;   // r - 22 >= 32 - bits > 0
+    if (sh >= 32) return 0;
+    const unsigned mh = (((hi & 0xFFFFFu) | 0x100000u) << 11) | (lo >> 21);   // m >> 21
+    const int q = (int)(((mh >> sh) + 1u) >> 1);
+    return (hi >> 31) ? -q : q;
 }
 
 template <int NP>
@@ -591,19 +593,19 @@ __global__ void __launch_bounds__(256) pack_split_kernel(const double *__restric
     if (t == 0) rexp[(k0 / KCH) * Rpad + r0 + rr] = ex;
 #pragma unroll
     for (int j = 0; j < PK / 16; ++j) {
-        const long long q = fixed_q(tile[rr][t + 16 * j], ex, 10 * NP - 1);
+        const int q = fixed_q(tile[rr][t + 16 * j], ex, 10 * NP - 1);
         if constexpr (NP == 2) {
-            const long long h = (q + 512) >> 10;
-            outp[0][rr][t + 16 * j] = __int2half_rn((int)h);            // |h| <= 512: exact in FP16
-            outp[1][rr][t + 16 * j] = __int2half_rn((int)(q - (h << 10)));
+            const int h = (q + 512) >> 10;   // arithmetic shift: floor
+            outp[0][rr][t + 16 * j] = __int2half_rn(h);            // |h| <= 512: exact in FP16
+            outp[1][rr][t + 16 * j] = __int2half_rn(q - h * 1024);
         } else {
             // q = 2^20 hi + 2^10 mid + lo, each in [-512, 512]
-            const long long h = (q + (1LL << 19)) >> 20;
-            const long long rem = q - (h << 20);
-            const long long m = (rem + 512) >> 10;
-            outp[0][rr][t + 16 * j] = __int2half_rn((int)h);
-            outp[1][rr][t + 16 * j] = __int2half_rn((int)m);
-            outp[2][rr][t + 16 * j] = __int2half_rn((int)(rem - (m << 10)));
+            const int h = (q + (1 << 19)) >> 20;
+            const int rem = q - h * 1048576;
+            const int m = (rem + 512) >> 10;
+            outp[0][rr][t + 16 * j] = __int2half_rn(h);
+            outp[1][rr][t + 16 * j] = __int2half_rn(m);
+            outp[2][rr][t + 16 * j] = __int2half_rn(rem - m * 1024);
         }
     }
     __syncthreads();
