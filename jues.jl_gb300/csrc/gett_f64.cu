@@ -95,12 +95,20 @@ __device__ __forceinline__ void gett_tile(const GroupProblem &g, long long tile,
     for (int i = 0; i < TM; ++i) {
         const long long om = sm.offCm[tr + 16 * i];
         if (om < 0) continue;
+        // a row's inputs are loaded before any of its outputs is stored (each element is this
+        // thread's alone; C and Cin may alias), so those loads are in flight together
+        double cin[TN];
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const long long on = sm.offCn[tc + 16 * j];
+            cin[j] = (g.beta != 0.0 && on >= 0) ? g.Cin[om + on] : 0.0;
+        }
 #pragma unroll
         for (int j = 0; j < TN; ++j) {
             const long long on = sm.offCn[tc + 16 * j];
             if (on < 0) continue;
             double v = g.alpha * acc[i][j];
-            if (g.beta != 0.0) v = fma(g.beta, g.Cin[om + on], v);
+            if (g.beta != 0.0) v = fma(g.beta, cin[j], v);
             g.C[om + on] = v;
         }
     }

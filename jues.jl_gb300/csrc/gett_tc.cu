@@ -497,13 +497,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             } else if (mrow < g.M) {
                 const long long rowoff = mode_off(g.mC, mrow);
+                const long long *co = coloff + half * HB;
+                // Each output element is read and written by this thread alone, so a batch's
+                // inputs are all loaded before any of its outputs is stored: the loads are in
+                // flight together instead of one load latency per column (C and Cin may alias).
+                constexpr int EB = HB < 32 ? HB : 32;
 #pragma unroll
-                for (int j = 0; j < HB; ++j) {
-                    const long long co = coloff[half * HB + j];
-                    if (co >= 0) {
-                        double val = g.alpha * (double)((j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]));
-                        if (g.beta != 0.0) val = fma(g.beta, g.Cin[rowoff + co], val);
-                        g.C[rowoff + co] = val;
+                for (int j0 = 0; j0 < HB; j0 += EB) {
+                    double cin[EB];
+#pragma unroll
+                    for (int j = 0; j < EB; ++j) {
+                        const long long c = co[j0 + j];
+                        cin[j] = (g.beta != 0.0 && c >= 0) ? __ldcs(g.Cin + rowoff + c) : 0.0;
+                    }
+#pragma unroll
+                    for (int j = 0; j < EB; ++j) {
+                        const long long c = co[j0 + j];
+                        const int jj = j0 + j;
+                        if (c >= 0) {
+                            double val = g.alpha * (double)((jj & 1) ? hi_f(acc2[jj >> 1]) : lo_f(acc2[jj >> 1]));
+                            if (g.beta != 0.0) val = fma(g.beta, cin[j], val);
+                            g.C[rowoff + c] = val;
+                        }
                     }
                 }
             }
@@ -520,22 +535,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 constexpr int PR = 16, PK = 128, KCH = 128;   // pack tile = one scaling chunk = two pipeline stages
 
-// FP64 operand -> integer-valued FP16 planes [2][Rpad][Kpad], K-major, and the per-(chunk,row)
+// FP64 operand -> integer-valued FP16 planes [NP][Rpad][Kpad], K-major, and the per-(chunk,row)
 // scales, in one pass.  A block covers 16 rows x one 128-wide K chunk (the last chunk may be 64
-// wide: Kpad is a multiple of 64), so the chunk maximum is a block-local reduction.  Each row
-// is handled by 16 consecutive lanes taking every 16th column (conflict-free shared-memory
-// reads); the FP16 planes are staged in shared memory and written as 16-byte rows.  The split works on the IEEE-754 bit pattern
+// wide: Kpad is a multiple of 64), so the chunk maximum is a block-local reduction.  Each
+// thread loads 8 elements (4 column pairs of one row when the source's rows are unit-stride,
+// one column pair of 4 rows when its K is) and keeps them in registers: the row maxima go
+// through shared-memory atomics, the planes are staged in shared memory as FP16 pairs and
+// written out as 8-byte pieces of 256-byte rows.  The split works on the IEEE-754 bit pattern
 // with integer arithmetic only (GB300 runs FP64 arithmetic at a small fraction of its integer
 // rate): for x = +-m 2^(E-1075) (m the 53-bit significand) and chunk scale e,
 //     q = rint(x 2^(19-e)) = round(m >> (1056 + e - E)),  hi = (q + 512) >> 10,  lo = q - 1024 hi,
 // so x ~ 2^(e-19) q = 2^(e-9) (hi + 2^-10 lo) with |hi| <= 512, |lo| <= 512.  The three-plane
 // form keeps 29 bits: q = rint(x 2^(29-e)) = 2^20 hi + 2^10 mid + lo, x ~ 2^(e-9) (hi + 2^-10 mid
-// + 2^-20 lo), |x - that| <= 2^(e-30).  Every element
-// of the padded tile and every scale is written, so nothing has to be cleared beforehand.
-__device__ __forceinline__ int exp_bound(double x) {
-    // smallest e with |x| < 2^e (INT_MIN for zero and subnormals, which are flushed)
-    const int E = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7FFu);
-    return E == 0 ? INT_MIN : E - 1022;
+// + 2^-20 lo), |x - that| <= 2^(e-30).  Every element of the padded tile and every scale is
+// written, so nothing has to be cleared beforehand.
+__device__ __forceinline__ int exp_field(double x) {
+    // biased exponent: 0 for zero and subnormals, which are flushed
+    return (int)(((unsigned)__double2hiint(x) >> 20) & 0x7FFu);
 }
 // q = rint(x 2^(bits - e)), ties away from zero, for |x| < 2^e: bits = 19 (two planes) or 29
 // (three planes).  With x = +-m 2^(E-1075), q = floor((m + 2^(r-1)) / 2^r), r = 1075 - bits + e - E
@@ -551,74 +567,122 @@ __device__ __forceinline__ int fixed_q(double x, int e, int bits) {
     const int q = (int)(((mh >> sh) + 1u) >> 1);
     return (hi >> 31) ? -q : q;
 }
-
+// the NP plane digits of q, each an integer in [-512, 512] (exact in FP16)
 template <int NP>
-__global__ void __launch_bounds__(256) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
+__device__ __forceinline__ void split_digits(int q, int (&d)[NP]) {
+    if constexpr (NP == 2) {
+        const int h = (q + 512) >> 10;   // arithmetic shift: floor
+        d[0] = h;
+        d[1] = q - h * 1024;
+    } else {
+        const int h = (q + (1 << 19)) >> 20;
+        const int rem = q - h * 1048576;
+        const int m = (rem + 512) >> 10;
+        d[0] = h;
+        d[1] = m;
+        d[2] = rem - m * 1024;
+    }
+}
+__device__ __forceinline__ uint32_t half_pair(int a, int b) {
+    const __half2 h = __halves2half2(__int2half_rn(a), __int2half_rn(b));
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// staged row pitch in 32-bit words (two FP16 each): 66 keeps the pair stores of both thread
+// layouts free of bank conflicts and the 8-byte row pieces aligned
+constexpr int PACK_PITCH = PK / 2 + 2;
+
+// KFAST: the source's K index is unit-stride (else its row index is)
+template <int NP, bool KFAST>
+__global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
-                                                         long long Kpad, int kfast, int *__restrict__ rexp,
+                                                         long long Kpad, int *__restrict__ rexp,
                                                          __half *__restrict__ dst) {
-    __shared__ double tile[PR][PK + 1];
-    __shared__ __align__(16) __half outp[NP][PR][PK];
+    __shared__ __align__(16) uint32_t outp[NP][PR][PACK_PITCH];
     __shared__ long long roff[PR], koff[PK];
-    // consecutive blocks follow the source's unit-stride index (K when kfast, rows otherwise),
-    // so the blocks resident at one time read long contiguous runs of it
-    const long long kblocks = (Kpad + PK - 1) / PK, rblocks = Rpad / PR;
-    const long long r0 = (kfast ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
-    const long long k0 = (kfast ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
-    const int tid = threadIdx.x;
+    __shared__ int rowE[PR];
+    // consecutive blocks follow the source's unit-stride index, so the blocks resident at one
+    // time read long contiguous runs of it
+    // block counts < 2^31 (checked at launch): 32-bit index arithmetic
+    const unsigned kblocks = (unsigned)((Kpad + PK - 1) / PK), rblocks = (unsigned)(Rpad / PR);
+    const long long r0 = (long long)(KFAST ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
+    const long long k0 = (long long)(KFAST ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (tid < PR) {
         const long long r = r0 + tid;
         roff[tid] = r < R ? mode_off(rmode, r) : -1;
+        rowE[tid] = 0;
     } else if (tid >= 64 && tid < 64 + PK) {
         const long long k = k0 + tid - 64;
         koff[tid - 64] = k < K ? mode_off(kmode, k) : -1;
     }
     __syncthreads();
+    // element (i, h): row row_of(i), column 2 pair_of(i) + h
+    auto row_of = [&](int i) { return KFAST ? (tid >> 6) + 4 * i : (tid & 15); };
+    auto pair_of = [&](int i) { return KFAST ? (tid & 63) : (tid >> 4) + 16 * i; };
+    double x[4][2];
 #pragma unroll
-    for (int i = 0; i < (PR * PK) / 256; ++i) {
-        const int e = tid + i * 256;
-        const int kk = kfast ? (e % PK) : (e / PR);
-        const int rr = kfast ? (e / PK) : (e % PR);
-        const long long a = roff[rr], b = koff[kk];
-        tile[rr][kk] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
-    }
-    __syncthreads();
-    // 16 lanes per row, lane t owns columns t, t + 16, ..., t + 112
-    const int rr = tid >> 4, t = tid & 15;
-    int ex = INT_MIN;
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < PK / 16; ++j) ex = max(ex, exp_bound(tile[rr][t + 16 * j]));
-#pragma unroll
-    for (int d = 1; d < 16; d <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, d));
-    if (t == 0) rexp[(k0 / KCH) * Rpad + r0 + rr] = ex;
-#pragma unroll
-    for (int j = 0; j < PK / 16; ++j) {
-        const int q = fixed_q(tile[rr][t + 16 * j], ex, 10 * NP - 1);
-        if constexpr (NP == 2) {
-            const int h = (q + 512) >> 10;   // arithmetic shift: floor
-            outp[0][rr][t + 16 * j] = __int2half_rn(h);            // |h| <= 512: exact in FP16
-            outp[1][rr][t + 16 * j] = __int2half_rn(q - h * 1024);
-        } else {
-            // q = 2^20 hi + 2^10 mid + lo, each in [-512, 512]
-            const int h = (q + (1 << 19)) >> 20;
-            const int rem = q - h * 1048576;
-            const int m = (rem + 512) >> 10;
-            outp[0][rr][t + 16 * j] = __int2half_rn(h);
-            outp[1][rr][t + 16 * j] = __int2half_rn(m);
-            outp[2][rr][t + 16 * j] = __int2half_rn(rem - m * 1024);
+        for (int h = 0; h < 2; ++h) {
+            const long long a = roff[row_of(i)], b = koff[2 * pair_of(i) + h];
+            x[i][h] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
         }
+    // row maxima of the exponent field
+    if constexpr (KFAST) {
+        // a warp's lanes share each of its four rows
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int m = __reduce_max_sync(0xffffffffu, max(exp_field(x[i][0]), exp_field(x[i][1])));
+            if (lane == 0) atomicMax(&rowE[row_of(i)], m);
+        }
+    } else {
+        // all eight elements share the thread's row; lanes l and l + 16 share a row
+        int m = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) m = max(m, max(exp_field(x[i][0]), exp_field(x[i][1])));
+        m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));
+        if (lane < 16) atomicMax(&rowE[lane], m);
     }
     __syncthreads();
-    // NP planes x PR rows x 16 segments of 8 halves
-#pragma unroll
-    for (int i = 0; i < (NP * PR * (PK / 8)) / 256; ++i) {
-        const int idx = tid + 256 * i;
-        const int seg = idx & 15, row = (idx >> 4) % PR, plane = idx / (16 * PR);
-        const long long k = k0 + 8 * seg;
-        if (k >= Kpad) continue;   // the 64-wide tail of the last chunk (Kpad is a multiple of 64)
-        *reinterpret_cast<uint4 *>(dst + (size_t)plane * Rpad * Kpad + (size_t)(r0 + row) * Kpad + k) =
-            *reinterpret_cast<const uint4 *>(&outp[plane][row][8 * seg]);
+    if (tid < PR) {
+        const int E = rowE[tid];
+        rexp[(k0 / KCH) * Rpad + r0 + tid] = E == 0 ? INT_MIN : E - 1022;
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = row_of(i);
+        const int E = rowE[r];
+        const int e = E == 0 ? INT_MIN : E - 1022;
+        int d0[NP], d1[NP];
+        split_digits<NP>(fixed_q(x[i][0], e, 10 * NP - 1), d0);
+        split_digits<NP>(fixed_q(x[i][1], e, 10 * NP - 1), d1);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) outp[p][r][pair_of(i)] = half_pair(d0[p], d1[p]);
+    }
+    __syncthreads();
+    // NP planes x PR rows x 32 pieces of 4 halves
+#pragma unroll
+    for (int j = 0; j < (NP * PR * 32) / 256; ++j) {
+        const int idx = tid + 256 * j;
+        const int seg = idx & 31, row = (idx >> 5) & (PR - 1), plane = idx >> 9;
+        const long long k = k0 + 4 * seg;
+        if (k >= Kpad) continue;   // the 64-wide tail of the last chunk (Kpad is a multiple of 64)
+        *reinterpret_cast<uint2 *>(dst + (size_t)plane * Rpad * Kpad + (size_t)(r0 + row) * Kpad + k) =
+            *reinterpret_cast<const uint2 *>(&outp[plane][row][2 * seg]);
+    }
+}
+
+template <int NP>
+void launch_pack(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
+                 long long Rpad, long long Kpad, int *ex, __half *dst) {
+    const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
+    JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
+    if (km.s0 == 1 && km.d0 > 1)
+        pack_split_kernel<NP, true><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex, dst);
+    else
+        pack_split_kernel<NP, false><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex, dst);
+    JUES_CHECK_CUDA(cudaGetLastError());
 }
 
 
@@ -782,18 +846,12 @@ static Packed pack_operand(Ctx *ctx, int slot, const double *src, const Mode &rm
         dst = pc.scratch[slot].p;
         ex = pc.scratch_exp[slot].p;
     }
-    const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
-    JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
-    const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     {
         Ctx::Scope s(ctx, "pack_split");
         if (np == 3)
-            pack_split_kernel<3><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
-                                                                            dst);
+            launch_pack<3>(ctx, src, rm, km, R, K, Rpad, Kpad, ex, dst);
         else
-            pack_split_kernel<2><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex,
-                                                                            dst);
-        JUES_CHECK_CUDA(cudaGetLastError());
+            launch_pack<2>(ctx, src, rm, km, R, K, Rpad, Kpad, ex, dst);
     }
     if (cache) pc.cached.push_back(std::move(ent));
     return Packed{dst, ex};
@@ -976,12 +1034,8 @@ void *noalloc_scratch_address(int device) {
 
 void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
                long long Rpad, long long Kpad, __half *dst, int *ex) {
-    const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
-    JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
-    const int kfast = (km.s0 == 1 && km.d0 > 1) ? 1 : 0;
     Ctx::Scope s(ctx, "pack_split_noalloc");
-    pack_split_kernel<2><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, kfast, ex, dst);
-    JUES_CHECK_CUDA(cudaGetLastError());
+    launch_pack<2>(ctx, src, rm, km, R, K, Rpad, Kpad, ex, dst);
 }
 }  // namespace
 
