@@ -166,6 +166,17 @@ __device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
 }
 __device__ __forceinline__ float lo_f(uint64_t x) { return __uint_as_float((uint32_t)x); }
 __device__ __forceinline__ float hi_f(uint64_t x) { return __uint_as_float((uint32_t)(x >> 32)); }
+// FP32 -> FP64 on the integer pipes (exact: the exponent is rebiased, the significand shifted);
+// subnormal, infinite and NaN inputs take the conversion instruction
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xFFu;
+    if ((e == 0u && (u << 1) != 0u) || e == 0xFFu) return (double)f;
+    const uint32_t hi = (u & 0x80000000u) | (e == 0u ? 0u : ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3));
+    return __hiloint2double((int)hi, (int)(e == 0u ? 0u : u << 29));
+}
+__device__ __forceinline__ void red_add_f64(double *p, double v) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
 
 // UMMA shared-memory descriptor of a K-major tile written by TMA with 128-byte swizzle:
 // start address >> 4, LBO unused (1), SBO = 1024 bytes between 8-row groups, version 1,
@@ -182,6 +193,11 @@ struct TcArgs {
     const int *expA, *expB;   // per-(chunk,row) power-of-two scales, [chunk][row]
     long long expA_ld, expB_ld;   // padded row counts (chunk strides)
     double alpha, beta;
+    // Epilogue arithmetic without the FP64 pipe (about two operations per clock per SM on
+    // GB300): alpha = (-1)^alpha_neg 2^alpha_k is folded into the FP32 row scale when
+    // alpha_pow2; beta_mode 0: C = alpha AB; 1: C += alpha AB in place (Cin == C, beta == 1),
+    // added by the L2's FP64 reduction unit; 2: C = Cin + alpha AB; 3: C = beta Cin + alpha AB.
+    int alpha_pow2, alpha_k, alpha_neg, beta_mode;
     double *C;
     const double *Cin;
     Mode mC, nC;
@@ -452,8 +468,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const int ea = ea_cur;
                 ea_cur = ea_next;
                 eb_cur = eb_next;
-                // row factor 2^(e_row - 18); the column factor comes from shared memory
-                const float rs = (ea == INT_MIN || ea - 18 < -126) ? 0.f : __int_as_float((ea - 18 + 127) << 23);
+                // row factor 2^(e_row - 18) (times alpha when that is a power of two); the column
+                // factor comes from shared memory
+                const int er = ea - 18 + g.alpha_k;
+                const float rs = (ea == INT_MIN || er < -126)
+                                     ? 0.f
+                                     : __int_as_float((er + 127) << 23 | (g.alpha_neg ? 0x80000000 : 0));
                 const float2 *cs = reinterpret_cast<const float2 *>(colsc + buf * BN + half * HB);
                 const uint64_t rs2 = pk2f(rs, rs), k2 = pk2f(0.0009765625f, 0.0009765625f);
                 // 32 columns per round: the NP accumulator loads in flight, one wait; then per
@@ -498,26 +518,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             } else if (mrow < g.M) {
                 const long long rowoff = mode_off(g.mC, mrow);
                 const long long *co = coloff + half * HB;
-                // Each output element is read and written by this thread alone, so a batch's
-                // inputs are all loaded before any of its outputs is stored: the loads are in
-                // flight together instead of one load latency per column (C and Cin may alias).
-                constexpr int EB = HB < 32 ? HB : 32;
+                double *out = g.C + rowoff;
+                auto value = [&](int j) {
+                    const double v = f32_to_f64((j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]));
+                    return g.alpha_pow2 ? v : g.alpha * v;
+                };
+                if (g.beta_mode <= 1) {
+                    // no input to read: plain stores, or in-place FP64 adds done in L2 (one owner
+                    // per element, so the sums are deterministic; round-to-nearest like the
+                    // FP64 add they replace)
 #pragma unroll
-                for (int j0 = 0; j0 < HB; j0 += EB) {
-                    double cin[EB];
-#pragma unroll
-                    for (int j = 0; j < EB; ++j) {
-                        const long long c = co[j0 + j];
-                        cin[j] = (g.beta != 0.0 && c >= 0) ? __ldcs(g.Cin + rowoff + c) : 0.0;
-                    }
-#pragma unroll
-                    for (int j = 0; j < EB; ++j) {
-                        const long long c = co[j0 + j];
-                        const int jj = j0 + j;
+                    for (int j = 0; j < HB; ++j) {
+                        const long long c = co[j];
                         if (c >= 0) {
-                            double val = g.alpha * (double)((jj & 1) ? hi_f(acc2[jj >> 1]) : lo_f(acc2[jj >> 1]));
-                            if (g.beta != 0.0) val = fma(g.beta, cin[j], val);
-                            g.C[rowoff + c] = val;
+                            if (g.beta_mode == 1)
+                                red_add_f64(out + c, value(j));
+                            else
+                                out[c] = value(j);
+                        }
+                    }
+                } else {
+                    // Each output element is read and written by this thread alone, so a batch's
+                    // inputs are all loaded before any of its outputs is stored: the loads are in
+                    // flight together instead of one load latency per column (C and Cin may alias).
+                    const double *in = g.Cin + rowoff;
+                    constexpr int EB = HB < 16 ? HB : 16;
+#pragma unroll
+                    for (int j0 = 0; j0 < HB; j0 += EB) {
+                        double cin[EB];
+#pragma unroll
+                        for (int j = 0; j < EB; ++j) {
+                            const long long c = co[j0 + j];
+                            cin[j] = c >= 0 ? __ldcs(in + c) : 0.0;
+                        }
+#pragma unroll
+                        for (int j = 0; j < EB; ++j) {
+                            const long long c = co[j0 + j];
+                            if (c >= 0)
+                                out[c] = g.beta_mode == 2 ? cin[j] + value(j0 + j) : fma(g.beta, cin[j], value(j0 + j));
                         }
                     }
                 }
@@ -887,6 +925,14 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
         g.kper = g.kblocks;
         g.partial = nullptr;
     }
+    // alpha = +-2^k, |k| <= 8, is folded into the FP32 row scale, which
+    // changes only the exponent (exact); the raw split-K partials never take it
+    int ak = 0;
+    const double am = std::frexp(std::fabs(g.alpha), &ak);
+    g.alpha_pow2 = (!g.partial && am == 0.5 && ak - 1 >= -8 && ak - 1 <= 8) ? 1 : 0;
+    g.alpha_k = g.alpha_pow2 ? ak - 1 : 0;
+    g.alpha_neg = (g.alpha_pow2 && g.alpha < 0) ? 1 : 0;
+    g.beta_mode = g.beta == 0.0 ? 0 : (g.beta == 1.0 ? (g.Cin == g.C ? 1 : 2) : 3);
     const long long items = tiles * g.ksplit;
     JUES_REQUIRE(items < (1LL << 31), "too many output tiles");
     // persistent: one CTA per SM (the stage ring takes most of shared memory)

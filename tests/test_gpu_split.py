@@ -79,6 +79,22 @@ def test_gemm_fp64(lib, M, N, K, ta, tb):
     assert np.allclose(got, want, rtol=1e-12, atol=1e-11 * np.sqrt(K))
 
 
+def test_gemm_split_epilogue_forms(lib):
+    """The epilogue's forms against the plain product P = gemm(A, B): alpha a power of two is
+    folded into the FP32 scale (exact), other alphas multiply in FP64, beta = 1 adds in place
+    (in L2), other betas read C.  All but the general beta are bit-exact images of P."""
+    rng = np.random.default_rng(11)
+    A = rng.normal(size=(1000, 129))
+    B = rng.normal(size=(129, 257))
+    C0 = rng.normal(size=(1000, 257))
+    P = lib.gemm(A, B, precision="split_bf16")
+    for alpha in (1.0, -0.5, 4.0, 0.7):
+        assert np.array_equal(lib.gemm(A, B, alpha=alpha, precision="split_bf16"), alpha * P)
+        assert np.array_equal(lib.gemm(A, B, C0, alpha=alpha, beta=1.0, precision="split_bf16"), C0 + alpha * P)
+        got = lib.gemm(A, B, C0, alpha=alpha, beta=-1.3, precision="split_bf16")
+        assert np.abs(got - (alpha * P - 1.3 * C0)).max() < 1e-14 * np.abs(got).max()
+
+
 @pytest.mark.parametrize("M,N,K,ta,tb", SHAPES)
 def test_gemm_split_bf16(lib, M, N, K, ta, tb):
     rng = np.random.default_rng(7 * M + N + K)
