@@ -166,14 +166,36 @@ __device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
 }
 __device__ __forceinline__ float lo_f(uint64_t x) { return __uint_as_float((uint32_t)x); }
 __device__ __forceinline__ float hi_f(uint64_t x) { return __uint_as_float((uint32_t)(x >> 32)); }
-// FP32 -> FP64 on the integer pipes (exact: the exponent is rebiased, the significand shifted);
-// subnormal, infinite and NaN inputs take the conversion instruction
+// FP32 -> FP64 on the integer pipes, exact for every input (GB300's FP64 pipe, conversions
+// included, runs at about two operations per clock per SM): the exponent is rebiased and the
+// significand shifted; subnormals are normalised with a leading-zero count
 __device__ __forceinline__ double f32_to_f64(float f) {
-    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xFFu;
-    if ((e == 0u && (u << 1) != 0u) || e == 0xFFu) return (double)f;
-    const uint32_t hi = (u & 0x80000000u) | (e == 0u ? 0u : ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3));
-    return __hiloint2double((int)hi, (int)(e == 0u ? 0u : u << 29));
+    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu, s = u & 0x80000000u;
+    uint32_t hi, lo;
+    if (e - 1u < 254u) {          // normal
+        hi = s | ((e + 896u) << 20) | (m >> 3);
+        lo = m << 29;
+    } else if (e == 0xFFu) {      // infinity, NaN
+        hi = s | 0x7FF00000u | (m >> 3);
+        lo = m << 29;
+    } else if (m == 0u) {         // zero
+        hi = s;
+        lo = 0u;
+    } else {                      // subnormal m 2^-149, leading bit at position b
+        const int b = 31 - __clz((int)m);
+        const uint64_t mant = ((uint64_t)m << (52 - b)) & 0xFFFFFFFFFFFFFull;
+        hi = s | ((uint32_t)(b + 874) << 20) | (uint32_t)(mant >> 32);
+        lo = (uint32_t)mant;
+    }
+    return __hiloint2double((int)hi, (int)lo);
 }
+// FP32 -> FP64 for a normal number or zero (the exponent rebiased by 1023 - 127 = 896)
+__device__ __forceinline__ double f32_to_f64_normal(float f) {
+    const uint32_t u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+    const uint32_t hi = (a == 0u ? 0u : (a >> 3) + (896u << 20)) | (u & 0x80000000u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 __device__ __forceinline__ void red_add_f64(double *p, double v) {
     asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
@@ -253,8 +275,14 @@ __device__ __forceinline__ TcItem tc_item(const TcArgs &g, long long w, int BN) 
     TcItem I;
     const long long tile = w % g.tiles;
     I.split = w / g.tiles;
-    I.m0 = (int)((tile % g.mtiles) * TBM);
-    I.n0 = (int)((tile / g.mtiles) * BN);
+    // raster: groups of (up to) 16 row tiles, rows fastest within a group, so the CTAs resident
+    // at one time reuse a few row tiles' operand rows from L2 across about ten column tiles
+    const long long G = min(g.mtiles, 16LL);
+    const long long span = G * (g.tiles / g.mtiles);
+    const long long grp = tile / span, in = tile - grp * span;
+    const long long gm = min(G, g.mtiles - grp * G);
+    I.m0 = (int)((grp * G + in % gm) * TBM);
+    I.n0 = (int)((in / gm) * BN);
     I.kb0 = (int)I.split * g.kper;
     I.nk = min(g.kblocks - I.kb0, g.kper);
     return I;
@@ -274,6 +302,74 @@ __device__ __forceinline__ bool drain_bar_any(bool pred) {
         : "memory");
     return r != 0;
 }
+
+// Column offsets of a thread's half tile: read from shared memory (any output mode), or
+// computed for a single-stride column mode
+struct ColsShared {
+    const long long *co;
+    __device__ __forceinline__ long long operator()(int j) const { return co[j]; }
+};
+struct ColsStrided {
+    long long base, step;
+    int nvalid;
+    __device__ __forceinline__ long long operator()(int j) const { return j < nvalid ? base + j * step : -1; }
+};
+
+// One thread's row of an output tile: HB FP32 sums (column pairs packed in acc2) scaled and
+// scattered through the output modes (co(j): column offsets, -1 past N).  Each form is its own
+// loop, so no FP64 instruction is issued that the form does not need: POW2 (alpha folded into
+// the FP32 scale) converts and stores only.  The conversion takes the short normal-or-zero
+// form, and branches off for subnormal, infinite and NaN sums.
+template <int HB, bool POW2, class Cols>
+__device__ __forceinline__ void tc_epilogue(const TcArgs &g, const uint64_t *acc2, const Cols co, long long rowoff) {
+    double *out = g.C + rowoff;
+    auto value = [&](int j) {
+        const float f = (j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]);
+        const uint32_t a = __float_as_uint(f) & 0x7FFFFFFFu;
+        double v;
+        if (__builtin_expect((a - 1u < 0x7FFFFFu) | (a > 0x7F7FFFFFu), 0))
+            v = f32_to_f64(f);   // subnormal, infinite or NaN
+        else
+            v = f32_to_f64_normal(f);
+        if constexpr (POW2)
+            return v;
+        else
+            return g.alpha * v;
+    };
+    if (g.beta_mode == 0) {
+#pragma unroll
+        for (int j = 0; j < HB; ++j)
+            if (co(j) >= 0) out[co(j)] = value(j);
+    } else if (g.beta_mode == 1) {
+        // in-place sums as L2 reductions: one owner per element, so they are deterministic,
+        // and round-to-nearest like the FP64 add they replace
+#pragma unroll
+        for (int j = 0; j < HB; ++j)
+            if (co(j) >= 0) red_add_f64(out + co(j), value(j));
+    } else {
+        // Each output element is read and written by this thread alone, so a batch's inputs are
+        // all loaded before any of its outputs is stored: the loads are in flight together
+        // instead of one load latency per column (C and Cin may alias).
+        const double *in = g.Cin + rowoff;
+        constexpr int EB = HB < 16 ? HB : 16;
+#pragma unroll
+        for (int j0 = 0; j0 < HB; j0 += EB) {
+            double cin[EB];
+#pragma unroll
+            for (int j = 0; j < EB; ++j) cin[j] = co(j0 + j) >= 0 ? __ldcs(in + co(j0 + j)) : 0.0;
+            if (g.beta_mode == 2) {
+#pragma unroll
+                for (int j = 0; j < EB; ++j)
+                    if (co(j0 + j) >= 0) out[co(j0 + j)] = cin[j] + value(j0 + j);
+            } else {
+#pragma unroll
+                for (int j = 0; j < EB; ++j)
+                    if (co(j0 + j) >= 0) out[co(j0 + j)] = fma(g.beta, cin[j], value(j0 + j));
+            }
+        }
+    }
+}
+
 
 template <int BN, int STAGES, int KC, int NP>
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -517,47 +613,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             } else if (mrow < g.M) {
                 const long long rowoff = mode_off(g.mC, mrow);
-                const long long *co = coloff + half * HB;
-                double *out = g.C + rowoff;
-                auto value = [&](int j) {
-                    const double v = f32_to_f64((j & 1) ? hi_f(acc2[j >> 1]) : lo_f(acc2[j >> 1]));
-                    return g.alpha_pow2 ? v : g.alpha * v;
-                };
-                if (g.beta_mode <= 1) {
-                    // no input to read: plain stores, or in-place FP64 adds done in L2 (one owner
-                    // per element, so the sums are deterministic; round-to-nearest like the
-                    // FP64 add they replace)
-#pragma unroll
-                    for (int j = 0; j < HB; ++j) {
-                        const long long c = co[j];
-                        if (c >= 0) {
-                            if (g.beta_mode == 1)
-                                red_add_f64(out + c, value(j));
-                            else
-                                out[c] = value(j);
-                        }
-                    }
+                const long long n1 = (long long)I.n0 + half * HB;
+                if (g.nC.d0 == MODE_BIG) {
+                    const ColsStrided cols{n1 * g.nC.s0, g.nC.s0, (int)max(-1LL, min((long long)HB, g.N - n1))};
+                    if (g.alpha_pow2)
+                        tc_epilogue<HB, true>(g, acc2, cols, rowoff);
+                    else
+                        tc_epilogue<HB, false>(g, acc2, cols, rowoff);
                 } else {
-                    // Each output element is read and written by this thread alone, so a batch's
-                    // inputs are all loaded before any of its outputs is stored: the loads are in
-                    // flight together instead of one load latency per column (C and Cin may alias).
-                    const double *in = g.Cin + rowoff;
-                    constexpr int EB = HB < 16 ? HB : 16;
-#pragma unroll
-                    for (int j0 = 0; j0 < HB; j0 += EB) {
-                        double cin[EB];
-#pragma unroll
-                        for (int j = 0; j < EB; ++j) {
-                            const long long c = co[j0 + j];
-                            cin[j] = c >= 0 ? __ldcs(in + c) : 0.0;
-                        }
-#pragma unroll
-                        for (int j = 0; j < EB; ++j) {
-                            const long long c = co[j0 + j];
-                            if (c >= 0)
-                                out[c] = g.beta_mode == 2 ? cin[j] + value(j0 + j) : fma(g.beta, cin[j], value(j0 + j));
-                        }
-                    }
+                    const ColsShared cols{coloff + half * HB};
+                    if (g.alpha_pow2)
+                        tc_epilogue<HB, true>(g, acc2, cols, rowoff);
+                    else
+                        tc_epilogue<HB, false>(g, acc2, cols, rowoff);
                 }
             }
         }
@@ -942,19 +1010,19 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
-// Number of K splits for a tile grid that underfills the GPU: the wave count times the stages
-// per split (plus a fixed per-CTA start-up of about five stages) is minimised over splits of
-// at least four stages, and taken when it saves at least 10%.  Grids of two waves or more are
-// left whole.
-static int choose_ksplit(long long tiles, int kblocks) {
+// Number of K splits: the wave count times the stages per split (plus a fixed per-CTA start-up
+// of about five stages) is minimised over splits of at least four stages, and taken when it
+// saves at least 10%: grids below two waves, and grids whose last wave is mostly empty (2.1
+// waves run as 3), gain; full grids do not.  The FP32 partial sums are kept under 1 GB.
+static int choose_ksplit(long long tiles, int kblocks, long long tile_elems) {
     constexpr long long kSms = 152;
-    if (tiles >= 2 * kSms || kblocks < 8) return 1;
+    if (kblocks < 8) return 1;
     auto cost = [&](int ks) {
         const long long waves = (tiles * ks + kSms - 1) / kSms;
         return (double)waves * ((kblocks + ks - 1) / ks + 5);
     };
     int best = 1;
-    for (int ks = 2; ks <= 256 && ks * 4 <= kblocks; ++ks)
+    for (int ks = 2; ks <= 256 && ks * 4 <= kblocks && (long long)ks * tiles * tile_elems * 4 <= (1LL << 30); ++ks)
         if (cost(ks) < cost(best)) best = ks;
     return cost(best) <= 0.9 * cost(1) ? best : 1;
 }
@@ -991,12 +1059,13 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name, int np) {
         gett_f64(ctx, a0, name);
         return;
     }
-    // tile width: smallest padded N, preferring wider tiles on ties
+    // tile width: least padded N, a 64-wide tile weighted 1.2 (per product it moves 1.5x the
+    // operand bytes of a 128-wide one, and its MMAs are half as wide), wider on ties
     int BN = widths[0];
     {
-        long long best = -1;
+        double best = -1;
         for (int cand : widths) {
-            long long p = roundup(a.N, cand);
+            const double p = (double)roundup(a.N, cand) * (cand == 64 && widths.size() > 1 ? 1.2 : 1.0);
             if (best < 0 || p < best) { best = p; BN = cand; }
         }
     }
@@ -1025,7 +1094,7 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name, int np) {
     t.expB_ld = Npad;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
-    const int ks0 = choose_ksplit(tiles, t.kblocks);
+    const int ks0 = choose_ksplit(tiles, t.kblocks, (long long)TBM * BN);
     if (ks0 > 1) {
         t.kper = (t.kblocks + ks0 - 1) / ks0;
         t.kper = (t.kper + TC_KC - 1) / TC_KC * TC_KC;
