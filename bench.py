@@ -424,7 +424,9 @@ def run_gpu(args):
             e2e_kernels = {k: ctx.profile(k)[0] for k in ("", "transform", "pack_split", "ccd_")}
             e2e_host = {k: ctx.profile("host:" + k)[0] for k in ("h2d_ao_eri", "cc_create", "integral_blocks",
                                                                  "release_ao_eri")}
-            e2e_kernels[""] -= ctx.profile("host:")[0]   # kernel events only
+            # page-locking inside the AO-integral copy (part of h2d_ao_eri)
+            e2e_host.update({"h2d_" + k: ctx.profile("h2d:" + k)[0] for k in ("register", "unregister")})
+            e2e_kernels[""] -= ctx.profile("host:")[0] + ctx.profile("h2d:")[0]   # kernel events only
             e2e_host["register_failures"] = ctx.profile("host:register_failed")[1]
             ctx.set_profiling(False)
             runs.append((t_e2e, len(lg), e2e_kernels, e2e_host))

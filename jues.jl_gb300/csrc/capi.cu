@@ -1,6 +1,7 @@
 // extern "C" entry points of libjuesgpu.so (declared in include/jues_gpu.h).
 #include <algorithm>
 #include <cstdlib>
+#include <chrono>
 #include <cstring>
 #include <string>
 
@@ -54,27 +55,84 @@ static const double *ao_operand(Ctx &c, const double *gao, size_t n4, int prec, 
 // Host -> device copy of a caller's array.  Large pageable arrays are registered (page-locked)
 // for the duration of the copy: the DMA engines then read them directly at link speed, where an
 // unregistered copy is staged through the driver's bounce buffers (measured on GB300 with Grace:
-// ~200 GB/s against ~6 GB/s for the 12.8 GB AO integrals at nbf=200; registering 12.8 GB costs
-// tens of milliseconds).
-DBuf<double> h2d(Ctx &ctx, const double *h, size_t n) {
-    DBuf<double> d(&ctx, n);
-    if (!n) return d;
-    const size_t bytes = n * sizeof(double);
-    bool registered = false;
-    if (bytes >= (size_t(64) << 20)) {
-        const cudaError_t e = cudaHostRegister(const_cast<double *>(h), bytes, cudaHostRegisterDefault);
+// ~200 GB/s against ~6 GB/s for the 12.8 GB AO integrals at nbf=200).  Registration costs tens
+// to hundreds of milliseconds for 12.8 GB, varying with the host's page state, so the array goes
+// in 512 MB pieces: the next piece is registered while the link copies this one, and each piece
+// is released once its copy has finished.
+namespace {
+struct H2DPieces {
+    struct Piece {
+        uintptr_t a, b;
+        bool reg = false;
+        cudaEvent_t done = nullptr;
+    };
+    Ctx &ctx;
+    std::vector<Piece> ps;
+    double reg_ms = 0.0, unreg_ms = 0.0;
+    explicit H2DPieces(Ctx &c) : ctx(c) {}
+    static double now_ms() {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+    }
+    void reg(Piece &p) {
+        const double t = now_ms();
+        const cudaError_t e = cudaHostRegister(reinterpret_cast<void *>(p.a), p.b - p.a, cudaHostRegisterDefault);
+        reg_ms += now_ms() - t;
         if (e == cudaSuccess) {
-            registered = true;
+            p.reg = true;
         } else {
             cudaGetLastError();   // already page-locked by the caller, or not registrable: plain copy
             if (ctx.profiling) ctx.prof["host:register_failed_" + std::to_string((int)e)].launches += 1;
         }
     }
-    JUES_CHECK_CUDA(cudaMemcpyAsync(d.p, h, bytes, cudaMemcpyHostToDevice, ctx.stream));
-    if (registered) {
-        JUES_CHECK_CUDA(cudaStreamSynchronize(ctx.stream));
-        cudaHostUnregister(const_cast<double *>(h));
+    void release(Piece &p) {
+        if (p.done) cudaEventSynchronize(p.done);
+        if (p.reg) {
+            const double t = now_ms();
+            cudaHostUnregister(reinterpret_cast<void *>(p.a));
+            unreg_ms += now_ms() - t;
+            p.reg = false;
+        }
     }
+    ~H2DPieces() {   // also on an error path: no range stays registered, no event leaks
+        for (Piece &p : ps) {
+            release(p);
+            if (p.done) cudaEventDestroy(p.done);
+        }
+        if (ctx.profiling) {
+            ctx.prof["h2d:register"].total_ms += reg_ms;
+            ctx.prof["h2d:unregister"].total_ms += unreg_ms;
+        }
+    }
+};
+}  // namespace
+
+DBuf<double> h2d(Ctx &ctx, const double *h, size_t n) {
+    DBuf<double> d(&ctx, n);
+    if (!n) return d;
+    const size_t bytes = n * sizeof(double);
+    if (bytes < (size_t(64) << 20)) {
+        JUES_CHECK_CUDA(cudaMemcpyAsync(d.p, h, bytes, cudaMemcpyHostToDevice, ctx.stream));
+        return d;
+    }
+    constexpr uintptr_t kPiece = uintptr_t(512) << 20, kAlign = uintptr_t(2) << 20;
+    const uintptr_t b0 = reinterpret_cast<uintptr_t>(h), b1 = b0 + bytes;
+    H2DPieces pc(ctx);
+    // interior cuts on 2 MB host addresses: no two pieces share a page
+    for (uintptr_t a = b0, c = (b0 + kPiece) / kAlign * kAlign; a < b1; a = c, c += kPiece) {
+        const uintptr_t e = c < b1 ? c : b1;
+        pc.ps.push_back({a, e});
+    }
+    for (auto &p : pc.ps) JUES_CHECK_CUDA(cudaEventCreateWithFlags(&p.done, cudaEventDisableTiming));
+    pc.reg(pc.ps[0]);
+    for (size_t i = 0; i < pc.ps.size(); ++i) {
+        H2DPieces::Piece &p = pc.ps[i];
+        JUES_CHECK_CUDA(cudaMemcpyAsync(d.p + (p.a - b0) / sizeof(double), reinterpret_cast<const void *>(p.a),
+                                        p.b - p.a, cudaMemcpyHostToDevice, ctx.stream));
+        JUES_CHECK_CUDA(cudaEventRecord(p.done, ctx.stream));
+        if (i + 1 < pc.ps.size()) pc.reg(pc.ps[i + 1]);
+        if (i >= 1) pc.release(pc.ps[i - 1]);
+    }
+    pc.release(pc.ps.back());
     return d;
 }
 

@@ -189,12 +189,16 @@ static void diis_step(CCState *s, double *x, const double *xn, size_t len) {
         s->dv[slot] = DBuf<double>(ctx, len);
         s->de[slot] = DBuf<double>(ctx, len);
     }
-    d2d(ctx, s->dv[slot].p, xn, len);
-    axpby(ctx, len, 1.0, xn, -1.0, x, s->de[slot].p);
+    // the new pair and its overlaps with the stored errors, in one pass
+    const int m = (int)s->dorder.size() + 1;
+    std::vector<const double *> olds(m - 1);
+    for (int k = 0; k < m - 1; ++k) olds[k] = s->de[s->dorder[k]].p;
+    std::vector<double> dots(m);
+    diis_error(ctx, len, xn, x, s->dv[slot].p, s->de[slot].p, m - 1, olds.data(), dots.data());
     s->dorder.push_back(slot);
-    const int m = (int)s->dorder.size();
     std::vector<double> row(m);
-    for (int k = 0; k < m; ++k) row[k] = dot(ctx, len, s->de[s->dorder[k]].p, s->de[slot].p);
+    for (int k = 0; k < m - 1; ++k) row[k] = dots[1 + k];
+    row[m - 1] = dots[0];
     for (int k = 0; k < m - 1; ++k) s->gram[k].push_back(row[k]);
     s->gram.push_back(row);
     double mx = 0.0;

@@ -260,6 +260,9 @@ void divide_by_d(Ctx *ctx, const double *in, const double *eps, int o, int v, do
 void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out);
 // sum_k c_k * vecs[k] -> out (length n)
 void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out);
+// DIIS bookkeeping in one pass: v_out = xn, e_out = xn - x, dots[0] = e.e, dots[1 + k] = olds[k].e
+void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
+                const double *const *olds, double *dots);
 // 1 if any element of x is NaN/Inf
 bool any_nonfinite(Ctx *ctx, const double *x, size_t n);
 

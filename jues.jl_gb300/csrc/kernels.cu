@@ -220,6 +220,40 @@ __global__ void lincomb_kernel(size_t n, int m, VecList vl, double *__restrict__
     }
 }
 
+// DIIS bookkeeping of one sweep in one pass: v = xn, e = xn - x, and the dots e.e and old_k.e
+// (the same grid, products and summation order as dot_kernel, so the sums are identical)
+__global__ void diis_error_kernel(size_t n, const double *__restrict__ xn, const double *__restrict__ x,
+                                  double *__restrict__ v_out, double *__restrict__ e_out, int nold, VecList olds,
+                                  double *part) {
+    double acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double xv = xn[i];
+        const double e = xv - x[i];
+        v_out[i] = xv;
+        e_out[i] = e;
+        acc[0] = fma(e, e, acc[0]);
+#pragma unroll
+        for (int k = 0; k < 15; ++k)
+            if (k < nold) acc[k + 1] = fma(olds.p[k][i], e, acc[k + 1]);
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        if (k > nold) break;
+        const double v = block_sum(acc[k]);
+        if (threadIdx.x == 0) part[(size_t)k * gridDim.x + blockIdx.x] = v;
+    }
+}
+
+// out[b] = sum of row b of part (rows of n), in reduce_partials' order
+__global__ void reduce_rows(const double *part, int n, double *out) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[(size_t)blockIdx.x * n + i];
+    v = block_sum(v);
+    if (threadIdx.x == 0) out[blockIdx.x] = v;
+}
+
 __global__ void t1_finalize_kernel(double *__restrict__ t1n, const double *__restrict__ eps, int o, int v,
                                    const double *__restrict__ t1old, double *part) {
     double acc = 0.0;
@@ -407,6 +441,24 @@ void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out) {
     Ctx::Scope s(ctx, "t_tilde");
     t_tilde_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(T, o, v, out);
     JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
+                const double *const *olds, double *dots) {
+    JUES_REQUIRE(nold >= 0 && nold <= 15, "diis_error supports up to 15 stored errors");
+    VecList vl;
+    for (int k = 0; k < nold; ++k) { vl.p[k] = olds[k]; vl.c[k] = 0.0; }
+    {
+        Ctx::Scope s(ctx, "diis_error");
+        diis_error_kernel<<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, xn, x, v_out, e_out, nold, vl, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    double *out = ctx->d_red + 65536 - 48;   // (nold + 1) <= 16 sums, clear of finish_reduce's slot
+    reduce_rows<<<nold + 1, 1024, 0, ctx->stream>>>(ctx->d_red, RED_BLOCKS, out);
+    ctx->count_launch();
+    JUES_CHECK_CUDA(cudaGetLastError());
+    JUES_CHECK_CUDA(cudaMemcpyAsync(dots, out, (nold + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    JUES_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out) {
