@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "staging.cuh"
 #include "gett_f64.cuh"
 #include "transform.cuh"
 
@@ -297,21 +298,16 @@ void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, do
     JUES_CHECK_CUDA(cudaEventCreate(&t3));
     JUES_CHECK_CUDA(cudaEventRecord(t0, ctx->stream));
     double *A = bp.arena.p;
-    HostPins pins;   // the systems' AO arrays and adjoint outputs, page-locked for this call
+    // the systems' inputs through the staging ring (no page-locking of the caller's arrays)
+    std::vector<HostSeg> ups;
+    ups.reserve(3 * (size_t)nsys);
     for (int s = 0; s < nsys; ++s) {
         const size_t n = (size_t)sys[s].n;
-        pins.pin(sys[s].gao, n * n * n * n * sizeof(double));
-        if (want_gb && gao_bar && gao_bar[s]) pins.pin(gao_bar[s], n * n * n * n * sizeof(double));
+        ups.push_back({A + bp.off_g[s], sys[s].gao, n * n * n * n * sizeof(double)});
+        ups.push_back({A + bp.off_C[s], sys[s].C, n * n * sizeof(double)});
+        ups.push_back({A + bp.off_eps[s], sys[s].eps, n * sizeof(double)});
     }
-    for (int s = 0; s < nsys; ++s) {
-        const size_t n = (size_t)sys[s].n;
-        JUES_CHECK_CUDA(cudaMemcpyAsync(A + bp.off_g[s], sys[s].gao, n * n * n * n * sizeof(double),
-                                        cudaMemcpyHostToDevice, ctx->stream));
-        JUES_CHECK_CUDA(cudaMemcpyAsync(A + bp.off_C[s], sys[s].C, n * n * sizeof(double), cudaMemcpyHostToDevice,
-                                        ctx->stream));
-        JUES_CHECK_CUDA(cudaMemcpyAsync(A + bp.off_eps[s], sys[s].eps, n * sizeof(double), cudaMemcpyHostToDevice,
-                                        ctx->stream));
-    }
+    staged_h2d(ctx, ups);
     JUES_CHECK_CUDA(cudaEventRecord(t1, ctx->stream));
     if (fresh) {
         autotune(ctx, bp);   // runs every stage once on the uploaded data
@@ -337,15 +333,13 @@ void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, do
     ctx->launches += (long long)bp.graph_nodes;
     JUES_CHECK_CUDA(cudaEventRecord(t2, ctx->stream));
     JUES_CHECK_CUDA(cudaMemcpyAsync(e_out, bp.energies.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<HostSeg> down;
     for (int s = 0; s < nsys; ++s) {
         const size_t n = (size_t)sys[s].n;
-        if (want_gb && gao_bar[s])
-            JUES_CHECK_CUDA(cudaMemcpyAsync(gao_bar[s], A + bp.off_gb[s], n * n * n * n * sizeof(double),
-                                            cudaMemcpyDeviceToHost, ctx->stream));
-        if (want_cb && C_bar[s])
-            JUES_CHECK_CUDA(cudaMemcpyAsync(C_bar[s], A + bp.off_cb[s], n * n * sizeof(double),
-                                            cudaMemcpyDeviceToHost, ctx->stream));
+        if (want_gb && gao_bar[s]) down.push_back({gao_bar[s], A + bp.off_gb[s], n * n * n * n * sizeof(double)});
+        if (want_cb && C_bar[s]) down.push_back({C_bar[s], A + bp.off_cb[s], n * n * sizeof(double)});
     }
+    staged_d2h(ctx, down);   // returns with the data in the caller's arrays
     JUES_CHECK_CUDA(cudaEventRecord(t3, ctx->stream));
     JUES_CHECK_CUDA(cudaEventSynchronize(t3));
     float up = 0.f, gr = 0.f, dn = 0.f;

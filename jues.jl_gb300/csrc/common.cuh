@@ -88,6 +88,7 @@ struct ProfRec {
 
 struct PackCache;  // split-precision operand cache (gett_tc.cu)
 struct BatchCache;  // batched MP2 plans and graphs (batch.cu)
+struct Staging;     // page-locked staging ring and copy threads (staging.cu)
 
 struct Ctx {
     int device = 0;
@@ -101,6 +102,7 @@ struct Ctx {
     double *d_red = nullptr;           // reduction scratch (1 << 16 doubles)
     PackCache *pack = nullptr;         // owned; destroyed by pack_cache_destroy
     BatchCache *batch = nullptr;       // owned; destroyed by batch_cache_destroy
+    Staging *staging = nullptr;        // owned; destroyed by staging_destroy
     void *splitk_ws = nullptr;         // split-K partial sums, grown on demand
     size_t splitk_bytes = 0;
     cudaMemPool_t pool = nullptr;      // stream-ordered pool behind alloc/free (keeps freed memory)
@@ -135,19 +137,6 @@ struct Ctx {
         ~HostPhase();
     };
     void check_flags();   // reads d_flags after a sync; throws on a set flag
-};
-
-// Page-locks caller-owned host ranges for the copies of one call and releases them at scope
-// exit (after the caller has synchronised).  A pageable copy is staged through the driver's
-// bounce buffers at a few GB/s; a registered one runs at link speed.  Ranges below min_bytes,
-// and ranges that cannot be registered (e.g. already page-locked), are copied as they are.
-struct HostPins {
-    std::vector<void *> regs;
-    void pin(const void *p, size_t bytes, size_t min_bytes = size_t(4) << 20);
-    HostPins() = default;
-    HostPins(const HostPins &) = delete;
-    HostPins &operator=(const HostPins &) = delete;
-    ~HostPins();
 };
 
 // device buffer owned by a context

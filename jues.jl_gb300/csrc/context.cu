@@ -8,6 +8,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "staging.cuh"
 
 namespace jues {
 
@@ -24,6 +25,8 @@ Ctx::~Ctx() {
     pack_cache_destroy(pk);
     batch_cache_destroy(batch);
     batch = nullptr;
+    staging_destroy(staging);
+    staging = nullptr;
     for (auto &kv : prof) {
         for (auto &e : kv.second.pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto &e : kv.second.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -75,18 +78,6 @@ void *Ctx::alloc(size_t bytes) {
     }
     mem_used += bytes;
     return p;
-}
-
-void HostPins::pin(const void *p, size_t bytes, size_t min_bytes) {
-    if (!p || bytes < min_bytes) return;
-    if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterDefault) == cudaSuccess)
-        regs.push_back(const_cast<void *>(p));
-    else
-        cudaGetLastError();
-}
-
-HostPins::~HostPins() {
-    for (void *p : regs) cudaHostUnregister(p);
 }
 
 void Ctx::free(void *p, size_t bytes) {
