@@ -220,27 +220,35 @@ __global__ void lincomb_kernel(size_t n, int m, VecList vl, double *__restrict__
     }
 }
 
-// DIIS bookkeeping of one sweep in one pass: v = xn, e = xn - x, and the dots e.e and old_k.e
-// (the same grid, products and summation order as dot_kernel, so the sums are identical)
-__global__ void diis_error_kernel(size_t n, const double *__restrict__ xn, const double *__restrict__ x,
-                                  double *__restrict__ v_out, double *__restrict__ e_out, int nold, VecList olds,
-                                  double *part) {
-    double acc[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) acc[k] = 0.0;
+// DIIS bookkeeping of one sweep, pass 1: v = xn, e = xn - x and e.e (the same grid, products and
+// summation order as dot_kernel, so the sum is identical)
+__global__ void diis_pair_kernel(size_t n, const double *__restrict__ xn, const double *__restrict__ x,
+                                 double *__restrict__ v_out, double *__restrict__ e_out, double *part) {
+    double acc = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const double xv = xn[i];
         const double e = xv - x[i];
         v_out[i] = xv;
         e_out[i] = e;
-        acc[0] = fma(e, e, acc[0]);
+        acc = fma(e, e, acc);
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// pass 2: old_k . e for the NOLD stored errors, e read once (loads only, no stores)
+template <int NOLD>
+__global__ void multi_dot_kernel(size_t n, VecList olds, const double *__restrict__ e, double *part) {
+    double acc[NOLD];
 #pragma unroll
-        for (int k = 0; k < 15; ++k)
-            if (k < nold) acc[k + 1] = fma(olds.p[k][i], e, acc[k + 1]);
+    for (int k = 0; k < NOLD; ++k) acc[k] = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double ei = e[i];
+#pragma unroll
+        for (int k = 0; k < NOLD; ++k) acc[k] = fma(__ldg(olds.p[k] + i), ei, acc[k]);
     }
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        if (k > nold) break;
+    for (int k = 0; k < NOLD; ++k) {
         const double v = block_sum(acc[k]);
         if (threadIdx.x == 0) part[(size_t)k * gridDim.x + blockIdx.x] = v;
     }
@@ -446,11 +454,25 @@ void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out) {
 void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
                 const double *const *olds, double *dots) {
     JUES_REQUIRE(nold >= 0 && nold <= 15, "diis_error supports up to 15 stored errors");
-    VecList vl;
-    for (int k = 0; k < nold; ++k) { vl.p[k] = olds[k]; vl.c[k] = 0.0; }
+    // partial sums: row 0 = e.e, rows 1..nold = old_k.e
     {
         Ctx::Scope s(ctx, "diis_error");
-        diis_error_kernel<<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, xn, x, v_out, e_out, nold, vl, ctx->d_red);
+        diis_pair_kernel<<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, xn, x, v_out, e_out, ctx->d_red);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    if (nold > 0) {
+        VecList vl;
+        for (int k = 0; k < nold; ++k) { vl.p[k] = olds[k]; vl.c[k] = 0.0; }
+        Ctx::Scope s(ctx, "diis_error");
+        double *part = ctx->d_red + RED_BLOCKS;
+        switch (nold) {
+#define JUES_MULTI_DOT(K) \
+    case K: multi_dot_kernel<K><<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, vl, e_out, part); break;
+            JUES_MULTI_DOT(1) JUES_MULTI_DOT(2) JUES_MULTI_DOT(3) JUES_MULTI_DOT(4) JUES_MULTI_DOT(5)
+            JUES_MULTI_DOT(6) JUES_MULTI_DOT(7) JUES_MULTI_DOT(8) JUES_MULTI_DOT(9) JUES_MULTI_DOT(10)
+            JUES_MULTI_DOT(11) JUES_MULTI_DOT(12) JUES_MULTI_DOT(13) JUES_MULTI_DOT(14) JUES_MULTI_DOT(15)
+#undef JUES_MULTI_DOT
+        }
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     double *out = ctx->d_red + 65536 - 48;   // (nold + 1) <= 16 sums, clear of finish_reduce's slot
