@@ -144,8 +144,17 @@ __global__ void splitk_reduce_kernel(const T *__restrict__ ws, int ks, long long
         long long m, n;
         divmod_ll(i, M, n, m);
         const T *p = ws + n * ld + m;
+        // eight partials loaded ahead of their (in-order) sum, so the loads overlap
         double acc = 0.0;
-        for (int s = 0; s < ks; ++s) acc += to_f64(p[s * sstride]);
+        int s = 0;
+        for (; s + 8 <= ks; s += 8) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = p[(long long)(s + u) * sstride];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc += to_f64(v[u]);
+        }
+        for (; s < ks; ++s) acc += to_f64(p[(long long)s * sstride]);
         const long long off = mode_off(mC, m) + mode_off(nC, n);
         double v = alpha == 1.0 ? acc : alpha * acc;
         if (beta != 0.0) v = fma(beta, Cin[off], v);

@@ -1072,6 +1072,15 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name, int np) {
         t.ksplit = (t.kblocks + t.kper - 1) / t.kper;
         t.partial = static_cast<float *>(ctx->splitk_scratch((size_t)t.ksplit * Mpad * Npad * sizeof(float)));
     }
+    // C = Cin + alpha AB into a dense column-major C: copy Cin over first and accumulate in
+    // place, so the epilogue's adds go to L2 reductions instead of the FP64 pipe
+    const bool disjoint = t.Cin + a.M * a.N <= t.C || t.C + a.M * a.N <= t.Cin;
+    if (t.ksplit <= 1 && a.beta == 1.0 && t.Cin != t.C && disjoint && a.mC.d0 == MODE_BIG && a.mC.s0 == 1 &&
+        a.nC.d0 == MODE_BIG && a.nC.s0 == a.M) {
+        JUES_CHECK_CUDA(cudaMemcpyAsync(a.C, t.Cin, (size_t)(a.M * a.N) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                        ctx->stream));
+        t.Cin = t.C;
+    }
     if (np == 3)
         launch_tc<64, 3, 3>(ctx, ma, mb, t, tiles, name);
     else if (BN == 128)
