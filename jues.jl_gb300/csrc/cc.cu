@@ -268,6 +268,10 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         Perm4 q{{o, v, v, o}, {1, ov * o, o, ov}, {1, o, ov, ov * v}};
         permute4(ctx, q, -1.0, s->ovov.p, 0.0, s->ovovK.p);
     }
+    if (method == 0) {
+        s->oovvT = DBuf<double>(ctx, t2n);
+        t_tilde(ctx, s->oovv.p, o, v, s->oovvT.p);
+    }
     s->invD = DBuf<double>(ctx, t2n);
     inv_denominators(ctx, s->eps.p, o, v, s->invD.p);
     s->T = DBuf<double>(ctx, t2n);
@@ -359,6 +363,11 @@ CCState *cc_create_df(Ctx *ctx, const double *b, int n, int naux, const double *
 }
 
 double cc_total_energy(CCState *s) {
+    // CCD (RCCD.jl:99-117): E = sum oovv[i,j,a,b] (2T[i,j,a,b] - T[j,i,a,b])
+    //                         = sum T[i,j,a,b] (2 oovv[i,j,a,b] - oovv[j,i,a,b]) (i <-> j in the second
+    // term), one dot product with weights formed once
+    if (s->method == 0 && s->oovvT.p)
+        return dot(s->ctx, (size_t)s->o * s->o * s->v * s->v, s->T.p, s->oovvT.p);
     double e = cc_energy(s->ctx, s->oovv.p, s->T.p, s->method == 1 ? s->t1.p : nullptr, s->o, s->v);
     if (s->fock && s->method == 1) e += 2.0 * dot(s->ctx, (size_t)s->o * s->v, s->fOV.p, s->t1.p);   // AutoRCCSD.jl:43
     return e;

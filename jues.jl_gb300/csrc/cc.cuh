@@ -15,6 +15,7 @@ struct CCState {
     // integrals, physicists' notation, column-major as the reference's get_eri blocks
     DBuf<double> eps, oovv, ovov, ovvo, oooo, vvvv, ooov, ovvv;
     DBuf<double> invD;           // 1 / D[i,j,a,b], formed once
+    DBuf<double> oovvT;          // CCD energy weights 2 oovv[i,j,a,b] - oovv[j,i,a,b], formed once
     DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;
