@@ -60,7 +60,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -70,6 +70,14 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def ready(self, timeout=5.0):
+        """Wait for nvidia-smi's first line (its start-up takes ~0.1 s), then drop it, so the
+        samples kept are the ones taken during the timed region that follows."""
+        t = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t < timeout:
+            time.sleep(0.01)
+        self.lines.clear()
 
     def stop(self):
         if not self.proc:
@@ -311,6 +319,7 @@ def run_gpu(args):
     launches0 = ctx.launches()
     clk = ClockSampler(local)
     clk.start()
+    clk.ready()
     barrier(pg)
     t0 = time.perf_counter()
     for _ in range(args.steps):

@@ -27,6 +27,7 @@
 #include <climits>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -202,6 +203,13 @@ struct TcArgs {
     int ksplit = 1;
     int kper = 0;
     float *partial = nullptr;
+    // Ragged last round (ksplit == 1): items [0, full_items) are whole tiles 0..full_items-1;
+    // the tail_tiles tiles after them are split tail_ks ways over K (tail_kper stages each), so
+    // the last round keeps every SM busy.  Their FP32 sums go to
+    // tail_partial[split][tail tile][BN][TBM] and tail_reduce_kernel finishes them.
+    long long full_items = 0;   // 0: no tail split
+    int tail_tiles = 0, tail_ks = 1, tail_kper = 0;
+    float *tail_partial = nullptr;
 };
 
 // Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-9 drain TMEM (two
@@ -237,25 +245,47 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// one work item of the persistent kernel: output tile (m0, n0) over stages [kb0, kb0 + nk)
-struct TcItem {
-    int m0, n0, kb0, nk;
-    long long split;
-};
-__device__ __forceinline__ TcItem tc_item(const TcArgs &g, long long w, int BN) {
-    TcItem I;
-    const long long tile = w % g.tiles;
-    I.split = w / g.tiles;
-    // raster: groups of (up to) 16 row tiles, rows fastest within a group, so the CTAs resident
-    // at one time reuse a few row tiles' operand rows from L2 across about ten column tiles
+// output tile index -> (m0, n0).  Raster: groups of (up to) 16 row tiles, rows fastest within a
+// group, so the CTAs resident at one time reuse a few row tiles' operand rows from L2 across
+// about ten column tiles.
+__device__ __forceinline__ void tc_tile_origin(const TcArgs &g, long long tile, int BN, int &m0, int &n0) {
     const long long G = min(g.mtiles, 16LL);
     const long long span = G * (g.tiles / g.mtiles);
     const long long grp = tile / span, in = tile - grp * span;
     const long long gm = min(G, g.mtiles - grp * G);
-    I.m0 = (int)((grp * G + in % gm) * TBM);
-    I.n0 = (int)((in / gm) * BN);
-    I.kb0 = (int)I.split * g.kper;
-    I.nk = min(g.kblocks - I.kb0, g.kper);
+    m0 = (int)((grp * G + in % gm) * TBM);
+    n0 = (int)((in / gm) * BN);
+}
+
+__host__ __device__ __forceinline__ long long tc_nitems(const TcArgs &g) {
+    return g.full_items > 0 ? g.full_items + (long long)g.tail_tiles * g.tail_ks : g.tiles * g.ksplit;
+}
+
+// one work item of the persistent kernel: output tile (m0, n0) over stages [kb0, kb0 + nk);
+// tail >= 0 marks a split part of a tail tile
+struct TcItem {
+    int m0, n0, kb0, nk;
+    long long split;
+    int tail;
+};
+__device__ __forceinline__ TcItem tc_item(const TcArgs &g, long long w, int BN) {
+    TcItem I;
+    long long tile;
+    if (g.full_items > 0 && w >= g.full_items) {
+        const long long u = w - g.full_items;
+        I.tail = (int)(u % g.tail_tiles);
+        I.split = u / g.tail_tiles;
+        tile = g.full_items + I.tail;
+        I.kb0 = (int)I.split * g.tail_kper;
+        I.nk = min(g.kblocks - I.kb0, g.tail_kper);
+    } else {
+        I.tail = -1;
+        tile = w % g.tiles;
+        I.split = w / g.tiles;
+        I.kb0 = (int)I.split * g.kper;
+        I.nk = min(g.kblocks - I.kb0, g.kper);
+    }
+    tc_tile_origin(g, tile, BN, I.m0, I.n0);
     return I;
 }
 
@@ -363,7 +393,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // persistent: CTA b processes work items b, b + gridDim.x, ...; an item is one output tile
     // over one K split.  Stage and chunk counters run on across items, so the pipeline and the
     // TMEM buffers never drain between tiles.
-    const long long nitems = g.tiles * g.ksplit;
+    const long long nitems = tc_nitems(g);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -572,7 +602,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 ok = false;
                 break;
             }
-            if (g.partial) {
+            if (I.tail >= 0) {
+                // a split part of a tail tile: raw sums (alpha folded in when a power of two),
+                // [split][tail tile][column][row], a warp writing 32 consecutive floats
+                float *dst = g.tail_partial + (((long long)I.split * g.tail_tiles + I.tail) * BN + half * HB) * TBM +
+                             quarter * 32 + lane;
+#pragma unroll
+                for (int j = 0; j < HB / 2; ++j) {
+                    dst[(long long)(2 * j) * TBM] = lo_f(acc2[j]);
+                    dst[(long long)(2 * j + 1) * TBM] = hi_f(acc2[j]);
+                }
+            } else if (g.partial) {
                 // raw partial sums, padded rows and columns included; a warp writes 32
                 // consecutive floats per column
                 const long long Mpad = g.mtiles * TBM, Npad = (g.tiles / g.mtiles) * BN;
@@ -608,6 +648,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc_fence_after();
         tmem_dealloc(tmem, Cfg::TMEM_COLS);
     }
+}
+
+// The split parts of the tail tiles, summed in split order in FP64 (deterministic), then
+// alpha (unless folded into the parts), beta and the output modes.  Grid (TBM BN / 256, tail
+// tiles): one element per thread, consecutive threads on consecutive rows (coalesced), the
+// parts of an element loaded before they are summed.
+__global__ void __launch_bounds__(256) tail_reduce_kernel(const TcArgs g, int BN) {
+    const int q = blockIdx.y;
+    const int e = blockIdx.x * 256 + threadIdx.x;
+    const int r = e % TBM, c = e / TBM;
+    int m0, n0;
+    tc_tile_origin(g, g.full_items + q, BN, m0, n0);
+    const long long m = (long long)m0 + r, n = (long long)n0 + c;
+    if (c >= BN || m >= g.M || n >= g.N) return;
+    const float *p = g.tail_partial + ((long long)q * BN + c) * TBM + r;
+    const long long sstride = (long long)g.tail_tiles * BN * TBM;
+    float part[16];
+#pragma unroll
+    for (int s = 0; s < 16; ++s) part[s] = s < g.tail_ks ? p[s * sstride] : 0.f;
+    double acc = 0.0;
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+        if (s < g.tail_ks) acc += to_f64(part[s]);
+    const long long off = mode_off(g.mC, m) + mode_off(g.nC, n);
+    double v = (g.alpha_pow2 || g.alpha == 1.0) ? acc : g.alpha * acc;
+    if (g.beta != 0.0) v = fma(g.beta, g.Cin[off], v);
+    g.C[off] = v;
 }
 
 constexpr int PR = 16, PK = 128, KCH = 128;   // pack tile = one scaling chunk = two pipeline stages
@@ -949,7 +1016,7 @@ static int sm_count(int device) {
 
 template <int BN, int STAGES, int NP>
 static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
-                      const char *name) {
+                      const char *name, bool allow_tail = true) {
     using Cfg = TcCfg<BN, STAGES, TC_KC, NP>;
     static bool attr_set = false;
     if (!attr_set) {
@@ -972,13 +1039,43 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
     g.alpha_k = g.alpha_pow2 ? ak - 1 : 0;
     g.alpha_neg = (g.alpha_pow2 && g.alpha < 0) ? 1 : 0;
     g.beta_mode = g.beta == 0.0 ? 0 : (g.beta == 1.0 ? (g.Cin == g.C ? 1 : 2) : 3);
-    const long long items = tiles * g.ksplit;
+    // A ragged last round (at most a quarter of the SMs busy) has its tiles split over K so that
+    // it keeps every SM busy: 2600 tiles on 152 SMs run as 17 full rounds plus 16 tiles x 9
+    // parts.  With fewer parts the saving (1 - 1/parts of a round) does not cover the reduction.
+    const long long sms = sm_count(ctx->device);
+    g.full_items = 0;
+    if (allow_tail && g.ksplit == 1) {
+        const long long rounds = (tiles + sms - 1) / sms, tail = tiles - (rounds - 1) * sms;
+        if (rounds >= 2 && 4 * tail <= sms && g.kblocks >= 4 * TC_KC) {
+            int ks = (int)std::min<long long>(sms / tail, 16);
+            int kper = (g.kblocks + ks - 1) / ks;
+            kper = std::max(2 * TC_KC, (kper + TC_KC - 1) / TC_KC * TC_KC);
+            ks = (g.kblocks + kper - 1) / kper;
+            if (ks >= 4) {
+                g.full_items = tiles - tail;
+                g.tail_tiles = (int)tail;
+                g.tail_ks = ks;
+                g.tail_kper = kper;
+                g.tail_partial = static_cast<float *>(
+                    ctx->splitk_scratch((size_t)ks * tail * BN * TBM * sizeof(float)));
+            }
+        }
+    }
+    const long long items = tc_nitems(g);
     JUES_REQUIRE(items < (1LL << 31), "too many output tiles");
     // persistent: one CTA per SM (the stage ring takes most of shared memory)
-    const long long grid = std::min<long long>(items, sm_count(ctx->device));
-    Ctx::Scope s(ctx, name);
-    gett_tc_kernel<BN, STAGES, TC_KC, NP><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
-    JUES_CHECK_CUDA(cudaGetLastError());
+    const long long grid = std::min<long long>(items, sms);
+    {
+        Ctx::Scope s(ctx, name);
+        gett_tc_kernel<BN, STAGES, TC_KC, NP><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    if (g.full_items > 0) {
+        const std::string nm = std::string(name) + ".reduce";
+        Ctx::Scope s(ctx, nm.c_str());
+        tail_reduce_kernel<<<dim3((unsigned)(TBM * BN / 256), (unsigned)g.tail_tiles), 256, 0, ctx->stream>>>(g, BN);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
 }
 
 // Number of K splits: the wave count times the stages per split (plus a fixed per-CTA start-up
@@ -1181,7 +1278,7 @@ void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
     t.expB_ld = Npad;
     const long long tiles = t.mtiles * (Npad / BN);
     JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
-    launch_tc<BN, 3, 2>(ctx, ma, mb, t, tiles, "gemm_noalloc");
+    launch_tc<BN, 3, 2>(ctx, ma, mb, t, tiles, "gemm_noalloc", false);   // no scratch: no tail split
 }
 
 }  // namespace jues

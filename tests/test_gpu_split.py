@@ -95,6 +95,26 @@ def test_gemm_split_epilogue_forms(lib):
         assert np.abs(got - (alpha * P - 1.3 * C0)).max() < 1e-14 * np.abs(got).max()
 
 
+def test_gemm_split_ragged_last_round(lib):
+    """160 output tiles on a GPU of ~150 SMs: the tiles of the ragged last round are split over K
+    (FP32 parts summed in FP64 by a second kernel).  Every tile must match the exact emulation of
+    the split representation, and the epilogue forms (alpha folded or not, beta = 1 in place,
+    general beta) must hold on the split tiles as on the whole ones."""
+    rng = np.random.default_rng(21)
+    A = rng.normal(size=(20480, 1024))
+    B = rng.normal(size=(1024, 128))
+    C0 = rng.normal(size=(20480, 128))
+    emu = emulate(A, B)
+    P = lib.gemm(A, B, precision="split_bf16")
+    assert np.abs(P - emu).max() < 1e-6 * np.abs(emu).max()
+    # the tail rows (the last tiles) were computed by the split path
+    assert np.abs(P[-1024:] - emu[-1024:]).max() < 1e-6 * np.abs(emu).max()
+    for alpha, beta in ((-0.5, 1.0), (0.7, 1.0), (4.0, 0.0), (0.7, -1.3)):
+        got = lib.gemm(A, B, C0, alpha=alpha, beta=beta, precision="split_bf16")
+        want = alpha * emu + beta * C0
+        assert np.abs(got - want).max() < 2e-6 * np.abs(want).max()
+
+
 @pytest.mark.parametrize("M,N,K,ta,tb", SHAPES)
 def test_gemm_split_bf16(lib, M, N, K, ta, tb):
     rng = np.random.default_rng(7 * M + N + K)
