@@ -13,6 +13,10 @@
  *  - A jues_ctx owns one CUDA stream and every device buffer it allocates.  A context is
  *    single-threaded; different contexts may be used concurrently.  Calls are synchronous
  *    at return.
+ *  - Host input arrays of 64 MB and more are page-locked in 512 MB pieces for the duration
+ *    of their copy and released before the call returns (arrays the caller has already
+ *    page-locked are copied as they are).  The batched entry points instead copy through a
+ *    page-locked staging ring owned by the context (host threads, 3 x 64 MB).
  *
  * Reference interfaces replaced (paths within mdav2/JuES.jl):
  *  jues_tei_transform  <- JuES.Transformation.tei_transform        src/Backend/Transformation.jl:15-20,39-93
