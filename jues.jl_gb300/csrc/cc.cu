@@ -128,6 +128,12 @@ double ccd_sweep(CCState *s, int prec) {
       plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
 
     s->cache_operands = false;
+    // with DIIS the step norm comes from its error vector (the same |Tn - T|^2), so the
+    // finalisation skips it: two of its five FP64 operations per element
+    if (s->opts.diis) {
+        t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, nullptr, s->Tn.p);
+        return -1.0;
+    }
     return t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p);
 }
 
@@ -169,7 +175,7 @@ static void diis_reset(CCState *s) {
 
 // x = vector fed into the sweep, xn = sweep output (both length len, device); on return x holds
 // the extrapolated vector.
-static void diis_step(CCState *s, double *x, const double *xn, size_t len) {
+static void diis_step(CCState *s, double *x, const double *xn, size_t len, double *ee = nullptr) {
     Ctx *ctx = s->ctx;
     const int cap = std::max(1, s->opts.diis_size - 1);
     if ((int)s->dv.size() < cap) {
@@ -199,6 +205,7 @@ static void diis_step(CCState *s, double *x, const double *xn, size_t len) {
     std::vector<double> row(m);
     for (int k = 0; k < m - 1; ++k) row[k] = dots[1 + k];
     row[m - 1] = dots[0];
+    if (ee) *ee = dots[0];   // |xn - x|^2
     for (int k = 0; k < m - 1; ++k) s->gram[k].push_back(row[k]);
     s->gram.push_back(row);
     double mx = 0.0;
@@ -439,10 +446,11 @@ static void cc_one(CCState *s, int prec) {
     } else {
         r2 = ccsd_sweep(s, prec);
     }
-    double rn = std::sqrt(r2);
     if (s->opts.diis) {
         if (s->method == 0) {
-            diis_step(s, s->T.p, s->Tn.p, t2n);
+            double ee = 0.0;
+            diis_step(s, s->T.p, s->Tn.p, t2n, &ee);
+            if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
         } else {
             // pack [t1; T2] contiguously for the DIIS vectors
             if (s->aux1.n < t1n + t2n) s->aux1 = DBuf<double>(ctx, t1n + t2n);
@@ -459,6 +467,7 @@ static void cc_one(CCState *s, int prec) {
         std::swap(s->T, s->Tn);
         if (s->method == 1) std::swap(s->t1, s->t1n);
     }
+    double rn = std::sqrt(r2);
     s->e_prev = s->energy;
     s->energy = cc_total_energy(s);
     if (s->auto_rms) {
