@@ -2,13 +2,16 @@
 //
 // The equations are those of src/CoupledCluster/RCCD.jl:234-303 (== mRCCD.jl:301-394) and
 // RCCSD.jl:187-289; intermediates as in RCCD.jl:169-467.  Every contraction is one GETT over
-// composite tensor modes, so no permuted copies of T2 are made.  Two exact rewrites reduce the
+// composite tensor modes, so no permuted copies of T2 are made.  Three exact rewrites reduce the
 // work without changing the result beyond rounding:
 //   * Wabef is never formed: sum_ef T[ij,ef] Wabef[ab,ef] = T.vvvv^T + 1/2 X^T.T with
 //     X[mn,ij] = sum_ef oovv[mn,ef] T[ij,ef]; X also gives Wmnij (= oooo + X/2), so the two
 //     ladders become T.vvvv^T + (oooo + X)^T.T  (2o^2v^4 + 4o^4v^2 instead of 4o^2v^4 + 2o^4v^2);
 //   * the terms of RCCD.jl:243-254 that are images of each other under (i,a)<->(j,b) are
-//     computed once into Z and added as Z[i,j,a,b] + Z[j,i,b,a] by the finalisation kernel.
+//     computed once into Z and added as Z[i,j,a,b] + Z[j,i,b,a] by the finalisation kernel;
+//   * the two Fmi terms, - T[i,m,a,b] Fmi[m,j] - T[m,j,a,b] Fmi[m,i], are hole-hole ladder
+//     terms with W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i], so they cost no GEMM
+//     of their own (that one had K = o and needed its own operand pack of T2).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -24,7 +27,7 @@ namespace jues {
 double ccd_sweep_flops(int o_, int v_) {
     double o = o_, v = v_;
     return 2 * o * o * v * v * v * v + 12 * o * o * o * v * v * v + 4 * o * o * o * o * v * v +
-           4 * o * o * v * v * v + 4 * o * o * o * v * v;
+           4 * o * o * v * v * v + 2 * o * o * o * v * v;
 }
 
 double ccd_reference_flops(int o_, int v_) {
@@ -86,7 +89,10 @@ double ccd_sweep(CCState *s, int prec) {
     // W'[mn,ij] = oooo[mn,ij] + sum_ef oovv[mn,ef] T[ij,ef]        (Wmnij + the Wabef T-part)
     G(s, prec, "ccd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), T, plain(oo), plain(1), 1.0, s->Wp.p,
       plain(1), plain(oo), s->oooo.p);
-    // L = oovv + (W')^T.T + T.vvvv^T                                     (RCCD.jl:243,245,246)
+    // - T[i,m,a,b] Fmi[m,j] - T[m,j,a,b] Fmi[m,i] (RCCD.jl:244) as hole-hole ladder terms:
+    // W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i]
+    wp_fmi(ctx, s->Wp.p, s->Fmi.p, (int)o);
+    // L = oovv + (W')^T.T + T.vvvv^T                                     (RCCD.jl:243-246)
     G(s, prec, "ccd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), T, plain(1), plain(oo),
       1.0, s->L.p, plain(1), plain(oo), W);
     G(s, prec, "ccd_pp_ladder", oo, vv, vv, 1.0, T, plain(1), plain(oo), s->vvvv.p, plain(vv), plain(1),
@@ -114,9 +120,6 @@ double ccd_sweep(CCState *s, int prec) {
     // + T[i,j,a,e] Fae[b,e]
     G(s, prec, "ccd_z_fae", oov, v, v, 1.0, T, plain(1), plain(oov), s->Fae.p, plain(v), plain(1), 0.0,
       Z, plain(1), plain(oov));
-    // - T[i,m,a,b] Fmi[m,j]
-    G(s, prec, "ccd_z_fmi", o * vv, o, o, -1.0, T, mode2(o, 1, oo), plain(o), s->Fmi.p, plain(1),
-      plain(o), 1.0, Z, mode2(o, 1, oo), plain(o));
     // + T[i,m,a,e] (2WmBeJ + WmBEj)[m,b,e,j]
     G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
       plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));

@@ -249,6 +249,8 @@ void divide_by_d(Ctx *ctx, const double *in, const double *eps, int o, int v, do
 void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out);
 // sum_k c_k * vecs[k] -> out (length n)
 void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out);
+// W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i] (o^4 W', o x o Fmi, column-major)
+void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o);
 // DIIS bookkeeping in one pass: v_out = xn, e_out = xn - x, dots[0] = e.e, dots[1 + k] = olds[k].e
 void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
                 const double *const *olds, double *dots);

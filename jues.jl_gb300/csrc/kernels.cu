@@ -262,6 +262,19 @@ __global__ void reduce_rows(const double *part, int n, double *out) {
     if (threadIdx.x == 0) out[blockIdx.x] = v;
 }
 
+// W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i]: the two Fmi terms of the T2 update
+// ride in the hole-hole ladder.  One thread per column (i,j), so no entry has two writers.
+__global__ void wp_fmi_kernel(double *__restrict__ Wp, const double *__restrict__ Fmi, int o) {
+    const long long oo = (long long)o * o;
+    for (long long ij = blockIdx.x * (long long)blockDim.x + threadIdx.x; ij < oo;
+         ij += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(ij % o), j = (int)(ij / o);
+        double *col = Wp + oo * ij;
+        for (int k = 0; k < o; ++k) col[i + (long long)o * k] -= Fmi[k + (long long)o * j];   // m = i, n = k
+        for (int k = 0; k < o; ++k) col[k + (long long)o * j] -= Fmi[k + (long long)o * i];   // m = k, n = j
+    }
+}
+
 __global__ void t1_finalize_kernel(double *__restrict__ t1n, const double *__restrict__ eps, int o, int v,
                                    const double *__restrict__ t1old, double *part) {
     double acc = 0.0;
@@ -481,6 +494,12 @@ void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v
     JUES_CHECK_CUDA(cudaGetLastError());
     JUES_CHECK_CUDA(cudaMemcpyAsync(dots, out, (nold + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     JUES_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o) {
+    Ctx::Scope s(ctx, "wp_fmi");
+    wp_fmi_kernel<<<grid_for((long long)o * o), 256, 0, ctx->stream>>>(Wp, Fmi, o);
+    JUES_CHECK_CUDA(cudaGetLastError());
 }
 
 void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out) {
