@@ -262,16 +262,20 @@ __global__ void reduce_rows(const double *part, int n, double *out) {
     if (threadIdx.x == 0) out[blockIdx.x] = v;
 }
 
-// W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i]: the two Fmi terms of the T2 update
-// ride in the hole-hole ladder.  One thread per column (i,j), so no entry has two writers.
-__global__ void wp_fmi_kernel(double *__restrict__ Wp, const double *__restrict__ Fmi, int o) {
-    const long long oo = (long long)o * o;
-    for (long long ij = blockIdx.x * (long long)blockDim.x + threadIdx.x; ij < oo;
-         ij += (long long)gridDim.x * blockDim.x) {
+// W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] (first = true) or [n = j] Fmi[m,i]: the two Fmi terms of
+// the T2 update ride in the hole-hole ladder.  One thread per (i, j, k); within one launch every
+// entry has one writer, and the two launches are ordered on the stream.
+__global__ void wp_fmi_kernel(double *__restrict__ Wp, const double *__restrict__ Fmi, int o, bool first) {
+    const long long oo = (long long)o * o, ooo = oo * o;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ooo;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % o);
+        const long long ij = t / o;
         const int i = (int)(ij % o), j = (int)(ij / o);
-        double *col = Wp + oo * ij;
-        for (int k = 0; k < o; ++k) col[i + (long long)o * k] -= Fmi[k + (long long)o * j];   // m = i, n = k
-        for (int k = 0; k < o; ++k) col[k + (long long)o * j] -= Fmi[k + (long long)o * i];   // m = k, n = j
+        if (first)
+            Wp[oo * ij + i + (long long)o * k] -= Fmi[k + (long long)o * j];   // m = i, n = k
+        else
+            Wp[oo * ij + k + (long long)o * j] -= Fmi[k + (long long)o * i];   // m = k, n = j
     }
 }
 
@@ -498,7 +502,10 @@ void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v
 
 void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o) {
     Ctx::Scope s(ctx, "wp_fmi");
-    wp_fmi_kernel<<<grid_for((long long)o * o), 256, 0, ctx->stream>>>(Wp, Fmi, o);
+    const long long n = (long long)o * o * o;
+    wp_fmi_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(Wp, Fmi, o, true);
+    wp_fmi_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(Wp, Fmi, o, false);
+    ctx->count_launch();
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
