@@ -14,7 +14,10 @@
 // correction term is 2^-10 smaller, so its rounding is below 1e-10 of the result.  Chunks
 // alternate between two TMEM buffers; eight warps scale each finished chunk by
 // 2^(e_r + e_c - 18) and add it into FP32 registers (round-to-nearest, unbiased) while the next
-// chunk runs, then apply alpha/beta in FP64 through the output tensor modes.  Operand tiles
+// chunk runs, then write the tile through the output tensor modes without the FP64 pipe
+// (integer FP32 -> FP64 conversion, power-of-two alpha folded into the FP32 scale, in-place
+// accumulation as L2 reductions).  The grid is persistent (one CTA per SM); a ragged last round
+// has its tiles split over K, their parts summed by tail_reduce_kernel.  Operand tiles
 // arrive by TMA (128-byte swizzle) into a STAGES-deep shared-memory ring guarded by mbarriers;
 // one thread issues the TMA loads and one the MMAs.  Every mbarrier wait is bounded by
 // %globaltimer; on expiry the CTA raises FLAG_TIMEOUT, skips its stores, frees its TMEM and
