@@ -137,6 +137,12 @@ JUES_API int jues_gemm_noalloc(jues_ctx *ctx, int transA, int transB, int M, int
                                const double *A_dev, int lda, const double *B_dev, int ldb, double beta,
                                double *C_dev, int ldc);
 
+/* Failure-path check: runs one device wait on a barrier phase that nothing completes, with the
+ * same bounded wait as the split GEMM's pipeline.  The wait gives up after its limit (~2 s), the
+ * kernel returns with the timeout flag set, and the call returns JUES_ETIMEOUT; the context stays
+ * usable.  Nothing faults or hangs. */
+JUES_API int jues_debug_expired_wait(jues_ctx *ctx);
+
 /* ---- four-index transformation -------------------------------------------------------
  * out[i,a,j,b] = sum C1[mu,i] C2[nu,a] C3[lam,j] C4[sig,b] gao[mu,nu,lam,sig]
  * (chemists' (C1 C2|C3 C4)); gao is n^4, Ck is n x dk, out is d1 x d2 x d3 x d4.

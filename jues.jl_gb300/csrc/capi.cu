@@ -352,6 +352,14 @@ int jues_gemm_noalloc(jues_ctx *ctx, int transA, int transB, int M, int N, int K
     });
 }
 
+int jues_debug_expired_wait(jues_ctx *ctx) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        JUES_CHECK_CUDA(cudaSetDevice(c.device));
+        expired_wait(&c);
+    });
+}
+
 int jues_tei_transform(jues_ctx *ctx, const double *gao, int n, const double *C1, int d1, const double *C2,
                        int d2, const double *C3, int d3, const double *C4, int d4, int precision,
                        double *out) {

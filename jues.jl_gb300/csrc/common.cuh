@@ -204,6 +204,8 @@ void splitk_reduce(Ctx *ctx, const double *ws, int ks, long long sstride, long l
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
 // split GEMM that packs into a static device array instead of allocating (see gett_tc.cu)
 void gett_tc_noalloc(Ctx *ctx, const GettArgs &g);
+// one device wait that nothing completes: throws JUES_ETIMEOUT after the bounded wait expires
+void expired_wait(Ctx *ctx);
 size_t gett_tc_noalloc_limit();
 void pack_cache_clear(Ctx *ctx);
 void pack_cache_destroy(PackCache *p);

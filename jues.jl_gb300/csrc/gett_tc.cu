@@ -101,6 +101,20 @@ __device__ bool mbar_wait_quiet(uint64_t *bar, uint32_t parity) {
         }
     }
 }
+// a wait on a barrier phase that nothing completes: the bounded wait expires and the kernel
+// raises FLAG_TIMEOUT, the failure path of every pipeline wait, exercised without a fault
+__global__ void expired_wait_kernel(unsigned *flags) {
+    __shared__ uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait(&bar, 0u, &abort_flag, flags)) atomicOr(flags, FLAG_TIMEOUT);
+}
+
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
                                             int z) {
     asm volatile(
@@ -1235,6 +1249,15 @@ void pack_into(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long
 }  // namespace
 
 size_t gett_tc_noalloc_limit() { return NOALLOC_SCRATCH_BYTES; }
+
+void expired_wait(Ctx *ctx) {
+    {
+        Ctx::Scope s(ctx, "expired_wait");
+        expired_wait_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_flags);
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    ctx->check_flags();   // throws JUES_ETIMEOUT and clears the flag
+}
 
 void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
     if (a.M <= 0 || a.N <= 0) return;

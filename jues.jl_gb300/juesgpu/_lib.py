@@ -70,6 +70,7 @@ SIGNATURES = {
     "jues_ctx_launch_count": (C.c_longlong, [VP]),
     "jues_gemm": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, DP, C.c_int,
                             DP, C.c_int, C.c_double, DP, C.c_int, C.c_int]),
+    "jues_debug_expired_wait": (C.c_int, [VP]),
     "jues_gemm_noalloc": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, VP, C.c_int,
                                     VP, C.c_int, C.c_double, VP, C.c_int]),
     "jues_tei_transform": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP,
