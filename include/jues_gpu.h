@@ -50,17 +50,30 @@ extern "C" {
 #define JUES_ETIMEOUT 6    /* a bounded device-side wait expired (kernel returned early) */
 #define JUES_ENODEV 7      /* no usable sm_103 device */
 
-/* arithmetic used for the bulk of the contractions */
-#define JUES_PREC_FP64 0       /* plain FP64 (the drop-in form)                          */
-#define JUES_PREC_SPLIT_BF16 1 /* tcgen05, operands as hi + lo 10-bit integers carried in
-                                  FP16, three products, ~2^-20 relative                  */
-#define JUES_PREC_SPLIT3 2     /* tcgen05, hi + mid + lo (30 bits), six products,
-                                  ~2^-24 relative (FP32 chunk sums)                      */
+/* Arithmetic used for the bulk of the contractions.  The split forms run on the tcgen05 tensor
+ * cores (kind::f16) with FP32 accumulation: every FP64 operand is cut into 10-bit integer digits
+ * ("planes") carried exactly in FP16, with a power-of-two scale per 128-wide K chunk of a row.
+ * Two planes (hi + lo, three products) keep ~2^-20 relative; three (hi + mid + lo, six products)
+ * keep ~2^-24, the FP32 rounding of the chunk sums. */
+#define JUES_PREC_FP64 0       /* plain FP64 (the drop-in form)                                   */
+#define JUES_PREC_SPLIT 1      /* the split form at <= 1 uEh: three planes for every contraction
+                                  that produces integrals (four-index transforms, get_eri blocks,
+                                  DF factors, the MP2 adjoint's back-transforms), two planes for
+                                  the CC sweeps, jues_gemm and (T)                               */
+#define JUES_PREC_SPLIT_BF16 JUES_PREC_SPLIT   /* earlier name of JUES_PREC_SPLIT              */
+#define JUES_PREC_SPLIT3 2     /* three planes for every contraction                              */
+#define JUES_PREC_SPLIT2 3     /* two planes for every contraction, integrals included: fastest,
+                                  ~5e-6 Eh MP2 error at nbf=200 (opt-in)                          */
 
 /* CC initial amplitudes */
 #define JUES_GUESS_ZERO 0  /* T2 = 0 (mRCCD.jl:239-256); first sweep gives MP2 amplitudes   */
 #define JUES_GUESS_MP2 1   /* T2 = <ij|ab>/D (mRCCSD.jl:66)                                  */
 #define JUES_GUESS_OVOV 2  /* T2 = (ij|ab)/D (RCCD.jl:145-160)                               */
+
+/* CCSD: the t1 term of Fae.  The reference's two CCSD forms differ there: RCCSD.jl:190 (and the
+ * textbook closed-shell equations) contract t1[m,f] with <ma|ef>, mRCCSD.jl:140 with <me|af>. */
+#define JUES_CCSD_FAE_RCCSD 0   /* <ma|ef>, RCCSD.jl:190                                        */
+#define JUES_CCSD_FAE_MRCCSD 1  /* <me|af>, mRCCSD.jl:140                                       */
 
 /* DF-RCCD equation variants */
 #define JUES_DF_REFERENCE 0  /* as DF-RCCD.jl: WmBeJ's last term reads (me|nf) T[n,j,f,b]     */
@@ -78,7 +91,9 @@ typedef struct {
     int precision;    /* JUES_PREC_*                                                       */
     int guess;        /* JUES_GUESS_*                                                      */
     int refine;       /* split precision only: number of closing FP64 sweeps               */
-    int transform_precision; /* precision of the integral transform; -1 = same as precision */
+    int transform_precision; /* precision of the integral transform; -1 = same as precision
+                                (JUES_PREC_SPLIT then means three-plane integrals)            */
+    int ccsd_fae;     /* CCSD only: JUES_CCSD_FAE_* (default JUES_CCSD_FAE_RCCSD)            */
 } jues_cc_opts;
 
 typedef struct {
@@ -121,18 +136,20 @@ JUES_API int jues_gemm(jues_ctx *ctx, int transA, int transB, int M, int N, int 
                        double *C, int ldc, int precision);
 
 /* Allocation-free variant of jues_gemm's split-precision path.  No counterpart in the
- * reference.  For callers that cannot allocate device memory when they contract: code running
- * under CUDA graph capture (where cudaMalloc is not permitted), hosts whose device memory is
- * owned by their own pool allocator, and fixed-budget callers.  A, B and C are DEVICE
- * pointers (column-major, C = alpha op(A) op(B) + beta C); the call allocates nothing: the
- * packed operands go to a static device array of 64 MiB that every GPU loading the library
- * holds until the process exits.  Problems whose packed operands,
- * 4 (Mpad + Npad) Kpad + 4 ceil(Kpad/64) (Mpad + Npad) bytes with Mpad, Npad and Kpad rounded
+ * reference.  For callers that cannot let the library allocate device memory when they
+ * contract: host frameworks that reserve the GPU's memory at start-up and hand it out from their
+ * own pool (a cudaMalloc from inside the library would fail, or escape their accounting), and
+ * long-running or fixed-budget services that must not grow their device footprint after
+ * start-up.  A, B and C are DEVICE pointers (column-major, C = alpha op(A) op(B) + beta C,
+ * two-plane split arithmetic; K = 0 gives C = beta C); the call allocates nothing: the packed
+ * operands go to a static device array of 64 MiB that every GPU loading the library holds until
+ * the process exits.  Problems whose packed operands,
+ * 4 (Mpad + Npad) Kpad + 4 ceil(Kpad/128) (Mpad + Npad) bytes with Mpad, Npad and Kpad rounded
  * up to 128, 128 and 64, exceed it are rejected with JUES_EINVAL.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress, with that device current); make
- * that first call before any stream capture.  All calls share the one array: calls whose
+ * looks up the array's device address (cudaGetSymbolAddress, with that device current).  All
+ * calls share the one array and each call rewrites every byte of it that it reads: calls whose
  * execution overlaps on the GPU (other streams, other contexts on the same device) race on it.
- * Runs on the context's stream and is synchronous at return. */
+ * Runs on the context's stream and is synchronous at return (it reads the device error flags). */
 JUES_API int jues_gemm_noalloc(jues_ctx *ctx, int transA, int transB, int M, int N, int K, double alpha,
                                const double *A_dev, int lda, const double *B_dev, int ldb, double beta,
                                double *C_dev, int ldc);
@@ -189,10 +206,13 @@ JUES_API int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const do
 
 /* ---- batched MP2 (no reference counterpart; the batched form) --------------------------
  * Energies and, when the pointer arrays are given, adjoints of many independent closed-shell
- * systems of uneven size.  All systems run in one CUDA graph of grouped persistent GETT
- * launches (13 stages); tile shapes are autotuned and the graph is cached for a repeated batch
- * signature.  Host arrays; gao_bar / C_bar are arrays of nsys host pointers (entries may be
- * NULL, the arrays themselves may be NULL). */
+ * systems of uneven size.  All systems run in one CUDA graph of grouped persistent launches (one
+ * per stage, 12 stages with the adjoint); the graph is cached for a repeated batch signature.
+ * precision: JUES_PREC_FP64 runs every stage as a grouped FP64 GETT; the split forms add, for
+ * every stage whose contractions all have K <= 64 (all but the final dE/dC stage when every
+ * nbf <= 64), the grouped three-plane tcgen05 GEMM as a candidate.  On first use each stage's
+ * form is chosen by timing the candidates (autotuning).  Host arrays; gao_bar / C_bar are arrays
+ * of nsys host pointers (entries may be NULL, the arrays themselves may be NULL). */
 typedef struct {
     int n, o;             /* nbf and nocc; nvir = n - o                               */
     const double *gao;    /* n^4 AO integrals, column-major                            */
@@ -205,10 +225,15 @@ typedef struct {
     int graph_nodes;      /* kernels in the captured graph                              */
     int tuned;            /* 1 if this call built, autotuned and captured the plan       */
     int nstages;          /* grouped GETT stages                                         */
-    int tile_shape[16];   /* chosen shape per stage: 0 64x64, 1 32x64, 2 64x32, 3 32x32  */
+    int tile_shape[16];   /* chosen form per stage: FP64 tiles 0 64x64, 1 32x64, 2 64x32,
+                             3 32x32; 4 the grouped three-plane tcgen05 GEMM             */
 } jues_batch_info;
 
-JUES_API int jues_batch_rmp2(jues_ctx *ctx, int nsys, const jues_mp2_system *systems, double e_bar,
+/* Which forms the batched entry point's autotuning may pick (no reference counterpart):
+ * 0 = time every candidate (default), 1 = the FP64 tile shapes only, 2 = the grouped tcgen05
+ * GEMM wherever it was built (split precision), FP64 tiles elsewhere. */
+JUES_API int jues_ctx_set_batch_form(jues_ctx *ctx, int form);
+JUES_API int jues_batch_rmp2(jues_ctx *ctx, int nsys, const jues_mp2_system *systems, int precision, double e_bar,
                              double *e_out, double **gao_bar, double **C_bar, jues_batch_info *info);
 
 /* ---- coupled cluster ------------------------------------------------------------------

@@ -2,12 +2,15 @@
 //
 // Every system's four-index transform, MP2 energy / Gamma seed, back-transform and dE/dC
 // contractions are laid out in one device arena.  Step k of every system forms one grouped,
-// persistent FP64 GETT launch (a tile list spanning all systems), so the whole batch is 13
-// launches: 4 forward quarters, the energy/Gamma kernel, 4 back-transform quarters, 3 steps of
-// the two three-quarter transforms and the final dE/dC contractions.  The sequence is captured
-// once into a CUDA graph and replayed; the tile shape of each grouped launch is chosen by timing
-// the candidate shapes with CUDA events on first use (autotuning), and both the plan and the
-// graph are cached by the batch signature (the list of (nbf, nocc) and the requested outputs).
+// persistent GETT launch (a tile list spanning all systems): 4 forward quarters, the
+// energy/Gamma kernels, 4 back-transform quarters, 3 steps of the two three-quarter transforms
+// and the final dE/dC contractions.  Each stage runs either as the grouped FP64 GETT with one of
+// four tile shapes or, in split precision, as the grouped three-plane tcgen05 GEMM (two grouped
+// operand packs and one persistent launch; stages whose contractions all have K <= 64).  The
+// form of each stage is chosen by timing the candidates with CUDA events on first use
+// (autotuning); the sequence is then captured once into a CUDA graph and replayed, and both the
+// plan and the graph are cached by the batch signature (the list of (nbf, nocc), the requested
+// outputs and the precision).
 #include <algorithm>
 #include <map>
 #include <string>
@@ -29,44 +32,105 @@ struct SysDesc {
     double *e;           // energy slot
     int o, v;
     double e_bar;
+    long long block0;    // first block of this system in mp2_gamma_grouped's grid
+    int nblocks;         // its blocks
+    int pairs_per_block; // (a <= b) pairs per block
 };
 
-// one block per system: Gamma = 2 e_bar (2K_iajb - K_ibja)/D and E = sum K(2K - K~)/D
-__global__ void mp2_gamma_grouped(const SysDesc *__restrict__ sys) {
-    const SysDesc s = sys[blockIdx.x];
-    const int o = s.o, v = s.v;
-    const long long ov = (long long)o * v;
-    const long long total = ov * ov;
-    double acc = 0.0;
-    for (long long x = threadIdx.x; x < total; x += blockDim.x) {
-        const long long r = x;
-        const int i = (int)(r % o);
-        const int a = (int)((r / o) % v);
-        const int j = (int)((r / ov) % o);
-        const int b = (int)(r / (ov * o));
-        const long long y = i + (long long)o * b + ov * j + ov * o * a;   // K[i,b,j,a]
-        const double inv = 1.0 / (s.eps[i] + s.eps[j] - s.eps[o + a] - s.eps[o + b]);
-        const double k = s.K[x], kx = s.K[y];
-        acc = fma(k * (2.0 * k - kx), inv, acc);
-        s.G[x] = 2.0 * s.e_bar * (2.0 * k - kx) * inv;
-    }
+// pair index p (a <= b) -> (a, b)
+__device__ __forceinline__ void pair_of(long long p, int &a, int &b) {
+    long long bb = (long long)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+    while (bb * (bb + 1) / 2 > p) --bb;
+    while ((bb + 1) * (bb + 2) / 2 <= p) ++bb;
+    b = (int)bb;
+    a = (int)(p - bb * (bb + 1) / 2);
+}
+
+__device__ __forceinline__ double block_total(double acc) {
     __shared__ double red[32];
     for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
+    __syncthreads();
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x < 32) {
         acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
         for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
-        if (threadIdx.x == 0) *s.e = acc;
     }
+    return acc;
 }
+
+// Gamma = 2 e_bar (2K_iajb - K_ibja)/D and the energy's partial sums.  Each block takes a run of
+// (a <= b) pairs of one system (several blocks per large system, so the largest systems do not
+// serialise on one block); for a pair both K[:,a,:,b] and K[:,b,:,a] are read once.  The block's
+// energy partial goes to part[block]; mp2_energy_grouped adds them per system in block order.
+__global__ void __launch_bounds__(256) mp2_gamma_grouped(const SysDesc *__restrict__ sys, int nsys,
+                                                         double *__restrict__ part) {
+    const long long blk = blockIdx.x;
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sys[mid].block0 <= blk) lo = mid; else hi = mid - 1;
+    }
+    const SysDesc &S = sys[lo];
+    const int o = S.o, v = S.v, oo = o * o;
+    const long long ov = (long long)o * v;
+    const long long npair = (long long)v * (v + 1) / 2;
+    const long long p0 = (blk - S.block0) * S.pairs_per_block;
+    const long long p1 = min(npair, p0 + S.pairs_per_block);
+    const double two_ebar = 2.0 * S.e_bar;
+    double acc = 0.0;
+    for (long long t = threadIdx.x; t < (p1 - p0) * oo; t += blockDim.x) {
+        const long long p = p0 + t / oo;
+        const int ij = (int)(t % oo), i = ij % o, j = ij / o;
+        int a, b;
+        pair_of(p, a, b);
+        const long long x_off = i + (long long)o * a + ov * j + ov * o * b;   // K[i,a,j,b]
+        const long long y_off = i + (long long)o * b + ov * j + ov * o * a;   // K[i,b,j,a]
+        const double inv = 1.0 / (S.eps[i] + S.eps[j] - S.eps[o + a] - S.eps[o + b]);
+        const double x = S.K[x_off];
+        if (a == b) {
+            acc = fma(x * x, inv, acc);
+            S.G[x_off] = two_ebar * x * inv;
+        } else {
+            const double y = S.K[y_off];
+            acc = fma(x * (2.0 * x - y) + y * (2.0 * y - x), inv, acc);
+            S.G[x_off] = two_ebar * (2.0 * x - y) * inv;
+            S.G[y_off] = two_ebar * (2.0 * y - x) * inv;
+        }
+    }
+    acc = block_total(acc);
+    if (threadIdx.x == 0) part[blk] = acc;
+}
+
+// one block per system: its blocks' partial energies added in block order (deterministic)
+__global__ void __launch_bounds__(256) mp2_energy_grouped(const SysDesc *__restrict__ sys,
+                                                          const double *__restrict__ part) {
+    const SysDesc &S = sys[blockIdx.x];
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < S.nblocks; k += blockDim.x) acc += part[S.block0 + k];
+    acc = block_total(acc);
+    if (threadIdx.x == 0) *S.e = acc;
+}
+
+// tile shape index kShapeTC: the grouped three-plane tcgen05 GEMM (gett_tc.cu)
+constexpr int kShapeTC = kNumTileShapes;
 
 struct Stage {
     std::vector<GroupProblem> probs;
+    std::vector<GettArgs> args;   // the same problems, for the grouped tcgen05 form
     DBuf<GroupProblem> dev;
+    TcGroup *tc = nullptr;        // built when the batch runs split precision and every K <= 64
     long long total = 0;
     int shape = 0;
     std::string name;
+    Stage() = default;
+    Stage(Stage &&o) noexcept
+        : probs(std::move(o.probs)), args(std::move(o.args)), dev(std::move(o.dev)), tc(o.tc), total(o.total),
+          shape(o.shape), name(std::move(o.name)) {
+        o.tc = nullptr;
+    }
+    Stage &operator=(Stage &&) = delete;
+    ~Stage() { tc_group_destroy(tc); }
 };
 
 }  // namespace
@@ -78,7 +142,8 @@ struct BatchPlan {
     std::vector<int> n, o;
     std::vector<Stage> stages;      // grouped GETT stages in order; energy runs after stage 4
     DBuf<SysDesc> sys;
-    DBuf<double> energies;
+    DBuf<double> energies, epart;
+    long long gamma_blocks = 0;
     int n_forward = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -95,15 +160,26 @@ struct BatchCache {
 
 void batch_cache_destroy(BatchCache *c) { delete c; }
 
+static void run_stage(Ctx *ctx, Stage &st) {
+    if (st.shape == kShapeTC)
+        tc_group_run(ctx, st.tc);
+    else
+        gett_f64_grouped_launch(ctx, st.dev.p, (int)st.probs.size(), st.total, st.shape, st.name.c_str());
+}
+
+static void run_gamma(Ctx *ctx, BatchPlan &bp) {
+    Ctx::Scope s(ctx, "batch_mp2_gamma");
+    mp2_gamma_grouped<<<(unsigned)bp.gamma_blocks, 256, 0, ctx->stream>>>(bp.sys.p, (int)bp.n.size(), bp.epart.p);
+    JUES_CHECK_CUDA(cudaGetLastError());
+    mp2_energy_grouped<<<(unsigned)bp.n.size(), 256, 0, ctx->stream>>>(bp.sys.p, bp.epart.p);
+    ctx->count_launch();
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
 static void run_stages(Ctx *ctx, BatchPlan &bp) {
     for (size_t k = 0; k < bp.stages.size(); ++k) {
-        Stage &st = bp.stages[k];
-        gett_f64_grouped_launch(ctx, st.dev.p, (int)st.probs.size(), st.total, st.shape, st.name.c_str());
-        if ((int)k + 1 == bp.n_forward) {
-            Ctx::Scope s(ctx, "batch_mp2_gamma");
-            mp2_gamma_grouped<<<(unsigned)bp.n.size(), 256, 0, ctx->stream>>>(bp.sys.p);
-            JUES_CHECK_CUDA(cudaGetLastError());
-        }
+        run_stage(ctx, bp.stages[k]);
+        if ((int)k + 1 == bp.n_forward) run_gamma(ctx, bp);
     }
 }
 
@@ -123,13 +199,16 @@ static void autotune(Ctx *ctx, BatchPlan &bp) {
         Stage &st = bp.stages[k];
         float best = -1.f;
         int best_shape = 0;
-        for (int sh = 0; sh < kNumTileShapes; ++sh) {
+        // the FP64 tile shapes, and the grouped tcgen05 form where it was built
+        const int first = (ctx->batch_form == 2 && st.tc) ? kShapeTC : 0;
+        const int last = (st.tc && ctx->batch_form != 1) ? kShapeTC : kNumTileShapes - 1;
+        for (int sh = first; sh <= last; ++sh) {
             st.shape = sh;
-            upload_stage(ctx, st);
+            if (sh != kShapeTC) upload_stage(ctx, st);
             // warm once, then time
-            gett_f64_grouped_launch(ctx, st.dev.p, (int)st.probs.size(), st.total, sh, st.name.c_str());
+            run_stage(ctx, st);
             JUES_CHECK_CUDA(cudaEventRecord(e0, ctx->stream));
-            gett_f64_grouped_launch(ctx, st.dev.p, (int)st.probs.size(), st.total, sh, st.name.c_str());
+            run_stage(ctx, st);
             JUES_CHECK_CUDA(cudaEventRecord(e1, ctx->stream));
             JUES_CHECK_CUDA(cudaEventSynchronize(e1));
             float ms = 0.f;
@@ -137,20 +216,17 @@ static void autotune(Ctx *ctx, BatchPlan &bp) {
             if (best < 0 || ms < best) { best = ms; best_shape = sh; }
         }
         st.shape = best_shape;
-        upload_stage(ctx, st);
+        if (st.shape != kShapeTC) upload_stage(ctx, st);
         // stages read what earlier stages wrote: run this one for real before tuning the next
-        gett_f64_grouped_launch(ctx, st.dev.p, (int)st.probs.size(), st.total, st.shape, st.name.c_str());
-        if ((int)k + 1 == bp.n_forward) {
-            mp2_gamma_grouped<<<(unsigned)bp.n.size(), 256, 0, ctx->stream>>>(bp.sys.p);
-            JUES_CHECK_CUDA(cudaGetLastError());
-        }
+        run_stage(ctx, st);
+        if ((int)k + 1 == bp.n_forward) run_gamma(ctx, bp);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
 }
 
 static std::unique_ptr<BatchPlan> make_plan(Ctx *ctx, const std::string &key, int nsys, const jues_mp2_system *sys,
-                                            double e_bar, bool want_gb, bool want_cb) {
+                                            double e_bar, bool want_gb, bool want_cb, bool split) {
     std::unique_ptr<BatchPlan> bp(new BatchPlan());
     bp->key = key;
     struct Off {
@@ -205,14 +281,26 @@ static std::unique_ptr<BatchPlan> make_plan(Ctx *ctx, const std::string &key, in
             int d[4] = {o, v, o, v};
             long long ostr[4] = {1, o, ov, ov * o};
             auto st = transform4_plan(A + f.g, n, Cs, d, A + f.K, ostr, A + f.b0, A + f.b1);
-            for (int k = 0; k < 4; ++k) fwd[k].probs.push_back(to_problem(st[k]));
+            for (int k = 0; k < 4; ++k) {
+                fwd[k].probs.push_back(to_problem(st[k]));
+                fwd[k].args.push_back(st[k]);
+            }
         }
-        descs[s] = SysDesc{A + f.K, A + f.eps, A + f.G, bp->energies.p + s, o, v, e_bar};
+        {
+            const long long npair = (long long)v * (v + 1) / 2;
+            const int ppb = std::max(1, 2048 / (o * o));
+            const int nb = (int)((npair + ppb - 1) / ppb);
+            descs[s] = SysDesc{A + f.K, A + f.eps, A + f.G, bp->energies.p + s, o, v, e_bar, bp->gamma_blocks, nb, ppb};
+            bp->gamma_blocks += nb;
+        }
         if (want_gb) {
             const double *Cs[4] = {Co, Cv, Co, Cv};
             int d[4] = {o, v, o, v};
             auto st = backtransform4_plan(A + f.G, d, n, Cs, A + f.gb, A + f.b0, A + f.b1);
-            for (int k = 0; k < 4; ++k) bwd[k].probs.push_back(to_problem(st[k]));
+            for (int k = 0; k < 4; ++k) {
+                bwd[k].probs.push_back(to_problem(st[k]));
+                bwd[k].args.push_back(st[k]);
+            }
         }
         if (want_cb) {
             // H = (mu a|j b) with scratch b0/b1 and H' = (i nu|j b) with scratch b2/b3: step k of
@@ -229,6 +317,8 @@ static std::unique_ptr<BatchPlan> make_plan(Ctx *ctx, const std::string &key, in
             for (int k = 0; k < 3; ++k) {
                 third[k].probs.push_back(to_problem(h[k]));
                 third[k].probs.push_back(to_problem(hp[k]));
+                third[k].args.push_back(h[k]);
+                third[k].args.push_back(hp[k]);
             }
             GettArgs a;   // dE/dC[mu,i] = 2 sum_{ajb} H[mu,(ajb)] G[i,(ajb)]
             a.M = n; a.N = o; a.K = ov * v;
@@ -238,6 +328,7 @@ static std::unique_ptr<BatchPlan> make_plan(Ctx *ctx, const std::string &key, in
             a.C = A + f.cb; a.mC = plain(1); a.nC = plain(n);
             a.Cin = nullptr;
             fin[0].probs.push_back(to_problem(a));
+            fin[0].args.push_back(a);
             GettArgs b;   // dE/dC[nu,a] = 2 sum_{ijb} H'[i,nu,j,b] G[i,a,j,b]
             b.M = n; b.N = v; b.K = (long long)o * o * v;
             b.alpha = 2.0; b.beta = 0.0;
@@ -246,6 +337,7 @@ static std::unique_ptr<BatchPlan> make_plan(Ctx *ctx, const std::string &key, in
             b.C = A + f.cb + (size_t)n * o; b.mC = plain(1); b.nC = plain(n);
             b.Cin = nullptr;
             fin[0].probs.push_back(to_problem(b));
+            fin[0].args.push_back(b);
         }
     }
     for (auto &st : fwd) { st.name = "batch_transform"; bp->stages.push_back(std::move(st)); }
@@ -258,20 +350,29 @@ static std::unique_ptr<BatchPlan> make_plan(Ctx *ctx, const std::string &key, in
         bp->stages.push_back(std::move(fin[0]));
     }
     bp->sys = DBuf<SysDesc>(ctx, nsys);
+    bp->epart = DBuf<double>(ctx, (size_t)bp->gamma_blocks);
     JUES_CHECK_CUDA(cudaMemcpyAsync(bp->sys.p, descs.data(), nsys * sizeof(SysDesc), cudaMemcpyHostToDevice,
                                     ctx->stream));
+    // split precision: every stage whose contractions all have K <= 64 (every stage but the final
+    // dE/dC one when nbf <= 64) gets the grouped three-plane tcgen05 form as a tuning candidate
+    if (split)
+        for (Stage &st : bp->stages) st.tc = tc_group_build(ctx, st.args, (st.name + "_tc").c_str());
     return bp;
 }
 
-static std::string signature(int nsys, const jues_mp2_system *sys, double e_bar, bool gb, bool cb) {
-    std::string k = std::to_string(nsys) + (gb ? "G" : "g") + (cb ? "C" : "c") + std::to_string(e_bar);
+static std::string signature(int nsys, const jues_mp2_system *sys, double e_bar, bool gb, bool cb, bool split,
+                             int form) {
+    std::string k = std::to_string(nsys) + (gb ? "G" : "g") + (cb ? "C" : "c") + (split ? "S" : "D") +
+                    std::to_string(form) + "," + std::to_string(e_bar);
     for (int s = 0; s < nsys; ++s) k += "," + std::to_string(sys[s].n) + ":" + std::to_string(sys[s].o);
     return k;
 }
 
-void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, double *e_out, double **gao_bar,
-                double **C_bar, jues_batch_info *info) {
+void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, int precision, double e_bar, double *e_out,
+                double **gao_bar, double **C_bar, jues_batch_info *info) {
     JUES_REQUIRE(nsys > 0, "nsys must be positive");
+    JUES_REQUIRE(valid_precision(precision), "unknown precision");
+    const bool split = is_split(precision);
     for (int s = 0; s < nsys; ++s) {
         JUES_REQUIRE(sys[s].gao && sys[s].C && sys[s].eps, "null pointer in a batch system");
         JUES_REQUIRE(sys[s].n > 0 && sys[s].o > 0 && sys[s].o < sys[s].n, "batch system needs 0 < nocc < nbf");
@@ -282,12 +383,12 @@ void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, do
         want_cb = want_cb || (C_bar && C_bar[s]);
     }
     if (!ctx->batch) ctx->batch = new BatchCache();
-    const std::string key = signature(nsys, sys, e_bar, want_gb, want_cb);
+    const std::string key = signature(nsys, sys, e_bar, want_gb, want_cb, split, ctx->batch_form);
     auto it = ctx->batch->plans.find(key);
     bool fresh = false;
     if (it == ctx->batch->plans.end()) {
         ctx->batch->plans.clear();   // one resident plan per context keeps memory bounded
-        it = ctx->batch->plans.emplace(key, make_plan(ctx, key, nsys, sys, e_bar, want_gb, want_cb)).first;
+        it = ctx->batch->plans.emplace(key, make_plan(ctx, key, nsys, sys, e_bar, want_gb, want_cb, split)).first;
         fresh = true;
     }
     BatchPlan &bp = *it->second;

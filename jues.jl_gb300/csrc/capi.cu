@@ -163,6 +163,8 @@ void check_opts(const jues_cc_opts &o) {
     if (o.refine < 0) throw Error(JUES_EINVAL, "refine must be >= 0");
     if (o.transform_precision != -1 && !valid_precision(o.transform_precision))
         throw Error(JUES_EINVAL, "unknown transform_precision");
+    if (o.ccsd_fae != JUES_CCSD_FAE_RCCSD && o.ccsd_fae != JUES_CCSD_FAE_MRCCSD)
+        throw Error(JUES_EINVAL, "unknown ccsd_fae variant");
 }
 
 }  // namespace
@@ -472,7 +474,7 @@ int jues_df_rmp2(jues_ctx *ctx, const double *pqP, int n, int naux, const double
             a.A = bia.p; a.mA = plain(1); a.kA = plain(ov);
             a.B = bia.p; a.kB = plain(ov); a.nB = plain(1);
             a.C = K.p; a.mC = plain(1); a.nC = plain(ov);
-            gett(&c, precision, a, "df_iajb");
+            gett(&c, integral_precision(precision), a, "df_iajb");
         }
         *e_out = mp2_gamma(&c, K.p, de.p, o, v, 1.0, nullptr);   // DF-RMP2.jl:36-42
         c.check_flags();
@@ -528,7 +530,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
                 a.A = H.p; a.mA = plain(1); a.kA = plain(n);
                 a.B = G.p; a.kB = plain(o); a.nB = plain(1);
                 a.C = cb.p; a.mC = plain(1); a.nC = plain(n);
-                gett(&c, precision, a, "adjoint_cocc");
+                gett(&c, integral_precision(precision), a, "adjoint_cocc");
             }
             {
                 // H'[i,nu,j,b] = (i nu|j b); dE/dC[nu,a] = 2 sum_{ijb} H'[i,nu,j,b] G[i,a,j,b]
@@ -543,7 +545,7 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
                 a.A = H.p; a.mA = plain(o); a.kA = mode3(o, o, 1, (long long)o * n, (long long)o * n * o);
                 a.B = G.p; a.kB = mode3(o, o, 1, ov, ov * o); a.nB = plain(o);
                 a.C = cb.p + (size_t)n * o; a.mC = plain(1); a.nC = plain(n);
-                gett(&c, precision, a, "adjoint_cvir");
+                gett(&c, integral_precision(precision), a, "adjoint_cvir");
             }
             d2h(c, C_bar, cb.p, cb.n);
         }
@@ -552,14 +554,22 @@ int jues_rmp2_adjoint(jues_ctx *ctx, const double *gao, int n, const double *C, 
     });
 }
 
-int jues_batch_rmp2(jues_ctx *ctx, int nsys, const jues_mp2_system *systems, double e_bar, double *e_out,
-                    double **gao_bar, double **C_bar, jues_batch_info *info) {
+int jues_ctx_set_batch_form(jues_ctx *ctx, int form) {
+    return guarded([&] {
+        Ctx &c = CX(ctx);
+        if (form < 0 || form > 2) throw Error(JUES_EINVAL, "batch form must be 0, 1 or 2");
+        c.batch_form = form;
+    });
+}
+
+int jues_batch_rmp2(jues_ctx *ctx, int nsys, const jues_mp2_system *systems, int precision, double e_bar,
+                    double *e_out, double **gao_bar, double **C_bar, jues_batch_info *info) {
     return guarded([&] {
         Ctx &c = CX(ctx);
         need(systems, "systems");
         need(e_out, "e_out");
         cudaSetDevice(c.device);
-        batch_rmp2(&c, nsys, systems, e_bar, e_out, gao_bar, C_bar, info);
+        batch_rmp2(&c, nsys, systems, precision, e_bar, e_out, gao_bar, C_bar, info);
     });
 }
 
@@ -575,6 +585,7 @@ int jues_cc_default_opts(jues_cc_opts *opts) {
         opts->guess = JUES_GUESS_ZERO;   // mRCCD.jl:245
         opts->refine = 2;
         opts->transform_precision = -1;
+        opts->ccsd_fae = JUES_CCSD_FAE_RCCSD;
     });
 }
 

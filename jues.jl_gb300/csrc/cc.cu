@@ -299,7 +299,6 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         s->t1 = DBuf<double>(ctx, (size_t)ov);
         s->t1n = DBuf<double>(ctx, (size_t)ov);
         s->Fme = DBuf<double>(ctx, (size_t)ov);
-        s->Wabef = DBuf<double>(ctx, (size_t)(vv * vv));
         fill(ctx, s->t1.p, (size_t)ov, 0.0);
     }
     // initial amplitudes
@@ -568,7 +567,15 @@ namespace jues {
 
 // ---------------------------------------------------------------------------------------
 // CCSD sweep (RCCSD.jl:150-289 on the six blocks of mRCCSD.jl:102-110).
-// Work buffers: Tt = t~(T2 + tau/2) for Fae/Fmi, then t~(T2); aux1 = T2 + tau; tau; Wabef.
+// Work buffers: Tt = t~(T2 + tau/2) for Fae/Fmi, then t~(T2); aux1 = T2 + tau; tau; aux2 = the
+// o^3 v intermediates.  Wabef is never formed: its vvvv part is the particle ladder on the
+// resident (cached) vvvv, its t1 parts go through Y[ij,a,m] = sum_ef Ttau[ij,ef] <am|ef>
+// (2 o^3 v^3 instead of forming and re-reading a v^4 array every sweep):
+//   sum_ef Ttau[ij,ef] (-t1[m,b] <am|ef> - t1[m,a] <mb|ef>) = -sum_m t1[m,b] Y[ij,a,m] - (image),
+// the second term being the (i,a) <-> (j,b) image of the first (<mb|ef> = <bm|fe> and
+// Ttau[ij,ef] = Ttau[ji,fe]), so only the first goes into Z.
+// Every contraction runs in the sweep's precision; the split engine keeps the ones with a
+// dimension below 16 in FP64 by itself.
 // ---------------------------------------------------------------------------------------
 double ccsd_sweep(CCState *s, int prec) {
     Ctx *ctx = s->ctx;
@@ -579,7 +586,11 @@ double ccsd_sweep(CCState *s, int prec) {
                  *ovov = s->ovov.p;
     if (s->tau.n < t2n) s->tau = DBuf<double>(ctx, t2n);
     if (s->aux1.n < t2n) s->aux1 = DBuf<double>(ctx, t2n);
+    if (s->aux2.n < (size_t)(ooo * v)) s->aux2 = DBuf<double>(ctx, (size_t)(ooo * v));
     double *tau = s->tau.p, *Ttau = s->aux1.p;
+    // T2 + tau is rewritten below and then only read in this sweep: its packs are shared between
+    // the GEMMs that read it in the same layout (the particle ladder, X and Y)
+    pack_cache_drop(ctx, Ttau);
     // tau[m,n,a,f] = t1[m,a] t1[n,f]: outer product as a K=1 GEMM over (m,a) x (n,f)
     G(s, JUES_PREC_FP64, "ccsd_tau", ov, ov, 1, 1.0, t1, plain(1), plain(0), t1, plain(0), plain(1), 0.0,
       tau, mode2(o, 1, oo), mode2(o, o, oov));
@@ -592,14 +603,17 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(oo), 0.0, s->Fae.p, plain(1), plain(v));
     G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, 2.0, ovvv, mode2(v, o, ovv), mode2(o, 1, ov), t1,
       plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0));
-    G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, -1.0, ovvv, mode2(v, o, ov), mode2(o, 1, ovv), t1,
+    // the exchange part: t1[m,f] <ma|ef> = ovvv[m,a,e,f] (RCCSD.jl:190), or t1[m,f] <me|af> =
+    // ovvv[m,e,a,f] (mRCCSD.jl:140)
+    const Mode fae_rows = s->opts.ccsd_fae == JUES_CCSD_FAE_MRCCSD ? mode2(v, ov, o) : mode2(v, o, ov);
+    G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, -1.0, ovvv, fae_rows, mode2(o, 1, ovv), t1,
       plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0));
     // Fmi (RCCSD.jl:195-203)
     G(s, prec, "ccsd_fmi", o, o, o * vv, 1.0, W, plain(1), plain(o), s->Tt.p, plain(o), plain(1), 0.0,
       s->Fmi.p, plain(1), plain(o));
-    G(s, JUES_PREC_FP64, "ccsd_fmi_t1", oo, 1, ov, 2.0, ooov, mode2(o, 1, oo), mode2(o, o, ooo), t1,
+    G(s, prec, "ccsd_fmi_t1", oo, 1, ov, 2.0, ooov, mode2(o, 1, oo), mode2(o, o, ooo), t1,
       plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0));
-    G(s, JUES_PREC_FP64, "ccsd_fmi_t1", oo, 1, ov, -1.0, ooov, mode2(o, o, oo), mode2(o, 1, ooo), t1,
+    G(s, prec, "ccsd_fmi_t1", oo, 1, ov, -1.0, ooov, mode2(o, o, oo), mode2(o, 1, ooo), t1,
       plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0));
     // Fme (RCCSD.jl:204-210)
     G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
@@ -610,31 +624,26 @@ double ccsd_sweep(CCState *s, int prec) {
         // non-canonical Fock terms: Fae += f_ae - 1/2 f_me t1[m,a], Fmi += f_mi + 1/2 t1[i,e] f_me,
         // Fme += f_me (the diagonals of f_oo and f_vv are zero; they sit in the resolvents)
         axpby(ctx, (size_t)vv, 1.0, s->fVV.p, 1.0, s->Fae.p, s->Fae.p);
-        G(s, JUES_PREC_FP64, "ccsd_fock", v, v, o, -0.5, t1, plain(o), plain(1), s->fOV.p, plain(1), plain(o),
+        G(s, prec, "ccsd_fock", v, v, o, -0.5, t1, plain(o), plain(1), s->fOV.p, plain(1), plain(o),
           1.0, s->Fae.p, plain(1), plain(v));
         axpby(ctx, (size_t)oo, 1.0, s->fOO.p, 1.0, s->Fmi.p, s->Fmi.p);
-        G(s, JUES_PREC_FP64, "ccsd_fock", o, o, v, 0.5, s->fOV.p, plain(1), plain(o), t1, plain(o), plain(1),
+        G(s, prec, "ccsd_fock", o, o, v, 0.5, s->fOV.p, plain(1), plain(o), t1, plain(o), plain(1),
           1.0, s->Fmi.p, plain(1), plain(o));
         axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, s->Fme.p, s->Fme.p);
     }
 
     // W' = oooo + t1[j,e] ooov[m,n,i,e] + t1[i,e] ooov[n,m,j,e] + sum_ef oovv[mn,ef] (T2+tau)[ij,ef]
-    G(s, JUES_PREC_FP64, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
+    G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
       plain(1), 1.0, s->Wp.p, plain(1), plain(ooo), s->oooo.p);
-    G(s, JUES_PREC_FP64, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
+    G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
       plain(1), 1.0, s->Wp.p, mode3(o, o, o, 1, ooo), plain(oo));
     G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
-      plain(1), plain(oo));
-    // Wabef without its T2 part: vvvv - t1[m,b] <am|ef> - t1[m,a] <mb|ef>  (<am|ef> = ovvv[m,a,f,e])
-    G(s, prec, "ccsd_wabef_t1", v * vv, v, o, -1.0, ovvv, mode3(v, v, o, ovv, ov), plain(1), t1, plain(1),
-      plain(o), 1.0, s->Wabef.p, mode3(v, v, 1, vv, v * vv), plain(v), s->vvvv.p);
-    G(s, prec, "ccsd_wabef_t1", v * vv, v, o, -1.0, ovvv, mode3(v, v, o, ov, ovv), plain(1), t1, plain(1),
-      plain(o), 1.0, s->Wabef.p, mode3(v, v, v, vv, v * vv), plain(1));
-    // L = oovv + W'^T (T2+tau) + (T2+tau) Wabef^T
+      plain(1), plain(oo), nullptr, false, true);
+    // L = oovv + W'^T (T2+tau) + (T2+tau) vvvv^T  (Wabef's t1 parts go through Y below)
     G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
       1.0, s->L.p, plain(1), plain(oo), W);
-    G(s, prec, "ccsd_pp_ladder", oo, vv, vv, 1.0, Ttau, plain(1), plain(oo), s->Wabef.p, plain(vv),
-      plain(1), 1.0, s->L.p, plain(1), plain(oo));
+    G(s, prec, "ccsd_pp_ladder", oo, vv, vv, 1.0, Ttau, plain(1), plain(oo), s->vvvv.p, plain(vv),
+      plain(1), 1.0, s->L.p, plain(1), plain(oo), nullptr, true, true);
 
     // ring intermediates; T~ of T2 alone from here on
     t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
@@ -646,32 +655,32 @@ double ccsd_sweep(CCState *s, int prec) {
       mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
     G(s, prec, "ccsd_wj", ov, ov, ov, -1.0, W, mode2(o, 1, oo), mode2(o, o, oov), tau, mode2(o, o, oo),
       mode2(v, oov, 1), 1.0, s->WJ.p, plain(1), plain(ov));
-    G(s, JUES_PREC_FP64, "ccsd_wj_t1", ovv, o, v, 1.0, ovvv, mode3(o, v, 1, ov, o), plain(ovv), t1,
+    G(s, prec, "ccsd_wj_t1", ovv, o, v, 1.0, ovvv, mode3(o, v, 1, ov, o), plain(ovv), t1,
       plain(o), plain(1), 1.0, s->WJ.p, mode3(o, v, 1, o, ov), plain(ovv));
-    G(s, JUES_PREC_FP64, "ccsd_wj_t1", ov * o, v, o, -1.0, ooov, mode3(o, v, o, ooo, oo), plain(1), t1,
+    G(s, prec, "ccsd_wj_t1", ov * o, v, o, -1.0, ooov, mode3(o, v, o, ooo, oo), plain(1), t1,
       plain(1), plain(o), 1.0, s->WJ.p, mode3(o, v, 1, o, ovv), plain(ov));
     // WK = WmBEj (RCCSD.jl:239-247 with <bm|ej> = ovov[m,b,j,e], <nm|ej> = ooov[m,n,j,e])
     G(s, prec, "ccsd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
       mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p);
     G(s, prec, "ccsd_wk", ov, ov, ov, 1.0, W, mode2(o, o, oo), mode2(o, 1, oov), tau, mode2(o, o, oo),
       mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov));
-    G(s, JUES_PREC_FP64, "ccsd_wk_t1", ovv, o, v, -1.0, ovvv, mode3(o, v, 1, ovv, o), plain(ov), t1,
+    G(s, prec, "ccsd_wk_t1", ovv, o, v, -1.0, ovvv, mode3(o, v, 1, ovv, o), plain(ov), t1,
       plain(o), plain(1), 1.0, s->WK.p, mode3(o, v, 1, o, ov), plain(ovv));
-    G(s, JUES_PREC_FP64, "ccsd_wk_t1", ov * o, v, o, 1.0, ooov, mode3(o, v, 1, ooo, oo), plain(o), t1,
+    G(s, prec, "ccsd_wk_t1", ov * o, v, o, 1.0, ooov, mode3(o, v, 1, ooo, oo), plain(o), t1,
       plain(1), plain(o), 1.0, s->WK.p, mode3(o, v, 1, o, ovv), plain(ov));
     axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
 
     // T1 (RCCSD.jl:248-259) into t1n, before the amplitudes change
     double *R1 = s->t1n.p;
-    G(s, JUES_PREC_FP64, "ccsd_t1", o, v, v, 1.0, t1, plain(1), plain(o), s->Fae.p, plain(v), plain(1),
+    G(s, prec, "ccsd_t1", o, v, v, 1.0, t1, plain(1), plain(o), s->Fae.p, plain(v), plain(1),
       0.0, R1, plain(1), plain(o));
-    G(s, JUES_PREC_FP64, "ccsd_t1", o, v, o, -1.0, s->Fmi.p, plain(o), plain(1), t1, plain(1), plain(o),
+    G(s, prec, "ccsd_t1", o, v, o, -1.0, s->Fmi.p, plain(o), plain(1), t1, plain(1), plain(o),
       1.0, R1, plain(1), plain(o));
-    G(s, JUES_PREC_FP64, "ccsd_t1", ov, 1, ov, 1.0, Tt, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
+    G(s, prec, "ccsd_t1", ov, 1, ov, 1.0, Tt, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
       plain(1), plain(0), 1.0, R1, plain(1), plain(0));
-    G(s, JUES_PREC_FP64, "ccsd_t1", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
+    G(s, prec, "ccsd_t1", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
       plain(0), 1.0, R1, plain(1), plain(0));
-    G(s, JUES_PREC_FP64, "ccsd_t1", ov, 1, ov, -1.0, ovov, mode2(o, ov, o), mode2(o, 1, oov), t1,
+    G(s, prec, "ccsd_t1", ov, 1, ov, -1.0, ovov, mode2(o, ov, o), mode2(o, 1, oov), t1,
       plain(1), plain(0), 1.0, R1, plain(1), plain(0));
     G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, ooov, plain(oo), mode2(oo, 1, ooo), Tt,
       mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o));
@@ -679,15 +688,22 @@ double ccsd_sweep(CCState *s, int prec) {
       mode3(o, v, 1, ovv, ov), plain(o), 1.0, R1, plain(1), plain(o));
 
     // F~ae[b,e] = Fae - 1/2 t1[m,b] Fme[m,e];  F~mi[m,j] = Fmi + 1/2 Fme[m,e] t1[j,e]
-    G(s, JUES_PREC_FP64, "ccsd_ftilde", v, v, o, -0.5, t1, plain(o), plain(1), s->Fme.p, plain(1),
+    G(s, prec, "ccsd_ftilde", v, v, o, -0.5, t1, plain(o), plain(1), s->Fme.p, plain(1),
       plain(o), 1.0, s->Fae.p, plain(1), plain(v));
-    G(s, JUES_PREC_FP64, "ccsd_ftilde", o, o, v, 0.5, s->Fme.p, plain(1), plain(o), t1, plain(o),
+    G(s, prec, "ccsd_ftilde", o, o, v, 0.5, s->Fme.p, plain(1), plain(o), t1, plain(o),
       plain(1), 1.0, s->Fmi.p, plain(1), plain(o));
 
     // Z (RCCSD.jl:264-284, one member of each (i,a)<->(j,b) pair)
     double *Z = s->Z.p;
     G(s, prec, "ccsd_z_fae", oov, v, v, 1.0, T, plain(1), plain(oov), s->Fae.p, plain(v), plain(1), 0.0,
       Z, plain(1), plain(oov));
+    // Wabef's t1 parts: Y[ij,(a,m)] = sum_ef Ttau[i,j,e,f] <am|ef> (<am|ef> = ovvv[m,a,f,e]), then
+    // Z[i,j,a,b] -= sum_m Y[ij,a,m] t1[m,b]
+    double *Y = s->aux2.p;
+    G(s, prec, "ccsd_y", oo, ov, vv, 1.0, Ttau, plain(1), plain(oo), ovvv, mode2(v, ovv, ov), mode2(v, o, 1),
+      0.0, Y, plain(1), plain(oo), nullptr, true, true);
+    G(s, prec, "ccsd_y_t1", oov, v, o, -1.0, Y, plain(1), plain(oov), t1, plain(1), plain(o), 1.0, Z,
+      plain(1), plain(oov));
     G(s, prec, "ccsd_z_fmi", o * vv, o, o, -1.0, T, mode2(o, 1, oo), plain(o), s->Fmi.p, plain(1),
       plain(o), 1.0, Z, mode2(o, 1, oo), plain(o));
     G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
@@ -697,22 +713,20 @@ double ccsd_sweep(CCState *s, int prec) {
     G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
       plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
     // - tau[i,m,e,a] <mb|ej>: Y1[i,m,j,b] = sum_e t1[i,e] oovv[m,j,e,b]; Z -= sum_m t1[m,a] Y1[i,m,j,b]
-    if (s->aux2.n < (size_t)(ooo * v)) s->aux2 = DBuf<double>(ctx, (size_t)(ooo * v));
-    double *Y = s->aux2.p;
-    G(s, JUES_PREC_FP64, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo),
+    G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo),
       mode3(o, o, 1, o, oov), 0.0, Y, plain(1), plain(o));
-    G(s, JUES_PREC_FP64, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, o, 1, oo, ooo), plain(o), t1,
+    G(s, prec, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, o, 1, oo, ooo), plain(o), t1,
       plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
     // - tau[i,m,e,b] <am|ej>: Y2[i,m,a,j] = sum_e t1[i,e] ovov[m,a,j,e]; Z -= sum_m Y2 t1[m,b]
-    G(s, JUES_PREC_FP64, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov),
+    G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov),
       plain(1), 0.0, Y, plain(1), plain(o));
-    G(s, JUES_PREC_FP64, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, v, 1, oo, oov), plain(o), t1,
+    G(s, prec, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, v, 1, oo, oov), plain(o), t1,
       plain(1), plain(o), 1.0, Z, mode3(o, v, 1, oo, o), plain(oov));
     // + t1[i,e] <ab|ej> = t1[i,e] ovvv[j,a,b,e]
     G(s, prec, "ccsd_z_ovvv", o, ovv, v, 1.0, t1, plain(1), plain(o), ovvv, plain(ovv), plain(1), 1.0, Z,
       plain(1), plain(o));
     // - t1[m,a] <mb|ij> = t1[m,a] ooov[m,j,i,b]
-    G(s, JUES_PREC_FP64, "ccsd_z_ooov", oov, v, o, -1.0, ooov, mode3(o, o, oo, o, ooo), plain(1), t1,
+    G(s, prec, "ccsd_z_ooov", oov, v, o, -1.0, ooov, mode3(o, o, oo, o, ooo), plain(1), t1,
       plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
 
     if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia

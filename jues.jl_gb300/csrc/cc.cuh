@@ -20,7 +20,6 @@ struct CCState {
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;
     DBuf<double> t1, t1n, Fme, tau;         // CCSD
-    DBuf<double> Wabef;                     // CCSD: vvvv + t1 terms
     DBuf<double> aux1, aux2;                // CCSD scratch
     // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
     std::vector<DBuf<double>> dv, de;

@@ -110,6 +110,8 @@ struct Ctx {
     // the split forms can pack host operands without a device copy (jues_ctx_set_ao_direct)
     bool ao_direct = false;
     bool ao_direct_supported = false;
+    int batch_form = 0;   // batched form: 0 autotune, 1 FP64 tiles only, 2 tcgen05 where built
+                          // (jues_ctx_set_batch_form)
     Ctx();
     ~Ctx();
 
@@ -191,8 +193,17 @@ void gett_f64(Ctx *ctx, const GettArgs &g, const char *name);
 // split precision on tcgen05: np = 2 operand planes (hi, lo; JUES_PREC_SPLIT_BF16) or 3 (hi,
 // mid, lo; JUES_PREC_SPLIT3)
 void gett_tc(Ctx *ctx, const GettArgs &g, const char *name, int np = 2);
-inline bool is_split(int precision) { return precision == JUES_PREC_SPLIT_BF16 || precision == JUES_PREC_SPLIT3; }
+inline bool is_split(int precision) {
+    return precision == JUES_PREC_SPLIT || precision == JUES_PREC_SPLIT3 || precision == JUES_PREC_SPLIT2;
+}
 inline bool valid_precision(int precision) { return precision == JUES_PREC_FP64 || is_split(precision); }
+// Arithmetic of a contraction whose result is an integral (four-index transforms, get_eri blocks,
+// DF factors and blocks, the MP2 adjoint's back-transforms).  Their rounding enters every energy
+// directly (two planes gave MP2 -4.8e-6 Eh at nbf=200, three -2.9e-10), so the split form keeps
+// three planes there; JUES_PREC_SPLIT2 keeps two.
+inline int integral_precision(int precision) {
+    return precision == JUES_PREC_SPLIT ? JUES_PREC_SPLIT3 : precision;
+}
 // split-K epilogue: C[mC(m) + nC(n)] = alpha sum_s ws[s sstride + n ld + m] + beta Cin[...],
 // the partials summed in FP64 in split order (deterministic)
 void splitk_reduce(Ctx *ctx, const float *ws, int ks, long long sstride, long long ld, long long M, long long N,
@@ -202,6 +213,12 @@ void splitk_reduce(Ctx *ctx, const double *ws, int ks, long long sstride, long l
                    double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
                    const char *name);
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
+// Grouped three-plane split GEMM of many independent problems with K <= 64 (the batched form):
+// build once (null when some problem has K > 64), then run (capturable in a CUDA graph)
+struct TcGroup;
+TcGroup *tc_group_build(Ctx *ctx, const std::vector<GettArgs> &probs, const char *name);
+void tc_group_run(Ctx *ctx, TcGroup *g);
+void tc_group_destroy(TcGroup *g);
 // split GEMM that packs into a static device array instead of allocating (see gett_tc.cu)
 void gett_tc_noalloc(Ctx *ctx, const GettArgs &g);
 // one device wait that nothing completes: throws JUES_ETIMEOUT after the bounded wait expires
@@ -210,8 +227,8 @@ size_t gett_tc_noalloc_limit();
 void pack_cache_clear(Ctx *ctx);
 void pack_cache_destroy(PackCache *p);
 void batch_cache_destroy(BatchCache *p);
-void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, double e_bar, double *e_out, double **gao_bar,
-                double **C_bar, jues_batch_info *info);
+void batch_rmp2(Ctx *ctx, int nsys, const jues_mp2_system *sys, int precision, double e_bar, double *e_out,
+                double **gao_bar, double **C_bar, jues_batch_info *info);
 void pack_cache_drop(Ctx *ctx, const void *ptr);
 void pack_cache_forget(Ctx *ctx, const void *p, size_t bytes);   // on every free of device memory
 

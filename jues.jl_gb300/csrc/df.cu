@@ -17,7 +17,7 @@ DBuf<double> df_fit(Ctx *ctx, int prec, const double *pqP, int n, int naux, cons
     a.A = pqP; a.mA = plain(1); a.kA = plain(nn);
     a.B = Jpqh; a.kB = plain(1); a.nB = plain(naux);
     a.C = b.p; a.mC = plain(1); a.nC = plain(nn);
-    gett(ctx, prec, a, "df_fit");
+    gett(ctx, integral_precision(prec), a, "df_fit");
     return b;
 }
 
@@ -32,7 +32,7 @@ void df_mo_factor(Ctx *ctx, int prec, const double *b, int n, int naux, const do
         a.A = C1; a.mA = plain(n); a.kA = plain(1);
         a.B = b; a.kB = plain(1); a.nB = plain(n);
         a.C = half.p; a.mC = plain(1); a.nC = plain(d1);
-        gett(ctx, prec, a, "df_half");
+        gett(ctx, integral_precision(prec), a, "df_half");
     }
     // out[p,q,Q] = sum_nu half[p,nu,Q] C2[nu,q]; rows are the composite (p,Q)
     {
@@ -42,7 +42,7 @@ void df_mo_factor(Ctx *ctx, int prec, const double *b, int n, int naux, const do
         a.A = half.p; a.mA = mode2(d1, 1, (long long)d1 * n); a.kA = plain(d1);
         a.B = C2; a.kB = plain(1); a.nB = plain(n);
         a.C = out; a.mC = mode2(d1, 1, (long long)d1 * d2); a.nC = plain(d1);
-        gett(ctx, prec, a, "df_half");
+        gett(ctx, integral_precision(prec), a, "df_half");
     }
 }
 
@@ -77,7 +77,7 @@ void contract_q(Ctx *ctx, int prec, const double *X, long long xr, const double 
     a.A = X; a.mA = plain(1); a.kA = plain(xr);
     a.B = Y; a.kB = plain(yr); a.nB = plain(1);
     a.C = out; a.mC = mC; a.nC = nC;
-    gett(ctx, prec, a, name);
+    gett(ctx, integral_precision(prec), a, name);
 }
 }  // namespace
 

@@ -325,7 +325,7 @@ void gett_f64_grouped_launch(Ctx *ctx, const GroupProblem *d_probs, int nprob, l
 }
 
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name) {
-    if (precision == JUES_PREC_SPLIT_BF16)
+    if (precision == JUES_PREC_SPLIT || precision == JUES_PREC_SPLIT2)
         gett_tc(ctx, g, name, 2);
     else if (precision == JUES_PREC_SPLIT3)
         gett_tc(ctx, g, name, 3);

@@ -27,6 +27,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -229,6 +230,13 @@ struct TcArgs {
     float *tail_partial = nullptr;
 };
 
+// one problem of a grouped launch (see gett_tc_kernel)
+struct TcGroupProb {
+    TcArgs a;
+    int rowA, rowB;
+    long long item0;
+};
+
 // Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues MMAs, warps 2-9 drain TMEM (two
 // warps per 32-lane TMEM quarter, each owning half of the tile's columns).
 // The MMA warp restarts both accumulators every KC stages (one scaling chunk of KCH = KC * 64
@@ -389,9 +397,14 @@ __device__ __forceinline__ void tc_epilogue(const TcArgs &g, const uint64_t *acc
 }
 
 
-template <int BN, int STAGES, int KC, int NP>
+// GROUPED: the launch covers many independent problems (a batch), each with one K block
+// (K <= 64); item w is output tile w - item0 of the problem whose [item0, next item0) holds it,
+// its operand rows start at rowA / rowB of the concatenated planes that mapA / mapB describe, and
+// g.tiles is the launch's total item count.
+template <int BN, int STAGES, int KC, int NP, bool GROUPED>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    gett_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcArgs g) {
+    gett_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   const __grid_constant__ TcArgs g, const TcGroupProb *__restrict__ gp, int ngp) {
     using Cfg = TcCfg<BN, STAGES, KC, NP>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -410,7 +423,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // persistent: CTA b processes work items b, b + gridDim.x, ...; an item is one output tile
     // over one K split.  Stage and chunk counters run on across items, so the pipeline and the
     // TMEM buffers never drain between tiles.
-    const long long nitems = tc_nitems(g);
+    const long long nitems = GROUPED ? g.tiles : tc_nitems(g);
+    // the problem of item w, its tile and its operand row offsets
+    auto locate = [&](long long w, const TcArgs *&G, int &ra, int &rb) -> TcItem {
+        if constexpr (GROUPED) {
+            int lo = 0, hi = ngp - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (gp[mid].item0 <= w) lo = mid; else hi = mid - 1;
+            }
+            G = &gp[lo].a;
+            ra = gp[lo].rowA;
+            rb = gp[lo].rowB;
+            return tc_item(*G, w - gp[lo].item0, BN);
+        } else {
+            G = &g;
+            ra = rb = 0;
+            return tc_item(g, w, BN);
+        }
+    };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -441,7 +472,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             long long it = 0;   // stages issued by this CTA
             bool stop = false;
             for (long long w = blockIdx.x; w < nitems && !stop; w += gridDim.x) {
-                const TcItem I = tc_item(g, w, BN);
+                const TcArgs *G;
+                int ra, rb;
+                const TcItem I = locate(w, G, ra, rb);
                 for (int kb = 0; kb < I.nk; ++kb, ++it) {
                     const int s = (int)(it % STAGES);
                     const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
@@ -454,10 +487,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const int kx = (I.kb0 + kb) * TBK;
                     mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
 #pragma unroll
-                    for (int p = 0; p < NP; ++p) tma_load_3d(st + p * Cfg::A_BYTES, &mapA, &full[s], kx, I.m0, p);
+                    for (int p = 0; p < NP; ++p)
+                        tma_load_3d(st + p * Cfg::A_BYTES, &mapA, &full[s], kx, I.m0 + ra, p);
 #pragma unroll
                     for (int p = 0; p < NP; ++p)
-                        tma_load_3d(st + NP * Cfg::A_BYTES + p * Cfg::B_BYTES, &mapB, &full[s], kx, I.n0, p);
+                        tma_load_3d(st + NP * Cfg::A_BYTES + p * Cfg::B_BYTES, &mapB, &full[s], kx, I.n0 + rb, p);
                 }
             }
             // the last load into each slot has landed (immediate unless an abort cut the MMA
@@ -474,7 +508,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             long long it = 0, gc = 0;
             bool stop = false;
             for (long long w = blockIdx.x; w < nitems && !stop; w += gridDim.x) {
-                const TcItem I = tc_item(g, w, BN);
+                const TcArgs *G;
+                int ra, rb;
+                const TcItem I = locate(w, G, ra, rb);
                 for (int kb = 0; kb < I.nk; ++kb, ++it) {
                     const int buf = (int)(gc & 1);
                     const bool first = (kb % KC) == 0;
@@ -534,7 +570,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         long long gc = 0;
         bool ok = true;
         for (long long w = blockIdx.x; w < nitems; w += gridDim.x) {
-            const TcItem I = tc_item(g, w, BN);
+            const TcArgs *G;
+            int ra, rb;
+            const TcItem I = locate(w, G, ra, rb);
             const int nchunks = (I.nk + KC - 1) / KC;
             const int chunk0 = I.kb0 / KC;   // kper is a multiple of KC
             // every drain thread has finished the previous item's epilogue (which reads coloff)
@@ -544,15 +582,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (dt < BN) {
                 const long long n = (long long)I.n0 + dt;
-                coloff[dt] = n < g.N ? mode_off(g.nC, n) : -1;
+                coloff[dt] = n < G->N ? mode_off(G->nC, n) : -1;
             }
             uint64_t acc2[HB / 2];   // FP32 pairs (columns 2j, 2j+1)
 #pragma unroll
             for (int j = 0; j < HB / 2; ++j) acc2[j] = 0ull;
             const long long mrow = (long long)I.m0 + quarter * 32 + lane;
             // the scales of chunk c + 1 are loaded while chunk c drains
-            const int *pa = g.expA + (long long)chunk0 * g.expA_ld + mrow;
-            const int *pb = g.expB + (long long)chunk0 * g.expB_ld + I.n0 + (dt < BN ? dt : 0);
+            const int *pa = G->expA + (long long)chunk0 * G->expA_ld + mrow;
+            const int *pb = G->expB + (long long)chunk0 * G->expB_ld + I.n0 + (dt < BN ? dt : 0);
             int ea_cur = __ldg(pa), eb_cur = __ldg(pb);
             bool bad = false;
             for (int c = 0; c < nchunks; ++c, ++gc) {
@@ -563,8 +601,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         (eb_cur == INT_MIN || eb_cur < -126) ? 0.f : __int_as_float((eb_cur + 127) << 23);
                 int ea_next = 0, eb_next = 0;
                 if (c + 1 < nchunks) {
-                    ea_next = __ldg(pa + (long long)(c + 1) * g.expA_ld);
-                    eb_next = __ldg(pb + (long long)(c + 1) * g.expB_ld);
+                    ea_next = __ldg(pa + (long long)(c + 1) * G->expA_ld);
+                    eb_next = __ldg(pb + (long long)(c + 1) * G->expB_ld);
                 }
                 if (drain_bar_any(bad || *abort_flag != 0)) {
                     bad = true;
@@ -584,10 +622,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 eb_cur = eb_next;
                 // row factor 2^(e_row - 18) (times alpha when that is a power of two); the column
                 // factor comes from shared memory
-                const int er = ea - 18 + g.alpha_k;
+                const int er = ea - 18 + G->alpha_k;
                 const float rs = (ea == INT_MIN || er < -126)
                                      ? 0.f
-                                     : __int_as_float((er + 127) << 23 | (g.alpha_neg ? 0x80000000 : 0));
+                                     : __int_as_float((er + 127) << 23 | (G->alpha_neg ? 0x80000000 : 0));
                 const float2 *cs = reinterpret_cast<const float2 *>(colsc + buf * BN + half * HB);
                 const uint64_t rs2 = pk2f(rs, rs), k2 = pk2f(0.0009765625f, 0.0009765625f);
                 // 32 columns per round: the NP accumulator loads in flight, one wait; then per
@@ -622,38 +660,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (I.tail >= 0) {
                 // a split part of a tail tile: raw sums (alpha folded in when a power of two),
                 // [split][tail tile][column][row], a warp writing 32 consecutive floats
-                float *dst = g.tail_partial + (((long long)I.split * g.tail_tiles + I.tail) * BN + half * HB) * TBM +
+                float *dst = G->tail_partial + (((long long)I.split * G->tail_tiles + I.tail) * BN + half * HB) * TBM +
                              quarter * 32 + lane;
 #pragma unroll
                 for (int j = 0; j < HB / 2; ++j) {
                     dst[(long long)(2 * j) * TBM] = lo_f(acc2[j]);
                     dst[(long long)(2 * j + 1) * TBM] = hi_f(acc2[j]);
                 }
-            } else if (g.partial) {
+            } else if (G->partial) {
                 // raw partial sums, padded rows and columns included; a warp writes 32
                 // consecutive floats per column
-                const long long Mpad = g.mtiles * TBM, Npad = (g.tiles / g.mtiles) * BN;
-                float *dst = g.partial + ((long long)I.split * Npad + I.n0 + half * HB) * Mpad + mrow;
+                const long long Mpad = G->mtiles * TBM, Npad = (G->tiles / G->mtiles) * BN;
+                float *dst = G->partial + ((long long)I.split * Npad + I.n0 + half * HB) * Mpad + mrow;
 #pragma unroll
                 for (int j = 0; j < HB / 2; ++j) {
                     dst[(long long)(2 * j) * Mpad] = lo_f(acc2[j]);
                     dst[(long long)(2 * j + 1) * Mpad] = hi_f(acc2[j]);
                 }
-            } else if (mrow < g.M) {
-                const long long rowoff = mode_off(g.mC, mrow);
+            } else if (mrow < G->M) {
+                const long long rowoff = mode_off(G->mC, mrow);
                 const long long n1 = (long long)I.n0 + half * HB;
-                if (g.nC.d0 == MODE_BIG) {
-                    const ColsStrided cols{n1 * g.nC.s0, g.nC.s0, (int)max(-1LL, min((long long)HB, g.N - n1))};
-                    if (g.alpha_pow2)
-                        tc_epilogue<HB, true>(g, acc2, cols, rowoff);
+                if (G->nC.d0 == MODE_BIG) {
+                    const ColsStrided cols{n1 * G->nC.s0, G->nC.s0, (int)max(-1LL, min((long long)HB, G->N - n1))};
+                    if (G->alpha_pow2)
+                        tc_epilogue<HB, true>(*G, acc2, cols, rowoff);
                     else
-                        tc_epilogue<HB, false>(g, acc2, cols, rowoff);
+                        tc_epilogue<HB, false>(*G, acc2, cols, rowoff);
                 } else {
                     const ColsShared cols{coloff + half * HB};
-                    if (g.alpha_pow2)
-                        tc_epilogue<HB, true>(g, acc2, cols, rowoff);
+                    if (G->alpha_pow2)
+                        tc_epilogue<HB, true>(*G, acc2, cols, rowoff);
                     else
-                        tc_epilogue<HB, false>(g, acc2, cols, rowoff);
+                        tc_epilogue<HB, false>(*G, acc2, cols, rowoff);
                 }
             }
         }
@@ -753,21 +791,17 @@ __device__ __forceinline__ uint32_t half_pair(int a, int b) {
 // layouts free of bank conflicts and the 8-byte row pieces aligned
 constexpr int PACK_PITCH = PK / 2 + 2;
 
-// KFAST: the source's K index is unit-stride (else its row index is)
+// One pack block: rows [r0, r0 + 16) x K chunk [k0, k0 + 128) of one operand.  KFAST: the
+// source's K index is unit-stride (else its row index is).  The planes go to
+// dst[plane pstride + row Kld + k], the scales to rexp[(k0 / 128) rexp_ld + row].
 template <int NP, bool KFAST>
-__global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
-                                                         long long R, long long K, long long Rpad,
-                                                         long long Kpad, int *__restrict__ rexp,
-                                                         __half *__restrict__ dst) {
+__device__ __forceinline__ void pack_block(const double *__restrict__ src, const Mode &rmode, const Mode &kmode,
+                                           long long R, long long K, long long Kpad, long long r0, long long k0,
+                                           int *__restrict__ rexp, long long rexp_ld, __half *__restrict__ dst,
+                                           long long pstride, long long Kld) {
     __shared__ __align__(16) uint32_t outp[NP][PR][PACK_PITCH];
     __shared__ long long roff[PR], koff[PK];
     __shared__ int rowE[PR];
-    // consecutive blocks follow the source's unit-stride index, so the blocks resident at one
-    // time read long contiguous runs of it
-    // block counts < 2^31 (checked at launch): 32-bit index arithmetic
-    const unsigned kblocks = (unsigned)((Kpad + PK - 1) / PK), rblocks = (unsigned)(Rpad / PR);
-    const long long r0 = (long long)(KFAST ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
-    const long long k0 = (long long)(KFAST ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid < PR) {
         const long long r = r0 + tid;
@@ -808,7 +842,7 @@ __global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__rest
     __syncthreads();
     if (tid < PR) {
         const int E = rowE[tid];
-        rexp[(k0 / KCH) * Rpad + r0 + tid] = E == 0 ? INT_MIN : E - 1022;
+        rexp[(k0 / KCH) * rexp_ld + r0 + tid] = E == 0 ? INT_MIN : E - 1022;
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -829,9 +863,52 @@ __global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__rest
         const int seg = idx & 31, row = (idx >> 5) & (PR - 1), plane = idx >> 9;
         const long long k = k0 + 4 * seg;
         if (k >= Kpad) continue;   // the 64-wide tail of the last chunk (Kpad is a multiple of 64)
-        *reinterpret_cast<uint2 *>(dst + (size_t)plane * Rpad * Kpad + (size_t)(r0 + row) * Kpad + k) =
+        *reinterpret_cast<uint2 *>(dst + (size_t)plane * pstride + (size_t)(r0 + row) * Kld + k) =
             *reinterpret_cast<const uint2 *>(&outp[plane][row][2 * seg]);
     }
+}
+
+template <int NP, bool KFAST>
+__global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
+                                                         long long R, long long K, long long Rpad,
+                                                         long long Kpad, int *__restrict__ rexp,
+                                                         __half *__restrict__ dst) {
+    // consecutive blocks follow the source's unit-stride index, so the blocks resident at one
+    // time read long contiguous runs of it
+    // block counts < 2^31 (checked at launch): 32-bit index arithmetic
+    const unsigned kblocks = (unsigned)((Kpad + PK - 1) / PK), rblocks = (unsigned)(Rpad / PR);
+    const long long r0 = (long long)(KFAST ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
+    const long long k0 = (long long)(KFAST ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
+    pack_block<NP, KFAST>(src, rmode, kmode, R, K, Kpad, r0, k0, rexp, Rpad, dst, Rpad * Kpad, Kpad);
+}
+
+// Grouped form: many operands (one per problem of a batch) with one 64-wide K block each
+// (K <= 64), their rows concatenated into one set of planes [NP][rows][64] so that one tensor
+// map covers all of them.  Problem p's rows start at row0, its blocks at block0.
+struct PackProb {
+    const double *src;
+    Mode r, k;
+    long long R, K, Rpad, row0, block0;
+};
+template <int NP>
+__global__ void __launch_bounds__(256, 6) pack_grouped_kernel(const PackProb *__restrict__ probs, int nprob,
+                                                              long long rows_total, int *__restrict__ rexp,
+                                                              __half *__restrict__ dst) {
+    const long long b = blockIdx.x;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (probs[mid].block0 <= b) lo = mid; else hi = mid - 1;
+    }
+    const PackProb &P = probs[lo];
+    const long long r0 = (b - P.block0) * PR;
+    // the unit-stride choice is uniform over a block
+    if (P.k.s0 == 1 && P.k.d0 > 1)
+        pack_block<NP, true>(P.src, P.r, P.k, P.R, P.K, 64, r0, 0, rexp + P.row0, rows_total, dst + P.row0 * 64,
+                             rows_total * 64, 64);
+    else
+        pack_block<NP, false>(P.src, P.r, P.k, P.R, P.K, 64, r0, 0, rexp + P.row0, rows_total, dst + P.row0 * 64,
+                              rows_total * 64, 64);
 }
 
 template <int NP>
@@ -1035,11 +1112,14 @@ template <int BN, int STAGES, int NP>
 static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &t, long long tiles,
                       const char *name, bool allow_tail = true) {
     using Cfg = TcCfg<BN, STAGES, TC_KC, NP>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES, TC_KC, NP>,
+    // the shared-memory limit is a per-device attribute of the kernel: set once on every device
+    // this instantiation launches on (the calling entry point made ctx->device current)
+    static std::atomic<unsigned long long> attr_set{0};
+    const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
+    if (!bit || !(attr_set.load() & bit)) {
+        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<BN, STAGES, TC_KC, NP, false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
-        attr_set = true;
+        attr_set.fetch_or(bit);
     }
     TcArgs g = t;
     g.tiles = tiles;
@@ -1084,7 +1164,8 @@ static void launch_tc(Ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, co
     const long long grid = std::min<long long>(items, sms);
     {
         Ctx::Scope s(ctx, name);
-        gett_tc_kernel<BN, STAGES, TC_KC, NP><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g);
+        gett_tc_kernel<BN, STAGES, TC_KC, NP, false>
+            <<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(ma, mb, g, nullptr, 0);
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     if (g.full_items > 0) {
@@ -1207,16 +1288,155 @@ void gett_tc(Ctx *ctx, const GettArgs &a0, const char *name, int np) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Grouped split GEMM for the batched form: many independent GETTs, each with K <= 64, in one
+// persistent launch of three-plane tcgen05 tiles.  Every problem's operand rows are packed into
+// one set of planes per side (rows concatenated, one 64-wide K block), so a single tensor map
+// per side covers the whole batch; the kernel finds an item's problem by binary search over the
+// problems' first items.  Building (allocations, tensor maps, tables) happens once; running is
+// two grouped pack launches and one GEMM launch, which a CUDA graph can capture.
+// ---------------------------------------------------------------------------------------
+struct TcGroup {
+    std::string name;
+    long long rowsA = 0, rowsB = 0, items = 0, blocksA = 0, blocksB = 0;
+    std::vector<PackProb> packA, packB;
+    std::vector<TcGroupProb> probs;
+    DBuf<PackProb> dpackA, dpackB;
+    DBuf<TcGroupProb> dprobs;
+    DBuf<__half> planesA, planesB;
+    DBuf<int> expA, expB;
+    CUtensorMap mapA, mapB;
+};
+
+constexpr int TG_BN = 64, TG_NP = 3, TG_STAGES = 3;
+
+TcGroup *tc_group_build(Ctx *ctx, const std::vector<GettArgs> &in, const char *name) {
+    for (const GettArgs &a : in)
+        if (a.K > TBK || a.K < 1) return nullptr;   // one K block per problem
+    std::unique_ptr<TcGroup> tg(new TcGroup());
+    tg->name = name;
+    for (const GettArgs &a0 : in) {
+        if (a0.M <= 0 || a0.N <= 0) continue;
+        GettArgs a = a0;
+        // the output's unit-stride mode on the TMEM-lane side unless padding says otherwise
+        // (rows pad to 128, columns to 64)
+        const bool m_unit = a.mC.s0 == 1 && a.mC.d0 > 1, n_unit = a.nC.s0 == 1 && a.nC.d0 > 1;
+        const double keep = (double)roundup(a.M, TBM) * roundup(a.N, TG_BN) * (m_unit ? 1.0 : 1.35);
+        const double swap = (double)roundup(a.N, TBM) * roundup(a.M, TG_BN) * (n_unit ? 1.0 : 1.35);
+        if (swap < keep) {
+            std::swap(a.M, a.N);
+            std::swap(a.A, a.B);
+            std::swap(a.mA, a.nB);
+            std::swap(a.kA, a.kB);
+            std::swap(a.mC, a.nC);
+        }
+        const long long Mpad = roundup(a.M, TBM), Npad = roundup(a.N, TG_BN);
+        TcGroupProb g{};
+        TcArgs &t = g.a;
+        t.M = a.M;
+        t.N = a.N;
+        t.kblocks = 1;
+        t.mtiles = Mpad / TBM;
+        t.tiles = t.mtiles * (Npad / TG_BN);
+        t.ksplit = 1;
+        t.kper = 1;
+        t.partial = nullptr;
+        t.full_items = 0;
+        t.alpha = a.alpha;
+        t.beta = a.beta;
+        int ak = 0;
+        const double am = std::frexp(std::fabs(a.alpha), &ak);
+        t.alpha_pow2 = (am == 0.5 && ak - 1 >= -8 && ak - 1 <= 8) ? 1 : 0;
+        t.alpha_k = t.alpha_pow2 ? ak - 1 : 0;
+        t.alpha_neg = (t.alpha_pow2 && a.alpha < 0) ? 1 : 0;
+        t.C = a.C;
+        t.Cin = a.Cin ? a.Cin : a.C;
+        t.beta_mode = a.beta == 0.0 ? 0 : (a.beta == 1.0 ? (t.Cin == t.C ? 1 : 2) : 3);
+        t.mC = a.mC;
+        t.nC = a.nC;
+        t.flags = ctx->d_flags;
+        t.expA_ld = t.expB_ld = 0;   // one K chunk: the chunk stride is never used
+        g.rowA = (int)tg->rowsA;
+        g.rowB = (int)tg->rowsB;
+        g.item0 = tg->items;
+        tg->packA.push_back(PackProb{a.A, a.mA, a.kA, a.M, a.K, Mpad, tg->rowsA, tg->blocksA});
+        tg->packB.push_back(PackProb{a.B, a.nB, a.kB, a.N, a.K, Npad, tg->rowsB, tg->blocksB});
+        tg->rowsA += Mpad;
+        tg->rowsB += Npad;
+        tg->blocksA += Mpad / PR;
+        tg->blocksB += Npad / PR;
+        tg->items += t.tiles;
+        tg->probs.push_back(g);
+    }
+    if (tg->probs.empty()) return tg.release();
+    JUES_REQUIRE(tg->rowsA < (1LL << 31) && tg->rowsB < (1LL << 31) && tg->blocksA < (1LL << 31) &&
+                     tg->blocksB < (1LL << 31) && tg->items < (1LL << 31),
+                 "batch too large for one grouped launch");
+    tg->planesA = DBuf<__half>(ctx, (size_t)TG_NP * tg->rowsA * TBK);
+    tg->planesB = DBuf<__half>(ctx, (size_t)TG_NP * tg->rowsB * TBK);
+    tg->expA = DBuf<int>(ctx, (size_t)tg->rowsA);
+    tg->expB = DBuf<int>(ctx, (size_t)tg->rowsB);
+    for (auto &g : tg->probs) {
+        g.a.expA = tg->expA.p + g.rowA;
+        g.a.expB = tg->expB.p + g.rowB;
+    }
+    tg->dpackA = DBuf<PackProb>(ctx, tg->packA.size());
+    tg->dpackB = DBuf<PackProb>(ctx, tg->packB.size());
+    tg->dprobs = DBuf<TcGroupProb>(ctx, tg->probs.size());
+    JUES_CHECK_CUDA(cudaMemcpyAsync(tg->dpackA.p, tg->packA.data(), tg->packA.size() * sizeof(PackProb),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    JUES_CHECK_CUDA(cudaMemcpyAsync(tg->dpackB.p, tg->packB.data(), tg->packB.size() * sizeof(PackProb),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    JUES_CHECK_CUDA(cudaMemcpyAsync(tg->dprobs.p, tg->probs.data(), tg->probs.size() * sizeof(TcGroupProb),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    tg->mapA = make_map(tg->planesA.p, tg->rowsA, TBK, TBM, TG_NP);
+    tg->mapB = make_map(tg->planesB.p, tg->rowsB, TBK, TG_BN, TG_NP);
+    JUES_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));   // the host tables stay valid until then
+    return tg.release();
+}
+
+void tc_group_run(Ctx *ctx, TcGroup *tg) {
+    if (!tg || tg->probs.empty()) return;
+    using Cfg = TcCfg<TG_BN, TG_STAGES, TC_KC, TG_NP>;
+    {
+        Ctx::Scope s(ctx, "pack_grouped");
+        pack_grouped_kernel<TG_NP><<<(unsigned)tg->blocksA, 256, 0, ctx->stream>>>(
+            tg->dpackA.p, (int)tg->packA.size(), tg->rowsA, tg->expA.p, tg->planesA.p);
+        JUES_CHECK_CUDA(cudaGetLastError());
+        pack_grouped_kernel<TG_NP><<<(unsigned)tg->blocksB, 256, 0, ctx->stream>>>(
+            tg->dpackB.p, (int)tg->packB.size(), tg->rowsB, tg->expB.p, tg->planesB.p);
+        ctx->count_launch();
+        JUES_CHECK_CUDA(cudaGetLastError());
+    }
+    static std::atomic<unsigned long long> attr_set{0};
+    const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
+    if (!bit || !(attr_set.load() & bit)) {
+        JUES_CHECK_CUDA(cudaFuncSetAttribute(gett_tc_kernel<TG_BN, TG_STAGES, TC_KC, TG_NP, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+        attr_set.fetch_or(bit);
+    }
+    TcArgs g{};
+    g.tiles = tg->items;
+    g.flags = ctx->d_flags;
+    const long long grid = std::min<long long>(tg->items, sm_count(ctx->device));
+    Ctx::Scope s(ctx, tg->name.c_str());
+    gett_tc_kernel<TG_BN, TG_STAGES, TC_KC, TG_NP, true><<<(unsigned)grid, TC_THREADS, Cfg::SMEM, ctx->stream>>>(
+        tg->mapA, tg->mapB, g, tg->dprobs.p, (int)tg->probs.size());
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void tc_group_destroy(TcGroup *tg) { delete tg; }
+
+// ---------------------------------------------------------------------------------------
 // Allocation-free variant of the split GEMM (jues_gemm_noalloc).
 //
-// Some callers cannot allocate device memory at the moment they need a contraction: code
-// running while a CUDA graph is being captured (cudaMalloc is not allowed there), host
-// frameworks whose device memory is owned entirely by their own pool allocator, and
-// fixed-budget or real-time callers that must not grow their footprint after start-up.
-// For them this variant packs its operands into one statically sized device array that is
-// part of the loaded module (every GPU that loads the library holds it until the process
-// exits) and allocates nothing itself.  The caller provides inputs and output in device
-// memory.
+// Some callers cannot let the library allocate device memory when they need a contraction:
+// host frameworks that reserve the GPU's memory at start-up and hand it out from their own pool
+// allocator (a cudaMalloc from inside the library would fail or escape their accounting), and
+// long-running or fixed-budget services that must not grow their device footprint after
+// start-up.  For them this variant packs its operands into one statically sized device array
+// that is part of the loaded module (every GPU that loads the library holds it until the process
+// exits) and allocates nothing itself.  The caller provides inputs and output in device memory.
+// The call ends by reading the device error flags, so it is synchronous at return.
 // ---------------------------------------------------------------------------------------
 constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(64) << 20;   // 64 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
@@ -1259,9 +1479,28 @@ void expired_wait(Ctx *ctx) {
     ctx->check_flags();   // throws JUES_ETIMEOUT and clears the flag
 }
 
+// C = beta C over an M x N output (K = 0: the product is empty); beta = 0 writes zeros
+__global__ void __launch_bounds__(256) scale_output_kernel(double *C, Mode mC, Mode nC, long long M, long long N,
+                                                           double beta) {
+    const long long total = M * N;
+    for (long long e = blockIdx.x * 256LL + threadIdx.x; e < total; e += (long long)gridDim.x * 256) {
+        const long long m = e % M, n = e / M;
+        double *p = C + mode_off(mC, m) + mode_off(nC, n);
+        *p = beta == 0.0 ? 0.0 : beta * *p;
+    }
+}
+
 void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {
     if (a.M <= 0 || a.N <= 0) return;
-    JUES_REQUIRE(a.K >= 1, "K must be positive");
+    JUES_REQUIRE(a.K >= 0, "K must be non-negative");
+    JUES_REQUIRE(!a.Cin || a.Cin == a.C, "the allocation-free GEMM accumulates into C itself");
+    if (a.K == 0) {
+        const long long blocks = std::min<long long>((a.M * a.N + 255) / 256, 152LL * 8);
+        Ctx::Scope s(ctx, "gemm_noalloc_scale");
+        scale_output_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(a.C, a.mC, a.nC, a.M, a.N, a.beta);
+        JUES_CHECK_CUDA(cudaGetLastError());
+        return;
+    }
     // fixed orientation and tile width: BN = 128, the A operand on the TMEM-lane side
     constexpr int BN = 128;
     const long long Mpad = roundup(a.M, TBM), Npad = roundup(a.N, BN), Kpad = roundup(a.K, TBK);

@@ -2,6 +2,8 @@
 //
 // Every reduction is deterministic: a fixed-size grid writes one FP64 partial per block,
 // and a single block sums the partials in a fixed order.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "common.cuh"
@@ -53,6 +55,70 @@ __global__ void permute4_kernel(Perm4 p, double alpha, const double *__restrict_
         double v = alpha * in[oi];
         if (beta != 0.0) v += beta * out[oo];
         out[oo] = v;
+    }
+}
+
+// Tiled form of permute4_kernel for a permutation that moves the input's unit-stride dimension
+// (ki) away from the output's (ko): a 32 x 32 tile of the (ki, ko) plane goes through shared
+// memory, so both the loads (along ki) and the stores (along ko) are coalesced.  VEC: 16-byte
+// loads and stores (two doubles per thread; the host checks alignment and even extents).
+// Block 32 x 8 threads; grid x = tiles of the plane, grid y strides over the other two dimensions.
+template <bool VEC>
+__global__ void __launch_bounds__(256) permute4_tiled_kernel(Perm4 p, int ki, int ko, int r1, int r2, double alpha,
+                                                             const double *__restrict__ in, double beta,
+                                                             double *__restrict__ out) {
+    __shared__ double tile[32][33];   // [ko][ki], odd pitch: column reads are conflict-free
+    const long long dki = p.d[ki], dko = p.d[ko];
+    const long long nti = (dki + 31) / 32;
+    const long long ti = blockIdx.x % nti, to = blockIdx.x / nti;
+    const long long i0 = ti * 32, o0 = to * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long long nrest = p.d[r1] * p.d[r2];
+    for (long long rest = blockIdx.y; rest < nrest; rest += gridDim.y) {
+        const long long a1 = rest % p.d[r1], a2 = rest / p.d[r1];
+        const long long bin = a1 * p.si[r1] + a2 * p.si[r2], bout = a1 * p.so[r1] + a2 * p.so[r2];
+        if (VEC) {
+            // lanes 0-15 load row y, lanes 16-31 row y + 1, two consecutive ki each
+            const int c = 2 * (tx & 15), rsub = tx >> 4;
+            for (int y = 2 * ty + rsub; y < 32; y += 16) {
+                const long long k = i0 + c, q = o0 + y;
+                if (q < dko && k < dki) {
+                    const double2 v = *reinterpret_cast<const double2 *>(in + bin + k + q * p.si[ko]);
+                    tile[y][c] = v.x;
+                    tile[y][c + 1] = v.y;
+                }
+            }
+            __syncthreads();
+            for (int y = 2 * ty + rsub; y < 32; y += 16) {
+                const long long q = o0 + c, k = i0 + y;
+                if (k < dki && q < dko) {
+                    double2 *dst = reinterpret_cast<double2 *>(out + bout + q + k * p.so[ki]);
+                    double2 v = make_double2(alpha * tile[c][y], alpha * tile[c + 1][y]);
+                    if (beta != 0.0) {
+                        const double2 w = *dst;
+                        v.x = fma(beta, w.x, v.x);
+                        v.y = fma(beta, w.y, v.y);
+                    }
+                    *dst = v;
+                }
+            }
+        } else {
+            for (int y = ty; y < 32; y += 8) {
+                const long long k = i0 + tx, q = o0 + y;
+                if (q < dko && k < dki) tile[y][tx] = in[bin + k + q * p.si[ko]];
+            }
+            __syncthreads();
+            for (int y = ty; y < 32; y += 8) {
+                const long long q = o0 + tx, k = i0 + y;
+                if (k < dki && q < dko) {
+                    double *dst = out + bout + q + k * p.so[ki];
+                    double v = alpha * tile[tx][y];
+                    if (beta != 0.0) v = fma(beta, *dst, v);
+                    *dst = v;
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -184,6 +250,72 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// The same finalisation with the (i,j) transposes through shared memory: block p handles the
+// pair (a <= b); Z[:,:,a,b] and Z[:,:,b,a] are contiguous o x o blocks, loaded coalesced into
+// shared memory on an odd row pitch (conflict-free transposed reads), so every global access is
+// unit-stride.  Dynamic shared memory 2 o pitch doubles (o <= 64).
+__global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__restrict__ L,
+                                                               const double *__restrict__ Z,
+                                                               const double *__restrict__ invD, int o, int v,
+                                                               const double *__restrict__ Told,
+                                                               double *__restrict__ Tn, double *part) {
+    extern __shared__ double zs[];   // [2][o][pitch]: zs[0] = Z_ab, zs[1] = Z_ba, element (i, j) at j + pitch i
+    const int pitch = o | 1;
+    const long long oo = (long long)o * o;
+    const long long npair = (long long)v * (v + 1) / 2;
+    const int ooi = o * o;
+    double acc = 0.0;
+    for (long long p = blockIdx.x; p < npair; p += gridDim.x) {
+        int a, b;
+        pair_ab(p, a, b);
+        const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
+        __syncthreads();   // the previous pair's reads of zs are done
+        for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
+            const int i = ij % o, j = ij / o;
+            zs[j + pitch * i] = Z[ab + ij];
+            zs[o * pitch + j + pitch * i] = Z[ba + ij];
+        }
+        __syncthreads();
+        for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
+            const int i = ij % o, j = ij / o;
+            // Z_ab[i,j] and Z_ba[j,i]; Z_ba[i,j] and Z_ab[j,i]
+            const double zab = zs[j + pitch * i], zba_t = zs[o * pitch + i + pitch * j];
+            const double inv = invD[ab + ij];   // D is symmetric in (a, b)
+            const double x = (L[ab + ij] + zab + zba_t) * inv;
+            Tn[ab + ij] = x;
+            if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
+            if (a != b) {
+                const double zba = zs[o * pitch + j + pitch * i], zab_t = zs[i + pitch * j];
+                const double y = (L[ba + ij] + zba + zab_t) * inv;
+                Tn[ba + ij] = y;
+                if (Told) { const double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
+            }
+        }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// T~[i,j,a,b] = 2 T[i,j,a,b] - T[j,i,a,b], one (a,b) block per iteration with its transpose
+// through shared memory (odd row pitch), every global access unit-stride
+__global__ void __launch_bounds__(256) t_tilde_smem_kernel(const double *__restrict__ T, int o, int v,
+                                                           double *__restrict__ out) {
+    extern __shared__ double ts[];
+    const int pitch = o | 1;
+    const long long oo = (long long)o * o, vv = (long long)v * v;
+    const int ooi = o * o;
+    for (long long ab = blockIdx.x; ab < vv; ab += gridDim.x) {
+        const double *Tb = T + oo * ab;
+        __syncthreads();
+        for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) ts[ij / o + pitch * (ij % o)] = Tb[ij];
+        __syncthreads();
+        for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
+            const int i = ij % o, j = ij / o;
+            out[oo * ab + ij] = fma(2.0, ts[j + pitch * i], -ts[i + pitch * j]);
+        }
+    }
 }
 
 __global__ void divide_by_d_kernel(const double *__restrict__ in, const double *__restrict__ eps, int o,
@@ -350,7 +482,37 @@ void permute4(Ctx *ctx, const Perm4 &p, double alpha, const double *in, double b
     long long total = p.d[0] * p.d[1] * p.d[2] * p.d[3];
     if (total == 0) return;
     Ctx::Scope s(ctx, "permute4");
-    permute4_kernel<<<grid_for(total), 256, 0, ctx->stream>>>(p, alpha, in, beta, out, total);
+    // the input's and the output's unit-stride dimensions (extent > 1)
+    int ki = -1, ko = -1;
+    for (int k = 0; k < 4; ++k) {
+        if (p.d[k] > 1 && p.si[k] == 1 && ki < 0) ki = k;
+        if (p.d[k] > 1 && p.so[k] == 1 && ko < 0) ko = k;
+    }
+    if (ki < 0 || ko < 0 || ki == ko) {
+        // both sides are coalesced along the same dimension (or neither has a unit stride)
+        permute4_kernel<<<grid_for(total), 256, 0, ctx->stream>>>(p, alpha, in, beta, out, total);
+        JUES_CHECK_CUDA(cudaGetLastError());
+        return;
+    }
+    int rest[2], nr = 0;
+    for (int k = 0; k < 4; ++k)
+        if (k != ki && k != ko) rest[nr++] = k;
+    const long long tiles = ((p.d[ki] + 31) / 32) * ((p.d[ko] + 31) / 32);
+    JUES_REQUIRE(tiles < (1LL << 31), "permutation too large");
+    const long long nrest = p.d[rest[0]] * p.d[rest[1]];
+    const unsigned gy = (unsigned)std::min<long long>(nrest, std::max<long long>(1, 152LL * 32 / std::max(1LL, tiles)) * 8);
+    // 16-byte accesses need even extents and strides along the tile and 16-byte aligned bases
+    bool vec = p.d[ki] % 2 == 0 && p.d[ko] % 2 == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0 &&
+               (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    for (int k = 0; k < 4; ++k)
+        if (k != ki) vec = vec && p.si[k] % 2 == 0;
+    for (int k = 0; k < 4; ++k)
+        if (k != ko) vec = vec && p.so[k] % 2 == 0;
+    const dim3 grid((unsigned)tiles, std::max(1u, gy)), block(32, 8);
+    if (vec)
+        permute4_tiled_kernel<true><<<grid, block, 0, ctx->stream>>>(p, ki, ko, rest[0], rest[1], alpha, in, beta, out);
+    else
+        permute4_tiled_kernel<false><<<grid, block, 0, ctx->stream>>>(p, ki, ko, rest[0], rest[1], alpha, in, beta, out);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -439,7 +601,19 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
     int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
     {
         Ctx::Scope s(ctx, "t2_finalize");
-        t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
+        if (o <= 64) {
+            const size_t smem = (size_t)2 * o * (o | 1) * sizeof(double);
+            static std::atomic<unsigned long long> attr_set{0};
+            const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
+            if (smem > 48 * 1024 && (!bit || !(attr_set.load() & bit))) {
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
+                attr_set.fetch_or(bit);
+            }
+            t2_finalize_smem_kernel<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
+        } else {
+            t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
+        }
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     return Told ? finish_reduce(ctx, nb) : 0.0;
@@ -464,7 +638,13 @@ void divide_by_d(Ctx *ctx, const double *in, const double *eps, int o, int v, do
 void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out) {
     long long n = (long long)o * o * v * v;
     Ctx::Scope s(ctx, "t_tilde");
-    t_tilde_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(T, o, v, out);
+    if (o <= 64) {
+        const size_t smem = (size_t)o * (o | 1) * sizeof(double);   // <= 33 KB
+        const long long vv = (long long)v * v;
+        t_tilde_smem_kernel<<<(unsigned)std::min<long long>(vv, 152LL * 16), 256, smem, ctx->stream>>>(T, o, v, out);
+    } else {
+        t_tilde_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(T, o, v, out);
+    }
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 

@@ -118,7 +118,7 @@ void transform4(Ctx *ctx, int prec, const double *g, int n, const double *const 
     std::vector<GettArgs> steps = transform4_plan(g, n, C, d_in, out, ostr, b0.p, b1.p);
     for (size_t k = 0; k < steps.size(); ++k) {
         steps[k].a_const = (k == 0) && g_const;
-        gett(ctx, prec, steps[k], k == 0 ? "transform_q1" : "transform_q234");
+        gett(ctx, integral_precision(prec), steps[k], k == 0 ? "transform_q1" : "transform_q234");
     }
 }
 
@@ -191,7 +191,8 @@ void backtransform4(Ctx *ctx, int prec, const double *X, const int d[4], int n, 
                     double *out) {
     const long long need = backtransform4_scratch(d, n);
     DBuf<double> b0(ctx, (size_t)need), b1(ctx, (size_t)need);
-    for (auto &a : backtransform4_plan(X, d, n, C, out, b0.p, b1.p)) gett(ctx, prec, a, "backtransform");
+    for (auto &a : backtransform4_plan(X, d, n, C, out, b0.p, b1.p))
+        gett(ctx, integral_precision(prec), a, "backtransform");
 }
 
 void get_eri_block(Ctx *ctx, int prec, const double *g, int n, const double *Cocc, int o,

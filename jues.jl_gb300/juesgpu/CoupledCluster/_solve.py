@@ -8,7 +8,7 @@ from .. import _lib
 
 
 def make_opts(maxit=40, e_conv=0.0, r_conv=1e-7, diis=True, diis_size=6, precision="fp64",
-              guess="zero", refine=2, transform_precision=None) -> _lib.CCOpts:
+              guess="zero", refine=2, transform_precision=None, ccsd_fae="rccsd") -> _lib.CCOpts:
     o = _lib.default_opts()
     o.maxit = int(maxit)
     o.e_conv = float(e_conv or 0.0)
@@ -19,6 +19,7 @@ def make_opts(maxit=40, e_conv=0.0, r_conv=1e-7, diis=True, diis_size=6, precisi
     o.guess = _lib.GUESS[guess]
     o.refine = int(refine)
     o.transform_precision = -1 if transform_precision is None else _lib.PREC[transform_precision]
+    o.ccsd_fae = _lib.CCSD_FAE[ccsd_fae]
     return o
 
 

@@ -75,11 +75,14 @@ def rmp2_adjoint(refWfn=None, *, gao=None, C=None, nocc=None, eps=None, e_bar: f
     return E.value, gb, cb
 
 
-def batch_rmp2(systems, *, e_bar: float = 1.0, adjoint: bool = False, device: int = 0):
+def batch_rmp2(systems, *, e_bar: float = 1.0, adjoint: bool = False, precision: str = "fp64",
+               device: int = 0):
     """MP2 energies (and adjoints) of many independent systems in one CUDA graph.
 
     systems: iterable of (gao, C, nocc, eps) or Wfn objects.  Returns (energies, gao_bars,
-    C_bars, info) with the gradient lists None unless ``adjoint``.
+    C_bars, info) with the gradient lists None unless ``adjoint``.  ``precision`` "fp64" runs
+    grouped FP64 GETTs; the split forms let each stage's autotuning pick the grouped
+    three-plane tcgen05 GEMM where every system's contraction has K <= 64.
     """
     items = []
     for s in systems:
@@ -101,6 +104,6 @@ def batch_rmp2(systems, *, e_bar: float = 1.0, adjoint: bool = False, device: in
         cptr = (_lib.DP * nsys)(*[_lib.ptr(x) for x in cbs])
     info = _lib.BatchInfo()
     ctx = _lib.context(device)
-    _lib.check(ctx.lib.jues_batch_rmp2(ctx.h, nsys, arr, float(e_bar), _lib.ptr(energies), gptr, cptr,
-                                       C_.byref(info)))
+    _lib.check(ctx.lib.jues_batch_rmp2(ctx.h, nsys, arr, _lib.PREC[precision], float(e_bar), _lib.ptr(energies),
+                                       gptr, cptr, C_.byref(info)))
     return energies, gbs, cbs, info

@@ -16,8 +16,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libjuesgpu.so")
 
 OK, EINVAL, ENOMEM, ECUDA, ENOTCONV, ENONFINITE, ETIMEOUT, ENODEV = range(8)
-PREC = {"fp64": 0, "split_bf16": 1, "split3": 2}
+# "split": the split form at <= 1 uEh (three integer planes for contractions that produce
+# integrals, two for the CC sweeps); "split_bf16" is its earlier name.  "split3" / "split2":
+# three / two planes everywhere.
+PREC = {"fp64": 0, "split": 1, "split_bf16": 1, "split3": 2, "split2": 3}
 GUESS = {"zero": 0, "mp2": 1, "ovov": 2}
+# CCSD Fae t1 term: "rccsd" = <ma|ef> (RCCSD.jl:190), "mrccsd" = <me|af> (mRCCSD.jl:140)
+CCSD_FAE = {"rccsd": 0, "mrccsd": 1}
 
 
 class JuESError(RuntimeError):
@@ -33,7 +38,8 @@ class NotConverged(JuESError):
 class CCOpts(C.Structure):
     _fields_ = [("maxit", C.c_int), ("e_conv", C.c_double), ("r_conv", C.c_double),
                 ("diis", C.c_int), ("diis_size", C.c_int), ("precision", C.c_int),
-                ("guess", C.c_int), ("refine", C.c_int), ("transform_precision", C.c_int)]
+                ("guess", C.c_int), ("refine", C.c_int), ("transform_precision", C.c_int),
+                ("ccsd_fae", C.c_int)]
 
 
 class IterLog(C.Structure):
@@ -80,7 +86,7 @@ SIGNATURES = {
     "jues_rmp2": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, DP]),
     "jues_df_rmp2": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP]),
     "jues_rmp2_adjoint": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, C.c_double, DP, DP, DP]),
-    "jues_batch_rmp2": (C.c_int, [VP, C.c_int, C.POINTER(MP2System), C.c_double, DP, C.POINTER(DP),
+    "jues_batch_rmp2": (C.c_int, [VP, C.c_int, C.POINTER(MP2System), C.c_int, C.c_double, DP, C.POINTER(DP),
                                   C.POINTER(DP), C.POINTER(BatchInfo)]),
     "jues_cc_default_opts": (C.c_int, [C.POINTER(CCOpts)]),
     "jues_rccd": (C.c_int, [VP, DP, C.c_int, DP, C.c_int, DP, C.c_int, DP, C.POINTER(CCOpts), DP,
@@ -99,6 +105,7 @@ SIGNATURES = {
                                   DP, DP, DP, DP, C.POINTER(IterLog), C.c_int, C.POINTER(C.c_int)]),
     "jues_cc_pT": (C.c_int, [VP, C.c_int, DP]),
     "jues_ctx_set_ao_direct": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
+    "jues_ctx_set_batch_form": (C.c_int, [VP, C.c_int]),
     "jues_cc_iterate": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "jues_cc_set_precision": (C.c_int, [VP, C.c_int]),
     "jues_cc_energy": (C.c_int, [VP, DP]),
@@ -189,6 +196,10 @@ class Context:
         a = C.c_int()
         check(self.lib.jues_ctx_set_ao_direct(self.h, 1 if enable else 0, C.byref(a)))
         return bool(a.value)
+
+    def set_batch_form(self, form: str):
+        """Forms the batched MP2 autotuning may pick: "auto", "fp64" or "tcgen05"."""
+        check(self.lib.jues_ctx_set_batch_form(self.h, {"auto": 0, "fp64": 1, "tcgen05": 2}[form]))
 
     def launches(self) -> int:
         return int(self.lib.jues_ctx_launch_count(self.h))

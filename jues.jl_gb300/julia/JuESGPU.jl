@@ -16,7 +16,11 @@ module JuESGPU
 using JuES.Wavefunction
 
 const LIB = get(ENV, "JUESGPU_LIB", joinpath(@__DIR__, "..", "lib", "libjuesgpu.so"))
-const PREC = Dict(:fp64 => Cint(0), :split_bf16 => Cint(1), :split3 => Cint(2))
+# :split is the split form at <= 1 uEh (three integer planes for contractions that produce
+# integrals, two for the CC sweeps); :split_bf16 is its earlier name; :split3 / :split2 use
+# three / two planes everywhere
+const PREC = Dict(:fp64 => Cint(0), :split => Cint(1), :split_bf16 => Cint(1), :split3 => Cint(2),
+                  :split2 => Cint(3))
 const GUESS = Dict(:zero => Cint(0), :mp2 => Cint(1), :ovov => Cint(2))
 const ENOTCONV = 4
 
@@ -30,6 +34,7 @@ struct CCOpts
     guess::Cint
     refine::Cint
     transform_precision::Cint
+    ccsd_fae::Cint      # 0: Fae's t1 term with <ma|ef> (RCCSD.jl:190); 1: <me|af> (mRCCSD.jl:140)
 end
 
 struct IterLog
@@ -146,10 +151,11 @@ try
 catch
 end
 
-function cc_solve(method, refWfn; maxit, r_conv, e_conv, diis, diis_size, precision, guess, refine)
+function cc_solve(method, refWfn; maxit, r_conv, e_conv, diis, diis_size, precision, guess, refine, ccsd_fae = 0)
     Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
     o, v = size(Co, 2), size(Cv, 2)
-    opts = Ref(CCOpts(maxit, e_conv, r_conv, diis, diis_size, PREC[precision], GUESS[guess], refine, Cint(-1)))
+    opts = Ref(CCOpts(maxit, e_conv, r_conv, diis, diis_size, PREC[precision], GUESS[guess], refine, Cint(-1),
+                      Cint(ccsd_fae)))
     e = Ref{Cdouble}(0.0)
     nit = Ref{Cint}(0)
     T2 = Array{Float64}(undef, o, o, v, v)
@@ -182,11 +188,14 @@ function do_rccd(refWfn::Wfn; maxit = 40, doprint = false, return_T2 = false, pr
     return return_T2 ? (E, T2) : E
 end
 
-"RCCSD.do_rccsd(refWfn; maxit=40, return_T=false) -- RCCSD.jl:33-116"
+"""
+    do_rccsd(refWfn; maxit=40, return_T=false) -- RCCSD.jl:33-116 (`ccsd_fae = 0`) and
+    mRCCSD.jl:35-101 (`ccsd_fae = 1`: Fae's t1 term as mRCCSD.jl:140)
+"""
 function do_rccsd(refWfn::Wfn; maxit = 40, return_T = false, precision = :fp64, diis = false,
-                  r_conv = 0.0, e_conv = 0.0, diis_size = 6, refine = 0, kwargs...)
+                  r_conv = 0.0, e_conv = 0.0, diis_size = 6, refine = 0, ccsd_fae = 0, kwargs...)
     E, t1, T2, _ = cc_solve(1, refWfn; maxit, r_conv, e_conv, diis = Cint(diis), diis_size,
-                            precision, guess = :mp2, refine)
+                            precision, guess = :mp2, refine, ccsd_fae)
     return return_T ? (E, T2) : E
 end
 
@@ -222,7 +231,7 @@ function do_df_rccd(refWfn::Wfn, pqP::AbstractArray{<:Real,3}, Jpqh = nothing; m
     J = Jpqh === nothing ? C_NULL : f64(Jpqh)
     Co, Cv = f64(refWfn.Cao), f64(refWfn.Cav)
     o, v = size(Co, 2), size(Cv, 2)
-    opts = Ref(CCOpts(maxit, e_conv, r_conv, Cint(diis), diis_size, PREC[precision], GUESS[:mp2], refine, Cint(-1)))
+    opts = Ref(CCOpts(maxit, e_conv, r_conv, Cint(diis), diis_size, PREC[precision], GUESS[:mp2], refine, Cint(-1), Cint(0)))
     e = Ref{Cdouble}(0.0)
     nit = Ref{Cint}(0)
     T2 = Array{Float64}(undef, o, o, v, v)
@@ -276,7 +285,7 @@ function auto_rccsd(wfn::Wfn; cc_max_iter = 50, cc_max_rms = 1e-10, cc_e_conv = 
     Cm = f64(wfn.Ca)
     n, nmo = size(Cm)
     ndocc = (wfn.nalpha + wfn.nbeta) ÷ 2
-    opts = Ref(CCOpts(cc_max_iter, cc_e_conv, cc_max_rms, Cint(diis), 6, PREC[precision], GUESS[:mp2], 0, Cint(-1)))
+    opts = Ref(CCOpts(cc_max_iter, cc_e_conv, cc_max_rms, Cint(diis), 6, PREC[precision], GUESS[:mp2], 0, Cint(-1), Cint(0)))
     e = Ref{Cdouble}(0.0)
     ept = Ref{Cdouble}(0.0)
     nit = Ref{Cint}(0)

@@ -1,7 +1,8 @@
 """Oracle energies of the seeded synthetic systems, committed as synthetic_golden.json.
 
 The GPU parity tests compare against these numbers (the oracle is too slow to rerun at
-nbf=100 inside a test).  Run: ``python tests/golden/make_synthetic_golden.py [S25 S100 ...]``.
+nbf=100 inside a test).  Run: ``python tests/golden/make_synthetic_golden.py [S25 S100 ...]``;
+``--ccsd-m S25 S100`` adds only the mRCCSD.jl-variant CCSD records.
 Test infrastructure only.
 """
 import json
@@ -43,7 +44,24 @@ def run(name):
     log = []
     ccsd.do_rccsd(w, form="m", fae_variant="jl", maxit=6, log=log, blocks=blocks)
     rec["ccsd_plain_6"] = log
+    rec.update(run_ccsd_m(name, w, blocks))
     rec["seconds"] = time.time() - t0
+    return rec
+
+
+def run_ccsd_m(name, w=None, blocks=None):
+    """mRCCSD.jl's own Fae t1 term (<me|af>, mRCCSD.jl:140): converged DIIS energy and log, and
+    six plain sweeps."""
+    w = w if w is not None else make_named(name).wfn()
+    blocks = blocks if blocks is not None else ccsd.make_rccsd_integrals(w)
+    rec = {}
+    log = []
+    e = ccsd.do_rccsd(w, form="m", fae_variant="m", maxit=60, diis=True, r_conv=1e-11, log=log,
+                      blocks=blocks)
+    rec["ccsd_m_diis"] = {"energy": e, "niter": len(log), "log": log}
+    log = []
+    ccsd.do_rccsd(w, form="m", fae_variant="m", maxit=6, log=log, blocks=blocks)
+    rec["ccsd_m_plain_6"] = log
     return rec
 
 
@@ -52,6 +70,14 @@ def main(names):
     if os.path.exists(OUT):
         with open(OUT) as f:
             data = json.load(f)
+    if names and names[0] == "--ccsd-m":
+        # add only the mRCCSD.jl-variant records to existing entries
+        for n in names[1:]:
+            data[n].update(run_ccsd_m(n))
+            with open(OUT, "w") as f:
+                json.dump(data, f, indent=1)
+            print(n, data[n]["ccsd_m_diis"]["energy"], flush=True)
+        return
     for n in names:
         data[n] = run(n)
         with open(OUT, "w") as f:

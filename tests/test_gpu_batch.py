@@ -53,3 +53,28 @@ def test_batch_rejects_bad_system(mp):
     C = np.eye(4, order="F")
     with pytest.raises(JuESError):
         mp.batch_rmp2([(g, C, 4, np.zeros(4))])
+
+
+@pytest.mark.parametrize("form", ["tcgen05", "auto"])
+def test_batch_split_grouped_tcgen05_matches_fp64(mp, form):
+    # split precision: the grouped three-plane tcgen05 GEMM (pinned, or as the autotuner picks)
+    # against the single-system FP64 adjoint; energies within 1e-9 Eh, gradients 1e-7 relative
+    from juesgpu import _lib
+    sy = systems(20, 10, 40, seed=3)
+    ctx = _lib.context(0)
+    ctx.set_batch_form(form)
+    try:
+        e, gbs, cbs, info = mp.batch_rmp2(sy, adjoint=True, e_bar=0.5, precision="split")
+        e2, gbs2, cbs2, info2 = mp.batch_rmp2(sy, adjoint=True, e_bar=0.5, precision="split")
+    finally:
+        ctx.set_batch_form("auto")
+    shapes = [info.tile_shape[k] for k in range(info.nstages)]
+    if form == "tcgen05":
+        # every stage but the final dE/dC one has K <= nbf <= 64
+        assert shapes[:-1] == [4] * (info.nstages - 1), shapes
+    assert info2.tuned == 0 and np.array_equal(e, e2)
+    for (g, C, o, eps), eb, gb, cb in zip(sy, e, gbs, cbs):
+        E, gs, cs = mp.rmp2_adjoint(gao=g, C=C, nocc=o, eps=eps, e_bar=0.5)
+        assert abs(E - eb) < 1e-9, (E, eb)
+        assert np.linalg.norm(gb - gs) < 1e-7 * np.linalg.norm(gs)
+        assert np.linalg.norm(cb - cs) < 1e-7 * np.linalg.norm(cs)

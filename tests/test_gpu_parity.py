@@ -112,16 +112,37 @@ def test_rccd_h2o_known_answer(jg):
     assert abs(RCCD.do_rccd(w) - E_CCD_H2O) < 1e-10          # 40 sweeps from (ij|ab)/D
 
 
-def test_rccd_per_iteration_matches_oracle(jg):
-    from juesgpu.CoupledCluster import mRCCD
-    ref = golden()["S25"]["ccd_zero_diis_8"]
-    w = make_named("S25").wfn()
-    e, log = mRCCD.do_rccd(w, maxit=8, r_conv=0.0, return_log=True)
-    assert len(log) == 8
+# per-iteration energy bars: 1e-12 Eh at nbf=25 (|E| ~ 0.03), 1e-11 Eh at nbf=100 (|E| ~ 1.4,
+# 10^6 more terms in each sum); step norms 1e-9 relative
+EBAR = {"S25": 1e-12, "S100": 1e-11}
+
+
+def check_log(log, ref, ebar):
+    assert len(log) == len(ref)
     for (it, en, rn, ms, p), (rit, ren, rrn) in zip(log, ref):
         assert it == rit
-        assert abs(en - ren) < 1e-12
-        assert abs(rn - rrn) < 1e-9 * max(1.0, rrn)
+        assert abs(en - ren) < ebar, (it, en, ren)
+        assert abs(rn - rrn) < 1e-9 * max(1.0, rrn), (it, rn, rrn)
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rccd_per_iteration_matches_oracle(jg, name):
+    # mRCCD.jl's driver: T2 = 0, DIIS (FP64) from the first sweep, 8 sweeps
+    from juesgpu.CoupledCluster import mRCCD
+    ref = golden()[name]["ccd_zero_diis_8"]
+    w = make_named(name).wfn()
+    e, log = mRCCD.do_rccd(w, maxit=8, r_conv=0.0, return_log=True)
+    check_log(log, ref, EBAR[name])
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rccd_mp2_guess_diis_trajectory_matches_oracle(jg, name):
+    # MP2 guess and DIIS to convergence: every sweep of the oracle's trajectory
+    from juesgpu.CoupledCluster import mRCCD
+    ref = golden()[name]["ccd_mp2guess_diis"]["log"]
+    w = make_named(name).wfn()
+    e, log = mRCCD.do_rccd(w, maxit=len(ref), r_conv=0.0, guess="mp2", return_log=True)
+    check_log(log, ref, EBAR[name])
 
 
 def test_rccd_amplitudes_match_oracle(jg):
@@ -157,14 +178,23 @@ def test_rccsd_h2o_known_answer(jg):
     assert abs(RCCSD.do_rccsd(h2o()) - E_CCSD_H2O) < 1e-10
 
 
-def test_rccsd_per_iteration_matches_oracle(jg):
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rccsd_per_iteration_matches_oracle(jg, name):
+    # RCCSD.jl's driver: T1 = 0, T2 = MP2, plain Jacobi sweeps
     from juesgpu.CoupledCluster._solve import solve
-    ref = golden()["S25"]["ccsd_plain_6"]
-    w = make_named("S25").wfn()
+    ref = golden()[name]["ccsd_plain_6"]
+    w = make_named(name).wfn()
     e, t1, T2, nit, log = solve(1, w, maxit=6, r_conv=0.0, diis=False, guess="mp2")
-    for (it, en, rn, ms, p), (rit, ren, rrn) in zip(log, ref):
-        assert abs(en - ren) < 1e-12
-        assert abs(rn - rrn) < 1e-9 * max(1.0, rrn)
+    check_log(log, ref, EBAR[name])
+
+
+@pytest.mark.parametrize("name", ["S25", "S100"])
+def test_rccsd_diis_trajectory_matches_oracle(jg, name):
+    from juesgpu.CoupledCluster._solve import solve
+    ref = golden()[name]["ccsd_diis"]["log"]
+    w = make_named(name).wfn()
+    e, t1, T2, nit, log = solve(1, w, maxit=len(ref), r_conv=0.0, diis=True, guess="mp2")
+    check_log(log, ref, EBAR[name])
 
 
 def test_rccsd_amplitudes_match_oracle(jg):
@@ -353,3 +383,53 @@ def test_df_rccd_session_and_errors(jg):
         CCSession(1, w, pqP=pqP)
     with pytest.raises(KeyError):
         jg.CoupledCluster.DFRCCD.do_df_rccd(w, pqP, variant="nope")
+
+
+# ------------------------------------------------------------------------------ Wfn{Float32}
+def f32_wfn(w):
+    """The Wfn{Float32} the reference's tests build (test/TestCoupledCluster.jl:23): every array
+    rounded to single precision."""
+    return wfn_from_rhf(w.Ca, w.epsa, w.ao_eri, w.nalpha, dtype=np.float32)
+
+
+def test_float32_wfn_through_the_c_abi(jg):
+    # Float32 arrays are promoted to FP64 on the way in (exactly), so the GPU must match the oracle
+    # run on the same rounded inputs at the drop-in bar
+    from juesgpu import MollerPlesset
+    from juesgpu.CoupledCluster import RCCSD, mRCCD
+    w32 = f32_wfn(make_named("S25").wfn())
+    assert w32.ao_eri.dtype == np.float32 and w32.Cao.dtype == np.float32
+    w64 = wfn_from_rhf(w32.Ca.astype(np.float64), w32.epsa.astype(np.float64),
+                       w32.ao_eri.astype(np.float64), w32.nalpha)
+    assert abs(MollerPlesset.do_rmp2(w32) - oracle.do_rmp2(w64)) < 1e-12
+    e_ccd = mRCCD.do_rccd(w32, maxit=60, r_conv=1e-11, guess="mp2")
+    assert abs(e_ccd - occd.do_rccd(w64, maxit=60, r_conv=1e-11, guess="mp2")) < 1e-10
+    e_ccsd = RCCSD.do_rccsd(w32, maxit=60, diis=True, r_conv=1e-11)
+    assert abs(e_ccsd - occsd.do_rccsd(w64, form="jl", maxit=60, diis=True, r_conv=1e-11)) < 1e-10
+
+
+def test_float32_h2o_close_to_the_known_answers(jg):
+    # the rounding of the inputs moves the H2O energies by far less than the reference's own
+    # FP32-vs-FP64 gap (7.8e-9 Eh for RCCD, test/TestCoupledCluster.jl:41-46)
+    from juesgpu import MollerPlesset
+    from juesgpu.CoupledCluster import mRCCD
+    w32 = f32_wfn(h2o())
+    assert abs(MollerPlesset.do_rmp2(w32) - E_MP2_H2O) < 1e-6
+    assert abs(mRCCD.do_rccd(w32, maxit=100, r_conv=1e-12) - E_CCD_H2O) < 1e-6
+
+
+# ------------------------------------------------------------------------------ mRCCSD.jl's Fae
+def test_mrccsd_fae_variant_matches_oracle(jg):
+    # mRCCSD.jl:140 contracts t1 with <me|af> in Fae where RCCSD.jl:190 uses <ma|ef>; the mirror of
+    # mRCCSD runs the former, checked sweep by sweep and converged against the oracle's mRCCSD form
+    from juesgpu.CoupledCluster import mRCCSD, RCCSD
+    from juesgpu.CoupledCluster._solve import solve
+    for name in ("S25", "S100"):
+        g = golden()[name]
+        w = make_named(name).wfn()
+        e, t1, T2, nit, log = solve(1, w, maxit=6, r_conv=0.0, diis=False, guess="mp2", ccsd_fae="mrccsd")
+        check_log(log, g["ccsd_m_plain_6"], EBAR[name])
+        e_m = mRCCSD.do_rccsd(w, maxit=60, diis=True, r_conv=1e-11)
+        assert abs(e_m - g["ccsd_m_diis"]["energy"]) < 1e-10
+        e_r = RCCSD.do_rccsd(w, maxit=60, diis=True, r_conv=1e-11)
+        assert abs(e_r - g["ccsd_diis"]["energy"]) < 1e-10

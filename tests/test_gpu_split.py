@@ -20,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 
 KCH = 128
+JUES_PREC_SPLIT = 1
 
 
 def split_rows(X):
@@ -323,3 +324,29 @@ def test_pack_cache_never_serves_a_freed_address(lib):
         _lib._ctxs[0] = saved
         fresh.close()
     assert e_after == e_fresh, (e_after, e_fresh)
+
+
+# ------------------------------------------------------------------------------ nbf = 200
+@pytest.fixture(scope="module")
+def s200():
+    return make_named("S200").wfn()
+
+
+def test_rmp2_default_split_s200_within_one_microhartree(lib, s200):
+    # the default split form keeps three planes in the transform: <= 1 uEh at the headline size
+    # (two planes, the opt-in "split2", gave -4.8e-6 Eh here)
+    from juesgpu import MollerPlesset
+    ref = json.load(open(os.path.join(GOLDEN, "synthetic_golden.json")))["S200"]["mp2"]
+    e = MollerPlesset.do_rmp2(s200, precision="split")
+    assert abs(e - ref) < 1e-6, (e, ref)
+
+
+def test_rccd_default_split_s200_converged_within_one_microhartree(lib, s200):
+    # the configuration the bench times: three-plane integrals, two-plane sweeps, no FP64 sweep,
+    # stopped at |dE| < 1e-7 Eh; against the FP64 oracle's converged energy
+    from juesgpu.CoupledCluster import mRCCD
+    ref = json.load(open(os.path.join(GOLDEN, "synthetic_golden.json")))["S200"]["ccd_mp2guess_diis"]["energy"]
+    e, log = mRCCD.do_rccd(s200, maxit=60, r_conv=0.0, e_conv=1e-7, guess="mp2", precision="split", refine=0,
+                           return_log=True)
+    assert len(log) < 60 and all(r[4] == JUES_PREC_SPLIT for r in log)
+    assert abs(e - ref) < 1e-6, (e, ref, len(log))

@@ -307,3 +307,22 @@ def test_auto_rccsd_oracle_pins():
                               epsa=w.epsa[1:], epsb=w.epsa[1:])
     assert abs(e_fc - ccsd.do_rccsd(act, maxit=80, diis=True)) < 1e-9
     assert abs(e_fc - e) > 1e-5
+
+
+def test_pipelined_sweep_is_the_reference_sweep():
+    # the CPU baseline's staged sweep (oracle/sampled.py) does exactly RCCD.jl's arithmetic: 16
+    # stages from the (ij|ab)/D guess equal one jl_cciter, and 32 stages two of them
+    from oracle.df_blocks import rccd_blocks_from_B
+    from oracle.sampled import PipelinedSweep
+    s = make_named("S25")
+    o = s.nocc
+    oovv, ovov, ovvo, oooo, vvvv = rccd_blocks_from_B(s.B, s.C, o)
+    ps = PipelinedSweep(oovv, ovov, ovvo, oooo, vvvv, s.eps, o, stages=16)
+    D = oracle.mp2.denominators(s.eps, o)
+    T = np.transpose(ovov, (0, 2, 1, 3)) / D
+    for sweep in range(2):
+        T = ccd.jl_cciter(T, oovv, vvvv, oooo, ovov, ovvo, D)
+        ks = [ps.step()[0] for _ in range(16)]
+        assert ks == list(range(16)) and ps.sweeps == sweep + 1
+        assert np.abs(ps.T - T).max() < 1e-13 * np.abs(T).max()
+        assert abs(ps.energy - ccd.ccenergy(T, oovv)) < 1e-13

@@ -53,3 +53,27 @@ def test_device_sweep_equals_reference_update():
     dev = device_form_sweep(T, oovv, vvvv, oooo, ovov, ovvo, D)
     assert np.abs(dev - ref).max() < 1e-12 * np.abs(ref).max()
     assert abs(energy_device_form(T, oovv) - ccd.ccenergy(T, oovv)) < 1e-13 * abs(ccd.ccenergy(T, oovv))
+
+
+def test_ccsd_wabef_t1_terms_through_y():
+    # ccsd_sweep never forms Wabef: its t1 parts, sum_ef Ttau[ij,ef] (-t1[m,b] <am|ef> - t1[m,a]
+    # <mb|ef>), become -sum_m t1[m,b] Y[ij,a,m] with Y = Ttau . <am|ef>, plus its (i,a)<->(j,b)
+    # image, which the finalisation adds (Z[i,j,a,b] + Z[j,i,b,a]).  On real integrals and a
+    # pair-symmetric Ttau the two agree to rounding.
+    from oracle import ccsd
+    w = make_named("S25").wfn()
+    oooo, ooov, oovv, ovov, ovvv, vvvv = ccsd.make_rccsd_integrals(w)
+    o, v = w.nalpha, oovv.shape[2]
+    rng = np.random.default_rng(3)
+    t1 = 0.05 * rng.normal(size=(o, v))
+    T2 = 0.05 * rng.normal(size=(o, o, v, v))
+    T2 = 0.5 * (T2 + T2.transpose(1, 0, 3, 2))                       # pair symmetry
+    Ttau = T2 + E("ia,jb->ijab", t1, t1)
+    # the reference's form: Wabef's t1 parts (<am|ef> = ovvv[m,a,f,e], <mb|ef> = ovvv[m,b,e,f])
+    W1 = -E("mb,mafe->abef", t1, ovvv) - E("ma,mbef->abef", t1, ovvv)
+    ref = E("ijef,abef->ijab", Ttau, W1)
+    # the device form: ccsd_y then ccsd_y_t1 into Z, symmetrised by t2_finalize
+    Y = E("ijef,mafe->ijam", Ttau, ovvv)
+    Z = -E("ijam,mb->ijab", Y, t1)
+    dev = Z + Z.transpose(1, 0, 3, 2)
+    assert np.abs(dev - ref).max() < 1e-14 * max(1.0, np.abs(ref).max())
