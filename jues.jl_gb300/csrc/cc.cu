@@ -600,26 +600,26 @@ double ccsd_sweep(CCState *s, int prec) {
 
     // Fae (RCCSD.jl:187-194)
     G(s, prec, "ccsd_fae", v, v, oov, -1.0, s->Tt.p, plain(oo), mode2(oo, 1, oov), W, mode2(oo, 1, oov),
-      plain(oo), 0.0, s->Fae.p, plain(1), plain(v));
+      plain(oo), 0.0, s->Fae.p, plain(1), plain(v), nullptr, false, true);
     G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, 2.0, ovvv, mode2(v, o, ovv), mode2(o, 1, ov), t1,
-      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0));
+      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0), nullptr, true, false);
     // the exchange part: t1[m,f] <ma|ef> = ovvv[m,a,e,f] (RCCSD.jl:190), or t1[m,f] <me|af> =
     // ovvv[m,e,a,f] (mRCCSD.jl:140)
     const Mode fae_rows = s->opts.ccsd_fae == JUES_CCSD_FAE_MRCCSD ? mode2(v, ov, o) : mode2(v, o, ov);
     G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, -1.0, ovvv, fae_rows, mode2(o, 1, ovv), t1,
-      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0));
+      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0), nullptr, true, false);
     // Fmi (RCCSD.jl:195-203)
     G(s, prec, "ccsd_fmi", o, o, o * vv, 1.0, W, plain(1), plain(o), s->Tt.p, plain(o), plain(1), 0.0,
-      s->Fmi.p, plain(1), plain(o));
+      s->Fmi.p, plain(1), plain(o), nullptr, true, false);
     G(s, prec, "ccsd_fmi_t1", oo, 1, ov, 2.0, ooov, mode2(o, 1, oo), mode2(o, o, ooo), t1,
-      plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0));
+      plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0), nullptr, true, false);
     G(s, prec, "ccsd_fmi_t1", oo, 1, ov, -1.0, ooov, mode2(o, o, oo), mode2(o, 1, ooo), t1,
-      plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0));
+      plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0), nullptr, true, false);
     // Fme (RCCSD.jl:204-210)
     G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
-      plain(0), 0.0, s->Fme.p, plain(1), plain(0));
+      plain(0), 0.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
     G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, -1.0, W, mode2(o, o, oo), mode2(o, 1, oov), t1, plain(1),
-      plain(0), 1.0, s->Fme.p, plain(1), plain(0));
+      plain(0), 1.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
     if (s->fock) {
         // non-canonical Fock terms: Fae += f_ae - 1/2 f_me t1[m,a], Fmi += f_mi + 1/2 t1[i,e] f_me,
         // Fme += f_me (the diagonals of f_oo and f_vv are zero; they sit in the resolvents)
@@ -634,11 +634,11 @@ double ccsd_sweep(CCState *s, int prec) {
 
     // W' = oooo + t1[j,e] ooov[m,n,i,e] + t1[i,e] ooov[n,m,j,e] + sum_ef oovv[mn,ef] (T2+tau)[ij,ef]
     G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
-      plain(1), 1.0, s->Wp.p, plain(1), plain(ooo), s->oooo.p);
+      plain(1), 1.0, s->Wp.p, plain(1), plain(ooo), s->oooo.p, true, false);
     G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
-      plain(1), 1.0, s->Wp.p, mode3(o, o, o, 1, ooo), plain(oo));
+      plain(1), 1.0, s->Wp.p, mode3(o, o, o, 1, ooo), plain(oo), nullptr, true, false);
     G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
-      plain(1), plain(oo), nullptr, false, true);
+      plain(1), plain(oo), nullptr, true, true);
     // L = oovv + W'^T (T2+tau) + (T2+tau) vvvv^T  (Wabef's t1 parts go through Y below)
     G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
       1.0, s->L.p, plain(1), plain(oo), W);
@@ -650,24 +650,24 @@ double ccsd_sweep(CCState *s, int prec) {
     const double *Tt = s->Tt.p;
     // WJ = WmBeJ (RCCSD.jl:229-238 with <mb|ej> = oovv[m,j,e,b], <mn|ej> = ooov[n,m,j,e])
     G(s, prec, "ccsd_wj", ov, ov, ov, 0.5, W, mode2(o, 1, oo), mode2(o, o, oov), Tt, mode2(o, 1, oo),
-      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p);
+      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p, true, false);
     G(s, prec, "ccsd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
-      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
+      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), nullptr, true, false);
     G(s, prec, "ccsd_wj", ov, ov, ov, -1.0, W, mode2(o, 1, oo), mode2(o, o, oov), tau, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WJ.p, plain(1), plain(ov));
+      mode2(v, oov, 1), 1.0, s->WJ.p, plain(1), plain(ov), nullptr, true, false);
     G(s, prec, "ccsd_wj_t1", ovv, o, v, 1.0, ovvv, mode3(o, v, 1, ov, o), plain(ovv), t1,
-      plain(o), plain(1), 1.0, s->WJ.p, mode3(o, v, 1, o, ov), plain(ovv));
+      plain(o), plain(1), 1.0, s->WJ.p, mode3(o, v, 1, o, ov), plain(ovv), nullptr, true, false);
     G(s, prec, "ccsd_wj_t1", ov * o, v, o, -1.0, ooov, mode3(o, v, o, ooo, oo), plain(1), t1,
-      plain(1), plain(o), 1.0, s->WJ.p, mode3(o, v, 1, o, ovv), plain(ov));
+      plain(1), plain(o), 1.0, s->WJ.p, mode3(o, v, 1, o, ovv), plain(ov), nullptr, true, false);
     // WK = WmBEj (RCCSD.jl:239-247 with <bm|ej> = ovov[m,b,j,e], <nm|ej> = ooov[m,n,j,e])
     G(s, prec, "ccsd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p);
+      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p, true, false);
     G(s, prec, "ccsd_wk", ov, ov, ov, 1.0, W, mode2(o, o, oo), mode2(o, 1, oov), tau, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov));
+      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), nullptr, true, false);
     G(s, prec, "ccsd_wk_t1", ovv, o, v, -1.0, ovvv, mode3(o, v, 1, ovv, o), plain(ov), t1,
-      plain(o), plain(1), 1.0, s->WK.p, mode3(o, v, 1, o, ov), plain(ovv));
+      plain(o), plain(1), 1.0, s->WK.p, mode3(o, v, 1, o, ov), plain(ovv), nullptr, true, false);
     G(s, prec, "ccsd_wk_t1", ov * o, v, o, 1.0, ooov, mode3(o, v, 1, ooo, oo), plain(o), t1,
-      plain(1), plain(o), 1.0, s->WK.p, mode3(o, v, 1, o, ovv), plain(ov));
+      plain(1), plain(o), 1.0, s->WK.p, mode3(o, v, 1, o, ovv), plain(ov), nullptr, true, false);
     axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
 
     // T1 (RCCSD.jl:248-259) into t1n, before the amplitudes change
@@ -679,13 +679,13 @@ double ccsd_sweep(CCState *s, int prec) {
     G(s, prec, "ccsd_t1", ov, 1, ov, 1.0, Tt, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
       plain(1), plain(0), 1.0, R1, plain(1), plain(0));
     G(s, prec, "ccsd_t1", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
-      plain(0), 1.0, R1, plain(1), plain(0));
+      plain(0), 1.0, R1, plain(1), plain(0), nullptr, true, false);
     G(s, prec, "ccsd_t1", ov, 1, ov, -1.0, ovov, mode2(o, ov, o), mode2(o, 1, oov), t1,
-      plain(1), plain(0), 1.0, R1, plain(1), plain(0));
+      plain(1), plain(0), 1.0, R1, plain(1), plain(0), nullptr, true, false);
     G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, ooov, plain(oo), mode2(oo, 1, ooo), Tt,
-      mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o));
+      mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o), nullptr, true, false);
     G(s, prec, "ccsd_t1_ovvv", o, v, ovv, 1.0, Tt, plain(1), mode3(o, v, o, oo, oov), ovvv,
-      mode3(o, v, 1, ovv, ov), plain(o), 1.0, R1, plain(1), plain(o));
+      mode3(o, v, 1, ovv, ov), plain(o), 1.0, R1, plain(1), plain(o), nullptr, false, true);
 
     // F~ae[b,e] = Fae - 1/2 t1[m,b] Fme[m,e];  F~mi[m,j] = Fmi + 1/2 Fme[m,e] t1[j,e]
     G(s, prec, "ccsd_ftilde", v, v, o, -0.5, t1, plain(o), plain(1), s->Fme.p, plain(1),
@@ -714,20 +714,20 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
     // - tau[i,m,e,a] <mb|ej>: Y1[i,m,j,b] = sum_e t1[i,e] oovv[m,j,e,b]; Z -= sum_m t1[m,a] Y1[i,m,j,b]
     G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo),
-      mode3(o, o, 1, o, oov), 0.0, Y, plain(1), plain(o));
+      mode3(o, o, 1, o, oov), 0.0, Y, plain(1), plain(o), nullptr, false, true);
     G(s, prec, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, o, 1, oo, ooo), plain(o), t1,
       plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
     // - tau[i,m,e,b] <am|ej>: Y2[i,m,a,j] = sum_e t1[i,e] ovov[m,a,j,e]; Z -= sum_m Y2 t1[m,b]
     G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov),
-      plain(1), 0.0, Y, plain(1), plain(o));
+      plain(1), 0.0, Y, plain(1), plain(o), nullptr, false, true);
     G(s, prec, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, v, 1, oo, oov), plain(o), t1,
       plain(1), plain(o), 1.0, Z, mode3(o, v, 1, oo, o), plain(oov));
     // + t1[i,e] <ab|ej> = t1[i,e] ovvv[j,a,b,e]
     G(s, prec, "ccsd_z_ovvv", o, ovv, v, 1.0, t1, plain(1), plain(o), ovvv, plain(ovv), plain(1), 1.0, Z,
-      plain(1), plain(o));
+      plain(1), plain(o), nullptr, false, true);
     // - t1[m,a] <mb|ij> = t1[m,a] ooov[m,j,i,b]
     G(s, prec, "ccsd_z_ooov", oov, v, o, -1.0, ooov, mode3(o, o, oo, o, ooo), plain(1), t1,
-      plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
+      plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo), nullptr, true, false);
 
     if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia
     double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p);

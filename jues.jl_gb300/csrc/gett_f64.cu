@@ -190,6 +190,47 @@ __global__ void __launch_bounds__(NT) gett_f64_grouped(const GroupProblem *__res
     }
 }
 
+// Offset of a mode index that advances by a fixed step: the division-free successor of
+// mode_off (the carries replace the divisions), so a K loop costs a few integer adds per
+// element instead of 32- or 64-bit divisions.
+struct ModeIter {
+    long long i0, i1, off;
+    __device__ __forceinline__ void init(const Mode &m, long long r) {
+        if (m.d0 == MODE_BIG) {
+            i0 = r;
+            i1 = 0;
+            off = r * m.s0;
+            return;
+        }
+        long long q;
+        divmod_ll(r, m.d0, q, i0);
+        if (m.d1 == MODE_BIG) {
+            i1 = q;
+            off = i0 * m.s0 + q * m.s1;
+            return;
+        }
+        long long q2;
+        divmod_ll(q, m.d1, q2, i1);
+        off = i0 * m.s0 + i1 * m.s1 + q2 * m.s2;
+    }
+    __device__ __forceinline__ void step(const Mode &m, int by) {
+        if (m.d0 == MODE_BIG) {
+            off += by * m.s0;
+            return;
+        }
+        i0 += by;
+        off += by * m.s0;
+        while (i0 >= m.d0) {
+            i0 -= m.d0;
+            off += m.s1 - m.d0 * m.s0;
+            if (m.d1 != MODE_BIG && ++i1 >= m.d1) {
+                i1 = 0;
+                off += m.s2 - m.d1 * m.s1;
+            }
+        }
+    }
+};
+
 // skinny GEMM (N <= 8): one warp per output row, lanes split K
 __global__ void gett_f64_skinny(GroupProblem g) {
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -203,12 +244,17 @@ __global__ void gett_f64_skinny(GroupProblem g) {
     long long onb[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) onb[j] = j < g.N ? mode_off(g.nB, j) : 0;
+    ModeIter ia, ib;
+    ia.init(g.kA, lane);
+    ib.init(g.kB, lane);
     for (long long k = lane; k < g.K; k += 32) {
-        const double a = __ldg(g.A + om + mode_off(g.kA, k));
-        const long long ok = mode_off(g.kB, k);
+        const double a = __ldg(g.A + om + ia.off);
+        const long long ok = ib.off;
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (j < g.N) acc[j] = fma(a, __ldg(g.B + ok + onb[j]), acc[j]);
+        ia.step(g.kA, 32);
+        ib.step(g.kB, 32);
     }
     const long long oc = mode_off(g.mC, m);
 #pragma unroll

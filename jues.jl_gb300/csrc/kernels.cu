@@ -253,9 +253,10 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
 }
 
 // The same finalisation with the (i,j) transposes through shared memory: block p handles the
-// pair (a <= b); Z[:,:,a,b] and Z[:,:,b,a] are contiguous o x o blocks, loaded coalesced into
-// shared memory on an odd row pitch (conflict-free transposed reads), so every global access is
-// unit-stride.  Dynamic shared memory 2 o pitch doubles (o <= 64).
+// pair (a <= b) (one pair per block, so resident blocks overlap their load and compute phases);
+// Z[:,:,a,b] and Z[:,:,b,a] are contiguous o x o blocks, loaded coalesced into shared memory on
+// an odd row pitch (conflict-free transposed reads), so every global access is unit-stride.
+// Dynamic shared memory 2 o pitch doubles (o <= 64).
 __global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__restrict__ L,
                                                                const double *__restrict__ Z,
                                                                const double *__restrict__ invD, int o, int v,
@@ -267,11 +268,12 @@ __global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__r
     const long long npair = (long long)v * (v + 1) / 2;
     const int ooi = o * o;
     double acc = 0.0;
-    for (long long p = blockIdx.x; p < npair; p += gridDim.x) {
+    (void)npair;
+    {
+        const long long p = blockIdx.x;   // one (a <= b) pair per block: blocks overlap their phases
         int a, b;
         pair_ab(p, a, b);
         const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
-        __syncthreads();   // the previous pair's reads of zs are done
         for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
             const int i = ij % o, j = ij / o;
             zs[j + pitch * i] = Z[ab + ij];
@@ -601,7 +603,8 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
     int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
     {
         Ctx::Scope s(ctx, "t2_finalize");
-        if (o <= 64) {
+        // one block per pair; the step norm's partials (one per block) must fit the reduction scratch
+        if (o <= 64 && npair <= 65536 - 64) {
             const size_t smem = (size_t)2 * o * (o | 1) * sizeof(double);
             static std::atomic<unsigned long long> attr_set{0};
             const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
@@ -610,6 +613,7 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
                 attr_set.fetch_or(bit);
             }
+            nb = (int)npair;
             t2_finalize_smem_kernel<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
         } else {
             t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
