@@ -332,19 +332,19 @@ CCState *cc_create(Ctx *ctx, int method, const double *g, int n, const double *C
     s->oooo = DBuf<double>(ctx, (size_t)(oo * oo));
     s->vvvv = DBuf<double>(ctx, (size_t)(vv * vv));
     Ctx::HostPhase ph_blocks(ctx, "host:integral_blocks");
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOVV", true, 0, s->oovv.p, true);
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVOV", true, 0, s->ovov.p, true);
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OOOO", true, 0, s->oooo.p, true);
-    get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "VVVV", true, 0, s->vvvv.p, true);
+    // the blocks share their common quarter steps (the occupied blocks' first quarter)
+    std::vector<std::pair<std::string, double *>> blocks = {
+        {"OOVV", s->oovv.p}, {"OVOV", s->ovov.p}, {"OOOO", s->oooo.p}, {"VVVV", s->vvvv.p}};
     if (method == 0) {
         s->ovvo = DBuf<double>(ctx, t2n);
-        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "OVVO", true, 0, s->ovvo.p, true);
+        blocks.push_back({"OVVO", s->ovvo.p});
     } else {
         s->ooov = DBuf<double>(ctx, (size_t)(oo * ov));
         s->ovvv = DBuf<double>(ctx, (size_t)(ov * vv));
-        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ooov", true, 0, s->ooov.p, true);
-        get_eri_block(ctx, iprec, g, n, Cocc, o, Cvir, v, "ovvv", true, 0, s->ovvv.p, true);
+        blocks.push_back({"ooov", s->ooov.p});
+        blocks.push_back({"ovvv", s->ovvv.p});
     }
+    get_eri_blocks(ctx, iprec, g, n, Cocc, o, Cvir, v, blocks, true, 0, true);
     pack_cache_drop(ctx, g);
     return cc_finish(std::move(s));
 }
