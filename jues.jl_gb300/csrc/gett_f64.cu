@@ -194,24 +194,26 @@ __global__ void __launch_bounds__(NT) gett_f64_grouped(const GroupProblem *__res
 // mode_off (the carries replace the divisions), so a K loop costs a few integer adds per
 // element instead of 32- or 64-bit divisions.
 struct ModeIter {
-    long long i0, i1, off;
+    int i0, i1;          // the mode's first two sub-indices (unused for a single-stride mode)
+    long long off;
     __device__ __forceinline__ void init(const Mode &m, long long r) {
         if (m.d0 == MODE_BIG) {
-            i0 = r;
-            i1 = 0;
+            i0 = i1 = 0;
             off = r * m.s0;
             return;
         }
-        long long q;
-        divmod_ll(r, m.d0, q, i0);
+        long long q, r0;
+        divmod_ll(r, m.d0, q, r0);
+        i0 = (int)r0;
         if (m.d1 == MODE_BIG) {
-            i1 = q;
-            off = i0 * m.s0 + q * m.s1;
+            i1 = 0;
+            off = r0 * m.s0 + q * m.s1;
             return;
         }
-        long long q2;
-        divmod_ll(q, m.d1, q2, i1);
-        off = i0 * m.s0 + i1 * m.s1 + q2 * m.s2;
+        long long q2, r1;
+        divmod_ll(q, m.d1, q2, r1);
+        i1 = (int)r1;
+        off = r0 * m.s0 + r1 * m.s1 + q2 * m.s2;
     }
     __device__ __forceinline__ void step(const Mode &m, int by) {
         if (m.d0 == MODE_BIG) {
@@ -221,7 +223,7 @@ struct ModeIter {
         i0 += by;
         off += by * m.s0;
         while (i0 >= m.d0) {
-            i0 -= m.d0;
+            i0 -= (int)m.d0;
             off += m.s1 - m.d0 * m.s0;
             if (m.d1 != MODE_BIG && ++i1 >= m.d1) {
                 i1 = 0;
@@ -231,34 +233,48 @@ struct ModeIter {
     }
 };
 
-// skinny GEMM (N <= 8): one warp per output row, lanes split K
-__global__ void gett_f64_skinny(GroupProblem g) {
+// skinny GEMM (N <= NN <= 8): one warp per output row, lanes split K
+template <int NN>
+__global__ void __launch_bounds__(256, NN == 1 ? 3 : 2) gett_f64_skinny(GroupProblem g) {
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= g.M) return;
     const long long m = warp;
     const long long om = mode_off(g.mA, m);
-    double acc[8];
+    double acc[NN];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] = 0.0;
-    long long onb[8];
+    for (int j = 0; j < NN; ++j) acc[j] = 0.0;
+    long long onb[NN];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) onb[j] = j < g.N ? mode_off(g.nB, j) : 0;
-    ModeIter ia, ib;
-    ia.init(g.kA, lane);
-    ib.init(g.kB, lane);
-    for (long long k = lane; k < g.K; k += 32) {
-        const double a = __ldg(g.A + om + ia.off);
-        const long long ok = ib.off;
+    for (int j = 0; j < NN; ++j) onb[j] = j < g.N ? mode_off(g.nB, j) : 0;
+    // four independent K positions per lane (k, k + 32, k + 64, k + 96): their loads are in
+    // flight together instead of one load latency per element
+    constexpr int U = 4;
+    ModeIter ia[U], ib[U];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (j < g.N) acc[j] = fma(a, __ldg(g.B + ok + onb[j]), acc[j]);
-        ia.step(g.kA, 32);
-        ib.step(g.kB, 32);
+    for (int u = 0; u < U; ++u) {
+        ia[u].init(g.kA, lane + 32 * u);
+        ib[u].init(g.kB, lane + 32 * u);
+    }
+    for (long long k = lane; k < g.K; k += 32 * U) {
+        double a[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) a[u] = k + 32 * u < g.K ? __ldg(g.A + om + ia[u].off) : 0.0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (k + 32 * u < g.K) {
+                const long long ok = ib[u].off;
+#pragma unroll
+                for (int j = 0; j < NN; ++j)
+                    if (j < g.N) acc[j] = fma(a[u], __ldg(g.B + ok + onb[j]), acc[j]);
+            }
+            ia[u].step(g.kA, 32 * U);
+            ib[u].step(g.kB, 32 * U);
+        }
     }
     const long long oc = mode_off(g.mC, m);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < NN; ++j) {
         if (j >= g.N) break;
         double v = acc[j];
 #pragma unroll
@@ -294,7 +310,10 @@ void gett_f64(Ctx *ctx, const GettArgs &a, const char *name) {
         long long blocks = (a.M * 32 + 255) / 256;
         JUES_REQUIRE(blocks < (1LL << 31), "GEMM too large for one launch");
         Ctx::Scope s(ctx, name);
-        gett_f64_skinny<<<(unsigned)blocks, 256, 0, ctx->stream>>>(g);
+        if (a.N == 1)
+            gett_f64_skinny<1><<<(unsigned)blocks, 256, 0, ctx->stream>>>(g);
+        else
+            gett_f64_skinny<8><<<(unsigned)blocks, 256, 0, ctx->stream>>>(g);
         JUES_CHECK_CUDA(cudaGetLastError());
         return;
     }
