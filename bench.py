@@ -458,7 +458,7 @@ def run_gpu(args):
     ring_ms, ring_n = ctx.profile("ccd_ring")
     pack_ms, pack_n = ctx.profile("pack_split")
     other_ms = {k: sum(ctx.profile(p)[0] for p in ps) / args.steps
-                for k, ps in (("fae_fmi", ("ccd_fae", "ccd_fmi", "ccd_z_fae", "wp_fmi")),
+                for k, ps in (("fae_fmi", ("fmi_trace", "fae_trace", "wp_fmi")),
                               ("x_hh_ladder", ("ccd_x", "ccd_hh_ladder")),
                               ("wj_wk", ("ccd_wj", "ccd_wk")),
                               ("t2_finalize", ("t2_finalize",)),

@@ -60,7 +60,72 @@ void d2d(Ctx *ctx, double *dst, const double *src, size_t n) {
     JUES_CHECK_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
 }
 
+// a non-owning view of n doubles of another buffer (no context: never freed through it)
+DBuf<double> view_of(double *p, size_t n) {
+    DBuf<double> d;
+    d.p = p;
+    d.n = n;
+    return d;
+}
+
 }  // namespace
+
+// ---------------------------------------------------------------------------------------
+// The ring contractions in split precision, on K-stacked packs (gett_tc_views).  With the
+// block width kb = roundup(ov, 128) and T2 read in the ring GEMMs' two layouts,
+//   R1 = T2[i,m,a,e] (rows (i,a), K (m,e)) and R23 = T2[m,i,a,e] (the same rows, m unit-stride),
+// and U (CCSD: T2 + 2 tau; CCD: T2) in the R23 layout:
+//   WJ  = J0 + [1/2 oovvT | -1/2 oovv] . [R1 ; U23]    (one GEMM, K = 2 ov)
+//   WK  = K0 + 1/2 oovv[n,m,e,f] . U23
+//   Z   = [R23 | R1] . [-WJ ; W12]                     (one GEMM, K = 2 ov)
+//       + R23 (rows (i,b)) . WK (columns (a,j))
+// Rows of WJ / WK are (m,e), columns (j,b); the weights are packed once (stackW).
+// ---------------------------------------------------------------------------------------
+static void ring_stacks_begin(CCState *s, const double *U) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v;
+    const long long kb = (ov + 127) / 128 * 128;
+    const bool ccsd = s->method == 1;
+    if (!s->stackW.buf.p) {
+        s->stackW.ensure(ctx, ov, 3 * kb, 2);
+        const double *wt = (s->reference_df_wmbej ? s->oovv.p : s->oovvT.p);
+        // CCD [-1/2 oovv | 1/2 oovvT | 1/2 oovv'], CCSD [1/2 oovvT | -1/2 oovv | 1/2 oovv']:
+        // rows (m,e), K (n,f)
+        pack_stacked(ctx, s->stackW, ccsd ? kb : 0, s->oovv.p, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, -0.5);
+        pack_stacked(ctx, s->stackW, ccsd ? 0 : kb, wt, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, 0.5);
+        pack_stacked(ctx, s->stackW, 2 * kb, s->oovv.p, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 0.5);
+    }
+    s->stackT.ensure(ctx, ov, (ccsd ? 3 : 2) * kb, 2);
+    pack_stacked(ctx, s->stackT, 0, s->T.p, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 1.0);    // R23
+    pack_stacked(ctx, s->stackT, kb, s->T.p, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, 1.0);   // R1
+    if (ccsd) pack_stacked(ctx, s->stackT, 2 * kb, U, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 1.0);
+    const Mode jb = mode2(o, ov * v, ov);
+    d2d(ctx, s->WJ.p, s->ovvoJ.p, (size_t)(ov * ov));
+    d2d(ctx, s->WK.p, s->ovovK.p, (size_t)(ov * ov));
+    // CCD: [R23 | R1] against [-1/2 oovv | 1/2 oovvT]; CCSD: [R1 | U23] against [1/2 oovvT | -1/2 oovv]
+    gett_tc_views(ctx, s->stackW.view(0, 2 * kb), s->stackT.view(ccsd ? kb : 0, 2 * kb), ov, ov, 1.0, 1.0, s->WJ.p,
+                  plain(1), jb, nullptr, ccsd ? "ccsd_wj" : "ccd_wj");
+    gett_tc_views(ctx, s->stackW.view(2 * kb, kb), s->stackT.view(ccsd ? 2 * kb : 0, kb), ov, ov, 1.0, 1.0, s->WK.p,
+                  plain(1), jb, nullptr, ccsd ? "ccsd_wk" : "ccd_wk");
+}
+
+// Z = [R23 | R1] . [-WJ ; W12] (beta 0), then Z += R23 . WK
+static void ring_stacks_z(CCState *s) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v;
+    const long long kb = (ov + 127) / 128 * 128;
+    const bool ccsd = s->method == 1;
+    s->stackR.ensure(ctx, ov, 2 * kb, 2);
+    pack_stacked(ctx, s->stackR, 0, s->WJ.p, plain(ov), plain(1), ov, ov, -1.0);
+    pack_stacked(ctx, s->stackR, kb, s->W12.p, plain(ov), plain(1), ov, ov, 1.0);
+    s->stackK.ensure(ctx, ov, kb, 2);
+    pack_stacked(ctx, s->stackK, 0, s->WK.p, plain(ov), plain(1), ov, ov, 1.0);
+    const char *name = ccsd ? "ccsd_ring" : "ccd_ring";
+    gett_tc_views(ctx, s->stackT.view(0, 2 * kb), s->stackR.view(0, 2 * kb), ov, ov, 1.0, 0.0, s->Z.p,
+                  mode2(o, 1, oo), mode2(v, oov, o), nullptr, name);
+    gett_tc_views(ctx, s->stackT.view(0, kb), s->stackK.view(0, kb), ov, ov, 1.0, 1.0, s->Z.p, mode2(o, 1, oov),
+                  mode2(v, oo, o), nullptr, name);
+}
 
 // ---------------------------------------------------------------------------------------
 // CCD sweep (FP64 or split precision for the contractions; everything else FP64)
@@ -72,23 +137,16 @@ double ccd_sweep(CCState *s, int prec) {
     // Every operand of this sweep is read-only once formed, so its split-precision packs can be
     // shared between the GEMMs that use it; the buffers that change from sweep to sweep lose
     // their packs here (the integrals keep theirs).
-    for (const double *p : {s->T.p, s->Tn.p, s->Tt.p, s->Wp.p, s->WJ.p, s->WK.p, s->W12.p, s->Fae.p, s->Fmi.p})
+    for (const double *p : {s->T.p, s->Tn.p, s->Wp.p, s->WJ.p, s->WK.p, s->W12.p, s->Fae.p, s->Fmi.p})
         pack_cache_drop(ctx, p);
     s->cache_operands = is_split(prec);
-    // T~[i,j,a,b] = 2T[i,j,a,b] - T[j,i,a,b]
-    t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
-    const double *Tt = s->Tt.p;
     const double *W = s->oovv.p;
 
-    // Fae[a,e] = -sum_{mnf} T~[m,n,a,f] oovv[m,n,e,f]                    (RCCD.jl:179)
-    G(s, prec, "ccd_fae", v, v, oov, -1.0, Tt, plain(oo), mode2(oo, 1, oov), W, mode2(oo, 1, oov),
-      plain(oo), 0.0, s->Fae.p, plain(1), plain(v));
-    // Fmi[m,i] = sum_{nef} oovv[m,n,e,f] T~[i,n,e,f]                      (RCCD.jl:216)
-    G(s, prec, "ccd_fmi", o, o, o * vv, 1.0, W, plain(1), plain(o), Tt, plain(o), plain(1), 0.0,
-      s->Fmi.p, plain(1), plain(o));
-    // W'[mn,ij] = oooo[mn,ij] + sum_ef oovv[mn,ef] T[ij,ef]        (Wmnij + the Wabef T-part)
+    // W'[mn,ij] = oooo[mn,ij] + X[mn,ij], X = sum_ef oovv[mn,ef] T[ij,ef]  (Wmnij + the Wabef T-part)
     G(s, prec, "ccd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), T, plain(oo), plain(1), 1.0, s->Wp.p,
       plain(1), plain(oo), s->oooo.p);
+    // Fmi[m,i] = sum_nef oovv[m,n,e,f] T~[i,n,e,f] = sum_n 2 X[mn,in] - X[mn,ni]      (RCCD.jl:216)
+    fmi_from_x(ctx, s->Wp.p, s->oooo.p, (int)o, s->Fmi.p);
     // - T[i,m,a,b] Fmi[m,j] - T[m,j,a,b] Fmi[m,i] (RCCD.jl:244) as hole-hole ladder terms:
     // W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i]
     wp_fmi(ctx, s->Wp.p, s->Fmi.p, (int)o);
@@ -98,37 +156,54 @@ double ccd_sweep(CCState *s, int prec) {
     G(s, prec, "ccd_pp_ladder", oo, vv, vv, 1.0, T, plain(1), plain(oo), s->vvvv.p, plain(vv), plain(1),
       1.0, s->L.p, plain(1), plain(oo), nullptr, false, true);
 
-    // ring intermediates in (me),(bj) layout
-    // WJ = WmBeJ = ovvo + 1/2 oovv[m,n,e,f] T~[n,j,f,b] - 1/2 oovv[n,m,e,f] T[n,j,f,b]  (RCCD.jl:400)
-    G(s, prec, "ccd_wj", ov, ov, ov, 0.5, W, mode2(o, 1, oo), mode2(o, o, oov), Tt, mode2(o, 1, oo),
-      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p);
-    if (s->reference_df_wmbej)
-        // DF-RCCD.jl:239-242 reads the last term as oovv[m,n,e,f] T[n,j,f,b] (bov[m,e]bov[n,f])
-        G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, 1, oo), mode2(o, o, oov), T, mode2(o, 1, oo),
-          mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
-    else
-        G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
-          mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov));
-    // WK = WmBEj = -ovov[m,b,j,e] + 1/2 T[j,n,f,b] oovv[n,m,e,f]                  (RCCD.jl:445)
-    G(s, prec, "ccd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p);
+    // Ring intermediates in (me),(bj) layout, their columns taken in (j,b) order.  With the pair
+    // symmetry T[i,j,a,b] = T[j,i,b,a] and oovvT = 2 oovv[m,n,e,f] - oovv[n,m,e,f]:
+    //   WmBeJ = ovvo + 1/2 oovv[m,n,e,f] T~[n,j,f,b] - 1/2 oovv[n,m,e,f] T[n,j,f,b]   (RCCD.jl:400)
+    //         = ovvo + 1/2 oovvT[m,n,e,f] T[j,n,b,f] - 1/2 oovv[m,n,e,f] T[n,j,b,f]
+    //   WmBEj = -ovov[m,b,j,e] + 1/2 T[j,n,f,b] oovv[n,m,e,f]                    (RCCD.jl:445)
+    //         = -ovov[m,b,j,e] + 1/2 oovv[n,m,e,f] T[n,j,b,f]
+    // so T enters as B in the two layouts the ring GEMMs below read it as A (one pack each) and
+    // no T~ is formed.  DF-RCCD.jl:239-242 reads WmBeJ's last term as oovv[m,n,e,f] T[n,j,f,b];
+    // then the first term's weights are oovv instead of oovvT.
+    // In split precision the two WmBeJ GEMMs and the first two ring GEMMs run K-stacked.
+    const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;   // two planes
+    const Mode jb = mode2(o, ov * v, ov);   // column (j,b) of a [(m,e),(b,j)] array
+    if (stacked) {
+        ring_stacks_begin(s, T);
+    } else {
+        d2d(ctx, s->WJ.p, s->ovvoJ.p, (size_t)(ov * ov));
+        d2d(ctx, s->WK.p, s->ovovK.p, (size_t)(ov * ov));
+        G(s, prec, "ccd_wj", ov, ov, ov, 0.5, s->reference_df_wmbej ? W : s->oovvT.p, mode2(o, 1, oo),
+          mode2(o, o, oov), T, mode2(o, o, oov), mode2(o, 1, oo), 1.0, s->WJ.p, plain(1), jb, nullptr, true);
+        G(s, prec, "ccd_wj", ov, ov, ov, -0.5, W, mode2(o, 1, oo), mode2(o, o, oov), T, mode2(o, 1, oov),
+          mode2(o, o, oo), 1.0, s->WJ.p, plain(1), jb, nullptr, true);
+        G(s, prec, "ccd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oov),
+          mode2(o, o, oo), 1.0, s->WK.p, plain(1), jb, nullptr, true);
+    }
     // W12 = 2 WJ + WK
     axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
+    // Fae[a,e] = -sum_{mnf} T~[m,n,a,f] oovv[m,n,e,f] (RCCD.jl:179) from the traces over m of the
+    // GEMM parts of WJ and WK at [(m,e),(a,m)]: -(tJ + 2 tK), or -2(tJ + tK) in the DF-RCCD.jl
+    // form; then W12[(j,e),(b,j)] += Fae[b,e], so that the first ring GEMM also gives the
+    // T[i,j,a,e] Fae[b,e] term of RCCD.jl:243
+    fae_from_rings(ctx, s->WJ.p, s->ovvoJ.p, s->WK.p, s->ovovK.p, (int)o, (int)v, s->reference_df_wmbej ? 2.0 : 1.0,
+                   2.0, s->Fae.p, s->W12.p);
 
     // Z: the terms of RCCD.jl:243-254 whose (i,a)<->(j,b) images are added by t2_finalize
     double *Z = s->Z.p;
-    // + T[i,j,a,e] Fae[b,e]
-    G(s, prec, "ccd_z_fae", oov, v, v, 1.0, T, plain(1), plain(oov), s->Fae.p, plain(v), plain(1), 0.0,
-      Z, plain(1), plain(oov));
-    // + T[i,m,a,e] (2WmBeJ + WmBEj)[m,b,e,j]
-    G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
-      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
-    // - T[m,i,a,e] WmBeJ[m,b,e,j]
-    G(s, prec, "ccd_ring", ov, ov, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WJ.p, plain(1),
-      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
-    // + T[m,i,b,e] WmBEj[m,a,e,j]
-    G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
-      plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
+    if (stacked) {
+        ring_stacks_z(s);
+    } else {
+        // + T[i,m,a,e] (2WmBeJ + WmBEj + [m = j] Fae)[m,b,e,j]
+        G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
+          plain(ov), 0.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
+        // - T[m,i,a,e] WmBeJ[m,b,e,j]
+        G(s, prec, "ccd_ring", ov, ov, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WJ.p, plain(1),
+          plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
+        // + T[m,i,b,e] WmBEj[m,a,e,j]
+        G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
+          plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
+    }
 
     s->cache_operands = false;
     // with DIIS the step norm comes from its error vector (the same |Tn - T|^2), so the
@@ -278,15 +353,37 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         Perm4 q{{o, v, v, o}, {1, ov * o, o, ov}, {1, o, ov, ov * v}};
         permute4(ctx, q, -1.0, s->ovov.p, 0.0, s->ovovK.p);
     }
-    if (method == 0) {
-        s->oovvT = DBuf<double>(ctx, t2n);
-        t_tilde(ctx, s->oovv.p, o, v, s->oovvT.p);
+    s->oovvT = DBuf<double>(ctx, t2n);
+    t_tilde(ctx, s->oovv.p, o, v, s->oovvT.p);
+    if (method == 1) {
+        // ooovT[m,n,i,e] = 2 ooov[m,n,i,e] - ooov[n,m,i,e]; c1, c2 = the ooov diagonal sums
+        const size_t n3 = (size_t)(oo * ov);
+        s->ooovT = DBuf<double>(ctx, n3);
+        DBuf<double> sw(ctx, n3);
+        Perm4 p{{o, o, o, v}, {o, 1, oo, oo * o}, {1, o, oo, oo * o}};
+        permute4(ctx, p, 1.0, s->ooov.p, 0.0, sw.p);
+        axpby(ctx, n3, 2.0, s->ooov.p, -1.0, sw.p, s->ooovT.p);
+        s->c12 = DBuf<double>(ctx, (size_t)(2 * ov));
+        ooov_diag_sums(ctx, s->ooov.p, o, v, s->c12.p);
     }
     s->invD = DBuf<double>(ctx, t2n);
     inv_denominators(ctx, s->eps.p, o, v, s->invD.p);
-    s->T = DBuf<double>(ctx, t2n);
-    s->Tn = DBuf<double>(ctx, t2n);
-    s->Tt = DBuf<double>(ctx, t2n);
+    if (method == 1) {
+        // [t1 | pad | T2] contiguous for DIIS, T2 16-byte aligned; the pad stays zero
+        s->xoff = (size_t)(ov + 1) / 2 * 2;
+        s->X = DBuf<double>(ctx, s->xoff + t2n);
+        s->Xn = DBuf<double>(ctx, s->xoff + t2n);
+        fill(ctx, s->X.p, s->xoff, 0.0);
+        fill(ctx, s->Xn.p, s->xoff, 0.0);
+        s->t1 = view_of(s->X.p, (size_t)ov);
+        s->T = view_of(s->X.p + s->xoff, t2n);
+        s->t1n = view_of(s->Xn.p, (size_t)ov);
+        s->Tn = view_of(s->Xn.p + s->xoff, t2n);
+    } else {
+        s->T = DBuf<double>(ctx, t2n);
+        s->Tn = DBuf<double>(ctx, t2n);
+    }
+    if (method == 1) s->Tt = DBuf<double>(ctx, t2n);   // the CCD sweep forms no T~
     s->Z = DBuf<double>(ctx, t2n);
     s->L = DBuf<double>(ctx, t2n);
     s->Wp = DBuf<double>(ctx, (size_t)(oo * oo));
@@ -296,9 +393,10 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
     s->Fae = DBuf<double>(ctx, (size_t)vv);
     s->Fmi = DBuf<double>(ctx, (size_t)oo);
     if (method == 1) {
-        s->t1 = DBuf<double>(ctx, (size_t)ov);
-        s->t1n = DBuf<double>(ctx, (size_t)ov);
         s->Fme = DBuf<double>(ctx, (size_t)ov);
+        s->U = DBuf<double>(ctx, t2n);
+        s->Fmt = DBuf<double>(ctx, (size_t)oo);
+        s->fwork = DBuf<double>(ctx, (size_t)(4 * vv + ov));
         fill(ctx, s->t1.p, (size_t)ov, 0.0);
     }
     // initial amplitudes
@@ -426,18 +524,17 @@ CCState *cc_create_auto(Ctx *ctx, const double *g, const double *h, int n, const
     d2d(ctx, s->t1n.p, s->fOV.p, (size_t)o * v);
     fill(ctx, s->t1.p, (size_t)o * v, 0.0);
     t1_finalize(ctx, s->t1n.p, s->eps.p, o, v, s->t1.p);
-    std::swap(s->t1, s->t1n);
+    d2d(ctx, s->t1.p, s->t1n.p, (size_t)o * v);
     s->energy = cc_total_energy(s.get());
     s->e_prev = s->energy;
     ctx->check_flags();
     return s.release();
 }
 
-// amplitude vector for DIIS: CCD = T2; CCSD = [t1; T2] packed in aux1
+// amplitude vector for DIIS: CCD = T2; CCSD = [t1 | pad | T2] (the X buffer)
 static void cc_one(CCState *s, int prec) {
     Ctx *ctx = s->ctx;
     const size_t t2n = (size_t)s->o * s->o * s->v * s->v;
-    const size_t t1n = (size_t)s->o * s->v;
     cudaEvent_t e0, e1;
     JUES_CHECK_CUDA(cudaEventCreate(&e0));
     JUES_CHECK_CUDA(cudaEventCreate(&e1));
@@ -454,20 +551,14 @@ static void cc_one(CCState *s, int prec) {
             diis_step(s, s->T.p, s->Tn.p, t2n, &ee);
             if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
         } else {
-            // pack [t1; T2] contiguously for the DIIS vectors
-            if (s->aux1.n < t1n + t2n) s->aux1 = DBuf<double>(ctx, t1n + t2n);
-            if (s->aux2.n < t1n + t2n) s->aux2 = DBuf<double>(ctx, t1n + t2n);
-            d2d(ctx, s->aux1.p, s->t1.p, t1n);
-            d2d(ctx, s->aux1.p + t1n, s->T.p, t2n);
-            d2d(ctx, s->aux2.p, s->t1n.p, t1n);
-            d2d(ctx, s->aux2.p + t1n, s->Tn.p, t2n);
-            diis_step(s, s->aux1.p, s->aux2.p, t1n + t2n);
-            d2d(ctx, s->t1.p, s->aux1.p, t1n);
-            d2d(ctx, s->T.p, s->aux1.p + t1n, t2n);
+            diis_step(s, s->X.p, s->Xn.p, s->xoff + t2n);
         }
     } else {
         std::swap(s->T, s->Tn);
-        if (s->method == 1) std::swap(s->t1, s->t1n);
+        if (s->method == 1) {
+            std::swap(s->t1, s->t1n);
+            std::swap(s->X, s->Xn);
+        }
     }
     double rn = std::sqrt(r2);
     s->e_prev = s->energy;
@@ -567,13 +658,21 @@ namespace jues {
 
 // ---------------------------------------------------------------------------------------
 // CCSD sweep (RCCSD.jl:150-289 on the six blocks of mRCCSD.jl:102-110).
-// Work buffers: Tt = t~(T2 + tau/2) for Fae/Fmi, then t~(T2); aux1 = T2 + tau; tau; aux2 = the
-// o^3 v intermediates.  Wabef is never formed: its vvvv part is the particle ladder on the
-// resident (cached) vvvv, its t1 parts go through Y[ij,a,m] = sum_ef Ttau[ij,ef] <am|ef>
-// (2 o^3 v^3 instead of forming and re-reading a v^4 array every sweep):
-//   sum_ef Ttau[ij,ef] (-t1[m,b] <am|ef> - t1[m,a] <mb|ef>) = -sum_m t1[m,b] Y[ij,a,m] - (image),
-// the second term being the (i,a) <-> (j,b) image of the first (<mb|ef> = <bm|fe> and
-// Ttau[ij,ef] = Ttau[ji,fe]), so only the first goes into Z.
+// Work buffers: aux1 = Ttau = T2 + tau, U = T2 + 2 tau (tau = t1 (x) t1, never stored); aux2 =
+// the o^3 v intermediates.  Rewrites, exact given the pair symmetry T2[i,j,a,b] = T2[j,i,b,a]:
+//   * Wabef is never formed: its vvvv part is the particle ladder on the resident (cached)
+//     vvvv, its t1 parts go through Y[ij,a,m] = sum_ef Ttau[ij,ef] <am|ef>:
+//       sum_ef Ttau[ij,ef] (-t1[m,b] <am|ef> - t1[m,a] <mb|ef>) = -sum_m t1[m,b] Y[ij,a,m] - (image),
+//     the image being added by the finalisation (Z[i,j,a,b] + Z[j,i,b,a]);
+//   * the T2 parts of WmBeJ / WmBEj are three GEMMs: 1/2 oovvT[m,n,e,f] T2[j,n,b,f] and
+//     -1/2 oovv[m,n,e,f] U[n,j,b,f] into WJ, 1/2 oovv[n,m,e,f] U[n,j,b,f] into WK, with T2 and
+//     U in the layouts the ring GEMMs read them in;
+//   * Fmi's T2 part is the trace of X = oovv . Ttau^T (the hole-hole intermediate), Fae's T2
+//     and t1 parts are traces of WJ and WK (ccsd_fae_kernel), T1's <ma|fe> terms traces of Y;
+//   * the F~ae term rides in the first ring GEMM (W12[(j,e),(b,j)] += F~ae[b,e]) and the F~mi
+//     terms in the hole-hole ladder (W'[(m,n),(i,j)] -= [m = i] F~mi[n,j] + [n = j] F~mi[m,i]),
+//     whose Ttau in place of T2 the finalisation undoes with the rank-one t1[i,a] q[b,j],
+//     q[b,j] = sum_m t1[m,b] F~mi[m,j], and its image.
 // Every contraction runs in the sweep's precision; the split engine keeps the ones with a
 // dimension below 16 in FP64 by itself.
 // ---------------------------------------------------------------------------------------
@@ -584,134 +683,129 @@ double ccsd_sweep(CCState *s, int prec) {
     const size_t t2n = (size_t)(oo * vv);
     const double *T = s->T.p, *t1 = s->t1.p, *W = s->oovv.p, *ooov = s->ooov.p, *ovvv = s->ovvv.p,
                  *ovov = s->ovov.p;
-    if (s->tau.n < t2n) s->tau = DBuf<double>(ctx, t2n);
     if (s->aux1.n < t2n) s->aux1 = DBuf<double>(ctx, t2n);
     if (s->aux2.n < (size_t)(ooo * v)) s->aux2 = DBuf<double>(ctx, (size_t)(ooo * v));
-    double *tau = s->tau.p, *Ttau = s->aux1.p;
-    // T2 + tau is rewritten below and then only read in this sweep: its packs are shared between
-    // the GEMMs that read it in the same layout (the particle ladder, X and Y)
-    pack_cache_drop(ctx, Ttau);
-    // tau[m,n,a,f] = t1[m,a] t1[n,f]: outer product as a K=1 GEMM over (m,a) x (n,f)
-    G(s, JUES_PREC_FP64, "ccsd_tau", ov, ov, 1, 1.0, t1, plain(1), plain(0), t1, plain(0), plain(1), 0.0,
-      tau, mode2(o, 1, oo), mode2(o, o, oov));
-    axpby(ctx, t2n, 1.0, T, 0.5, tau, Ttau);                 // T2 + tau/2
-    t_tilde(ctx, Ttau, (int)o, (int)v, s->Tt.p);             // 2Ts - Ts[n,m,..]
-    axpby(ctx, t2n, 1.0, T, 1.0, tau, Ttau);                 // T2 + tau (ladders)
+    double *Ttau = s->aux1.p, *U = s->U.p;
+    double *tGJ = s->fwork.p, *tGK = tGJ + vv, *H1 = tGK + vv, *G2 = H1 + vv, *q = G2 + vv;
+    // T2, Ttau and U are read-only in this sweep: their packs are shared between the GEMMs that
+    // read them in the same layout (the ladders, X and Y; WJ, WK and the rings)
+    for (const double *p : {(const double *)s->T.p, (const double *)s->Tn.p, (const double *)Ttau, (const double *)U})
+        pack_cache_drop(ctx, p);
+    ccsd_tau(ctx, T, t1, (int)o, (int)v, Ttau, U);
 
-    // Fae (RCCSD.jl:187-194)
-    G(s, prec, "ccsd_fae", v, v, oov, -1.0, s->Tt.p, plain(oo), mode2(oo, 1, oov), W, mode2(oo, 1, oov),
-      plain(oo), 0.0, s->Fae.p, plain(1), plain(v), nullptr, false, true);
-    G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, 2.0, ovvv, mode2(v, o, ovv), mode2(o, 1, ov), t1,
-      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0), nullptr, true, false);
-    // the exchange part: t1[m,f] <ma|ef> = ovvv[m,a,e,f] (RCCSD.jl:190), or t1[m,f] <me|af> =
-    // ovvv[m,e,a,f] (mRCCSD.jl:140)
-    const Mode fae_rows = s->opts.ccsd_fae == JUES_CCSD_FAE_MRCCSD ? mode2(v, ov, o) : mode2(v, o, ov);
-    G(s, JUES_PREC_FP64, "ccsd_fae_t1", vv, 1, ov, -1.0, ovvv, fae_rows, mode2(o, 1, ovv), t1,
-      plain(1), plain(0), 1.0, s->Fae.p, plain(1), plain(0), nullptr, true, false);
-    // Fmi (RCCSD.jl:195-203)
-    G(s, prec, "ccsd_fmi", o, o, o * vv, 1.0, W, plain(1), plain(o), s->Tt.p, plain(o), plain(1), 0.0,
-      s->Fmi.p, plain(1), plain(o), nullptr, true, false);
+    // Fme = sum_nf oovvT[m,n,e,f] t1[n,f] (RCCSD.jl:204-210)
+    G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, 1.0, s->oovvT.p, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
+      plain(0), 0.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
+    // W' = oooo + X, X = sum_ef oovv[mn,ef] Ttau[ij,ef] (Wmnij and Wabef's T2 + tau parts)
+    G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
+      plain(1), plain(oo), s->oooo.p, true, true);
+    // Fmi (RCCSD.jl:195-203): sum_nef oovv[m,n,e,f] (2 Ts[i,n,e,f] - Ts[n,i,e,f]), Ts = T2 + tau/2,
+    // = the trace of X less 1/2 Fme[m,e] t1[i,e]; then the ooov t1 terms
+    fmi_from_x(ctx, s->Wp.p, s->oooo.p, (int)o, s->Fmi.p);
+    G(s, JUES_PREC_FP64, "ccsd_fmi", o, o, v, -0.5, s->Fme.p, plain(1), plain(o), t1, plain(o), plain(1), 1.0,
+      s->Fmi.p, plain(1), plain(o));
     G(s, prec, "ccsd_fmi_t1", oo, 1, ov, 2.0, ooov, mode2(o, 1, oo), mode2(o, o, ooo), t1,
       plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0), nullptr, true, false);
     G(s, prec, "ccsd_fmi_t1", oo, 1, ov, -1.0, ooov, mode2(o, o, oo), mode2(o, 1, ooo), t1,
       plain(1), plain(0), 1.0, s->Fmi.p, plain(1), plain(0), nullptr, true, false);
-    // Fme (RCCSD.jl:204-210)
-    G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
-      plain(0), 0.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
-    G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, -1.0, W, mode2(o, o, oo), mode2(o, 1, oov), t1, plain(1),
-      plain(0), 1.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
+    // W' += t1[j,e] ooov[m,n,i,e] + t1[i,e] ooov[n,m,j,e]
+    G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
+      plain(1), 1.0, s->Wp.p, plain(1), plain(ooo), nullptr, true, false);
+    G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
+      plain(1), 1.0, s->Wp.p, mode3(o, o, o, 1, ooo), plain(oo), nullptr, true, false);
     if (s->fock) {
-        // non-canonical Fock terms: Fae += f_ae - 1/2 f_me t1[m,a], Fmi += f_mi + 1/2 t1[i,e] f_me,
-        // Fme += f_me (the diagonals of f_oo and f_vv are zero; they sit in the resolvents)
-        axpby(ctx, (size_t)vv, 1.0, s->fVV.p, 1.0, s->Fae.p, s->Fae.p);
-        G(s, prec, "ccsd_fock", v, v, o, -0.5, t1, plain(o), plain(1), s->fOV.p, plain(1), plain(o),
-          1.0, s->Fae.p, plain(1), plain(v));
+        // non-canonical Fock terms: Fmi += f_mi + 1/2 t1[i,e] f_me, Fme += f_me (Fae's are in
+        // ccsd_fae_kernel; the diagonals of f_oo and f_vv are zero, they sit in the resolvents)
         axpby(ctx, (size_t)oo, 1.0, s->fOO.p, 1.0, s->Fmi.p, s->Fmi.p);
         G(s, prec, "ccsd_fock", o, o, v, 0.5, s->fOV.p, plain(1), plain(o), t1, plain(o), plain(1),
           1.0, s->Fmi.p, plain(1), plain(o));
         axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, s->Fme.p, s->Fme.p);
     }
-
-    // W' = oooo + t1[j,e] ooov[m,n,i,e] + t1[i,e] ooov[n,m,j,e] + sum_ef oovv[mn,ef] (T2+tau)[ij,ef]
-    G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
-      plain(1), 1.0, s->Wp.p, plain(1), plain(ooo), s->oooo.p, true, false);
-    G(s, prec, "ccsd_wmnij_t1", ooo, o, v, 1.0, ooov, plain(1), plain(ooo), t1, plain(o),
-      plain(1), 1.0, s->Wp.p, mode3(o, o, o, 1, ooo), plain(oo), nullptr, true, false);
-    G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
-      plain(1), plain(oo), nullptr, true, true);
-    // L = oovv + W'^T (T2+tau) + (T2+tau) vvvv^T  (Wabef's t1 parts go through Y below)
+    // F~mi[m,j] = Fmi + 1/2 Fme[m,e] t1[j,e], into the hole-hole ladder
+    d2d(ctx, s->Fmt.p, s->Fmi.p, (size_t)oo);
+    G(s, JUES_PREC_FP64, "ccsd_ftilde", o, o, v, 0.5, s->Fme.p, plain(1), plain(o), t1, plain(o), plain(1), 1.0,
+      s->Fmt.p, plain(1), plain(o));
+    wp_fmi(ctx, s->Wp.p, s->Fmt.p, (int)o);
+    // L = oovv + W'^T Ttau + Ttau vvvv^T  (Wabef's t1 parts go through Y below)
     G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
-      1.0, s->L.p, plain(1), plain(oo), W);
+      1.0, s->L.p, plain(1), plain(oo), W, false, true);
     G(s, prec, "ccsd_pp_ladder", oo, vv, vv, 1.0, Ttau, plain(1), plain(oo), s->vvvv.p, plain(vv),
       plain(1), 1.0, s->L.p, plain(1), plain(oo), nullptr, true, true);
 
-    // ring intermediates; T~ of T2 alone from here on
-    t_tilde(ctx, T, (int)o, (int)v, s->Tt.p);
-    const double *Tt = s->Tt.p;
-    // WJ = WmBeJ (RCCSD.jl:229-238 with <mb|ej> = oovv[m,j,e,b], <mn|ej> = ooov[n,m,j,e])
-    G(s, prec, "ccsd_wj", ov, ov, ov, 0.5, W, mode2(o, 1, oo), mode2(o, o, oov), Tt, mode2(o, 1, oo),
-      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), s->ovvoJ.p, true, false);
-    G(s, prec, "ccsd_wj", ov, ov, ov, -0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, 1, oo),
-      mode2(v, oov, o), 1.0, s->WJ.p, plain(1), plain(ov), nullptr, true, false);
-    G(s, prec, "ccsd_wj", ov, ov, ov, -1.0, W, mode2(o, 1, oo), mode2(o, o, oov), tau, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WJ.p, plain(1), plain(ov), nullptr, true, false);
+    // ring intermediates (RCCSD.jl:229-247), layout [(m,e),(b,j)], columns taken in (j,b) order
+    const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;   // two planes
+    const Mode jb = mode2(o, ov * v, ov);
+    if (stacked) {
+        ring_stacks_begin(s, U);
+    } else {
+        d2d(ctx, s->WJ.p, s->ovvoJ.p, (size_t)(ov * ov));
+        d2d(ctx, s->WK.p, s->ovovK.p, (size_t)(ov * ov));
+        G(s, prec, "ccsd_wj", ov, ov, ov, 0.5, s->oovvT.p, mode2(o, 1, oo), mode2(o, o, oov), T, mode2(o, o, oov),
+          mode2(o, 1, oo), 1.0, s->WJ.p, plain(1), jb, nullptr, true, true);
+        G(s, prec, "ccsd_wj", ov, ov, ov, -0.5, W, mode2(o, 1, oo), mode2(o, o, oov), U, mode2(o, 1, oov),
+          mode2(o, o, oo), 1.0, s->WJ.p, plain(1), jb, nullptr, true, true);
+        G(s, prec, "ccsd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), U, mode2(o, 1, oov),
+          mode2(o, o, oo), 1.0, s->WK.p, plain(1), jb, nullptr, true, true);
+    }
+    ring_traces(ctx, s->WJ.p, s->ovvoJ.p, s->WK.p, s->ovovK.p, (int)o, (int)v, tGJ, tGK);
+    // the t1 terms: WJ += t1[j,f] <mb|ef> - t1[n,b] <mn|ej>, WK += -t1[j,f] <mb|fe> + t1[n,b] <nm|ej>
     G(s, prec, "ccsd_wj_t1", ovv, o, v, 1.0, ovvv, mode3(o, v, 1, ov, o), plain(ovv), t1,
       plain(o), plain(1), 1.0, s->WJ.p, mode3(o, v, 1, o, ov), plain(ovv), nullptr, true, false);
     G(s, prec, "ccsd_wj_t1", ov * o, v, o, -1.0, ooov, mode3(o, v, o, ooo, oo), plain(1), t1,
       plain(1), plain(o), 1.0, s->WJ.p, mode3(o, v, 1, o, ovv), plain(ov), nullptr, true, false);
-    // WK = WmBEj (RCCSD.jl:239-247 with <bm|ej> = ovov[m,b,j,e], <nm|ej> = ooov[m,n,j,e])
-    G(s, prec, "ccsd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), T, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), s->ovovK.p, true, false);
-    G(s, prec, "ccsd_wk", ov, ov, ov, 1.0, W, mode2(o, o, oo), mode2(o, 1, oov), tau, mode2(o, o, oo),
-      mode2(v, oov, 1), 1.0, s->WK.p, plain(1), plain(ov), nullptr, true, false);
     G(s, prec, "ccsd_wk_t1", ovv, o, v, -1.0, ovvv, mode3(o, v, 1, ovv, o), plain(ov), t1,
       plain(o), plain(1), 1.0, s->WK.p, mode3(o, v, 1, o, ov), plain(ovv), nullptr, true, false);
     G(s, prec, "ccsd_wk_t1", ov * o, v, o, 1.0, ooov, mode3(o, v, 1, ooo, oo), plain(o), t1,
       plain(1), plain(o), 1.0, s->WK.p, mode3(o, v, 1, o, ovv), plain(ov), nullptr, true, false);
     axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
+    // Fae (the exchange t1 term as RCCSD.jl:190 or mRCCSD.jl:140), H1, G2; W12 += [m = j] F~ae
+    ccsd_fae(ctx, s->WJ.p, s->ovvoJ.p, s->WK.p, s->ovovK.p, tGJ, tGK, t1, s->c12.p, s->Fme.p,
+             s->fock ? s->fOV.p : nullptr, s->fock ? s->fVV.p : nullptr, (int)o, (int)v,
+             s->opts.ccsd_fae == JUES_CCSD_FAE_MRCCSD, s->Fae.p, H1, G2, s->W12.p);
 
-    // T1 (RCCSD.jl:248-259) into t1n, before the amplitudes change
+    // Y[ij,(a,m)] = sum_ef Ttau[i,j,e,f] <am|ef> (<am|ef> = ovvv[m,a,f,e])
+    double *Y = s->aux2.p;
+    G(s, prec, "ccsd_y", oo, ov, vv, 1.0, Ttau, plain(1), plain(oo), ovvv, mode2(v, ovv, ov), mode2(v, o, 1),
+      0.0, Y, plain(1), plain(oo), nullptr, true, true);
+
+    // T1 (RCCSD.jl:248-259) into t1n
     double *R1 = s->t1n.p;
     G(s, prec, "ccsd_t1", o, v, v, 1.0, t1, plain(1), plain(o), s->Fae.p, plain(v), plain(1),
       0.0, R1, plain(1), plain(o));
     G(s, prec, "ccsd_t1", o, v, o, -1.0, s->Fmi.p, plain(o), plain(1), t1, plain(1), plain(o),
       1.0, R1, plain(1), plain(o));
-    G(s, prec, "ccsd_t1", ov, 1, ov, 1.0, Tt, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
+    // Fme[m,e] (2 T2[i,m,a,e] - T2[m,i,a,e])
+    G(s, prec, "ccsd_t1", ov, 1, ov, 2.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
+      plain(1), plain(0), 1.0, R1, plain(1), plain(0));
+    G(s, prec, "ccsd_t1", ov, 1, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->Fme.p,
       plain(1), plain(0), 1.0, R1, plain(1), plain(0));
     G(s, prec, "ccsd_t1", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
       plain(0), 1.0, R1, plain(1), plain(0), nullptr, true, false);
     G(s, prec, "ccsd_t1", ov, 1, ov, -1.0, ovov, mode2(o, ov, o), mode2(o, 1, oov), t1,
       plain(1), plain(0), 1.0, R1, plain(1), plain(0), nullptr, true, false);
-    G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, ooov, plain(oo), mode2(oo, 1, ooo), Tt,
+    // - sum_mne T2[m,n,a,e] (2 <mn|ie> - <nm|ie>)
+    G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, s->ooovT.p, plain(oo), mode2(oo, 1, ooo), T,
       mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o), nullptr, true, false);
-    G(s, prec, "ccsd_t1_ovvv", o, v, ovv, 1.0, Tt, plain(1), mode3(o, v, o, oo, oov), ovvv,
-      mode3(o, v, 1, ovv, ov), plain(o), 1.0, R1, plain(1), plain(o), nullptr, false, true);
-
-    // F~ae[b,e] = Fae - 1/2 t1[m,b] Fme[m,e];  F~mi[m,j] = Fmi + 1/2 Fme[m,e] t1[j,e]
-    G(s, prec, "ccsd_ftilde", v, v, o, -0.5, t1, plain(o), plain(1), s->Fme.p, plain(1),
-      plain(o), 1.0, s->Fae.p, plain(1), plain(v));
-    G(s, prec, "ccsd_ftilde", o, o, v, 0.5, s->Fme.p, plain(1), plain(o), t1, plain(o),
-      plain(1), 1.0, s->Fmi.p, plain(1), plain(o));
+    // the <ma|fe> terms from Y
+    t1_ytrace(ctx, Y, t1, G2, H1, (int)o, (int)v, R1);
 
     // Z (RCCSD.jl:264-284, one member of each (i,a)<->(j,b) pair)
     double *Z = s->Z.p;
-    G(s, prec, "ccsd_z_fae", oov, v, v, 1.0, T, plain(1), plain(oov), s->Fae.p, plain(v), plain(1), 0.0,
-      Z, plain(1), plain(oov));
-    // Wabef's t1 parts: Y[ij,(a,m)] = sum_ef Ttau[i,j,e,f] <am|ef> (<am|ef> = ovvv[m,a,f,e]), then
-    // Z[i,j,a,b] -= sum_m Y[ij,a,m] t1[m,b]
-    double *Y = s->aux2.p;
-    G(s, prec, "ccsd_y", oo, ov, vv, 1.0, Ttau, plain(1), plain(oo), ovvv, mode2(v, ovv, ov), mode2(v, o, 1),
-      0.0, Y, plain(1), plain(oo), nullptr, true, true);
+    // + T2[i,m,a,e] (2 WmBeJ + WmBEj + [m = j] F~ae)[m,b,e,j] - T2[m,i,a,e] WmBeJ[m,b,e,j]
+    // + T2[m,i,b,e] WmBEj[m,a,e,j]
+    if (stacked) {
+        ring_stacks_z(s);
+    } else {
+        G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
+          plain(ov), 0.0, Z, mode2(o, 1, oo), mode2(v, oov, o), nullptr, true, false);
+        G(s, prec, "ccsd_ring", ov, ov, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WJ.p, plain(1),
+          plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o), nullptr, true, false);
+        G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
+          plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o), nullptr, true, false);
+    }
+    // Wabef's t1 parts: Z[i,j,a,b] -= sum_m Y[ij,a,m] t1[m,b]
     G(s, prec, "ccsd_y_t1", oov, v, o, -1.0, Y, plain(1), plain(oov), t1, plain(1), plain(o), 1.0, Z,
       plain(1), plain(oov));
-    G(s, prec, "ccsd_z_fmi", o * vv, o, o, -1.0, T, mode2(o, 1, oo), plain(o), s->Fmi.p, plain(1),
-      plain(o), 1.0, Z, mode2(o, 1, oo), plain(o));
-    G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
-      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
-    G(s, prec, "ccsd_ring", ov, ov, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WJ.p, plain(1),
-      plain(ov), 1.0, Z, mode2(o, 1, oo), mode2(v, oov, o));
-    G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
-      plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o));
     // - tau[i,m,e,a] <mb|ej>: Y1[i,m,j,b] = sum_e t1[i,e] oovv[m,j,e,b]; Z -= sum_m t1[m,a] Y1[i,m,j,b]
     G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo),
       mode3(o, o, 1, o, oov), 0.0, Y, plain(1), plain(o), nullptr, false, true);
@@ -730,7 +824,10 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo), nullptr, true, false);
 
     if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia
-    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p);
+    // q[b,j] = sum_m t1[m,b] F~mi[m,j]: the hole-hole ladder's tau[i,m,a,b] F~mi[m,j] terms, undone
+    G(s, JUES_PREC_FP64, "ccsd_q", v, o, o, 1.0, t1, plain(o), plain(1), s->Fmt.p, plain(1), plain(o), 0.0, q,
+      plain(1), plain(v));
+    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p, t1, q);
     // t1n = R1 / D_ia and its step norm
     const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, t1);
     s->r1sq = r1;

@@ -15,12 +15,24 @@ struct CCState {
     // integrals, physicists' notation, column-major as the reference's get_eri blocks
     DBuf<double> eps, oovv, ovov, ovvo, oooo, vvvv, ooov, ovvv;
     DBuf<double> invD;           // 1 / D[i,j,a,b], formed once
-    DBuf<double> oovvT;          // CCD energy weights 2 oovv[i,j,a,b] - oovv[j,i,a,b], formed once
+    DBuf<double> oovvT;          // 2 oovv[i,j,a,b] - oovv[j,i,a,b], formed once (CCD energy weights,
+                                 // ring and Fme weights)
+    DBuf<double> ooovT, c12;     // CCSD: 2 ooov[m,n,i,e] - ooov[n,m,i,e]; the ooov diagonal sums c1, c2
     DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;
-    DBuf<double> t1, t1n, Fme, tau;         // CCSD
+    DBuf<double> t1, t1n, Fme, U, Fmt;      // CCSD: U = T2 + 2 tau, Fmt = F~mi
+    // CCSD: the amplitudes [t1 | pad | T2] and the sweep's output in one buffer each (the DIIS
+    // vectors); t1, T and t1n, Tn are views into them, T2 starting at element xoff (even)
+    DBuf<double> X, Xn;
+    size_t xoff = 0;
+    DBuf<double> fwork;                     // CCSD: ring traces tGJ, tGK, H1, G2 (v x v each), q (v x o)
     DBuf<double> aux1, aux2;                // CCSD scratch
+    // split precision: K-stacked packs of the ring contractions.  stackW (constant, built once):
+    // the WmBeJ / WmBEj weights [a | b | 1/2 oovv[n,m,e,f]] with (a, b) = (-1/2 oovv, 1/2 oovvT)
+    // (CCD) or (1/2 oovvT, -1/2 oovv) (CCSD); stackT: T2[m,i,a,e] | T2[i,m,a,e] (| U[m,i,a,e],
+    // CCSD); stackR: -WJ | W12; stackK: WK
+    StackedPack stackW, stackT, stackR, stackK;
     // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
     std::vector<DBuf<double>> dv, de;
     std::vector<std::vector<double>> gram;   // gram[k][l] = e_k . e_l, k,l in insertion order
@@ -29,8 +41,8 @@ struct CCState {
     std::vector<int> dorder;   // slots in insertion order
     double energy = 0.0, e_prev = 0.0;
     int iters = 0;
-    int refine_left = -1;
-    bool cache_operands = false;   // keep split packs of sweep operands (CCD only)   // split precision: closing FP64 sweeps left (-1 = not started)
+    int refine_left = -1;          // split precision: closing FP64 sweeps left (-1 = not started)
+    bool cache_operands = false;   // keep split packs of every sweep operand (CCD)
     bool converged = false;
     bool reference_df_wmbej = false;   // DF-RCCD.jl's index order in WmBeJ's last term
     // general (non-canonical) Fock matrix, AutoRCCSD.jl: off-diagonal occupied and virtual

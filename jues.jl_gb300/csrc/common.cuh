@@ -213,6 +213,30 @@ void splitk_reduce(Ctx *ctx, const double *ws, int ks, long long sstride, long l
                    double alpha, double beta, double *C, const double *Cin, const Mode &mC, const Mode &nC,
                    const char *name);
 void gett(Ctx *ctx, int precision, const GettArgs &g, const char *name);
+// K-stacked split-precision operands (gett_tc.cu).  A StackedPack holds np planes of rows_pad x
+// pitch FP16 digits and their [chunk][row] scales; pack_stacked writes one operand (R x K over the
+// modes, times a power-of-two scale) into K columns [k0, k0 + roundup(K, 128)), and a view of
+// adjacent blocks is one operand of gett_tc_views, which runs C = alpha A.B^T + beta Cin over the
+// stacked K.  So sum_s A_s B_s^T is one GEMM.
+struct PackedView {
+    const uint16_t *planes = nullptr;
+    const int *exps = nullptr;
+    long long rows_pad = 0, kpad = 0, pitch = 0;
+    int np = 2;
+};
+struct StackedPack {
+    DBuf<uint16_t> buf;
+    DBuf<int> exps;
+    long long rows_pad = 0, pitch = 0;
+    int np = 2;
+    void ensure(Ctx *ctx, long long rows, long long kcols, int planes);
+    PackedView view(long long k0, long long kcols) const;
+};
+void pack_stacked(Ctx *ctx, StackedPack &sp, long long k0, const double *src, const Mode &rm, const Mode &km,
+                  long long R, long long K, double scale);
+void gett_tc_views(Ctx *ctx, const PackedView &A, const PackedView &B, long long M, long long N, double alpha,
+                   double beta, double *C, const Mode &mC, const Mode &nC, const double *Cin, const char *name);
+
 // Grouped three-plane split GEMM of many independent problems with K <= 64 (the batched form):
 // build once (null when some problem has K > 64), then run (capturable in a CUDA graph)
 struct TcGroup;
@@ -254,10 +278,11 @@ double mp2_energy(Ctx *ctx, const double *K, const double *eps, int o, int v);
 double mp2_gamma(Ctx *ctx, const double *K, const double *eps, int o, int v, double e_bar, double *G);
 // CC energy: sum oovv[i,j,a,b] (2 X[i,j,a,b] - X[j,i,a,b]) with X = T2 (+ t1 t1 when t1)
 double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t1, int o, int v);
-// T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a]) invD ; returns ||Tn - Told||^2
-// if Told != nullptr.  Writes Tn.
+// T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a] + C[i,j,a,b] + C[j,i,b,a]) invD
+// with C[i,j,a,b] = t1[i,a] q[b,j] when t1 and q (v x o) are given; returns ||Tn - Told||^2 if
+// Told != nullptr.  Writes Tn.
 double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
-                   const double *Told, double *Tn);
+                   const double *Told, double *Tn, const double *t1 = nullptr, const double *q = nullptr);
 // invD[i,j,a,b] = 1 / (e_i + e_j - e_a - e_b)
 void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out);
 // t1n[i,a] /= (e_i - e_a) in place; returns ||t1n - t1old||^2
@@ -270,6 +295,26 @@ void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out);
 void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out);
 // W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i] (o^4 W', o x o Fmi, column-major)
 void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o);
+// Fmi[m,i] = sum_n 2 X[m,n,i,n] - X[m,n,n,i], X = Wp - oooo (o^4 arrays [(m,n),(i,j)])
+void fmi_from_x(Ctx *ctx, const double *Wp, const double *oooo, int o, double *Fmi);
+// Fae[a,e] = -(cJ tr(WJ - J0) + cK tr(WK - K0))[a,e], traces over m of [(m,e),(a,m)]; when W12 is
+// given, W12[(j,e),(a,j)] += Fae[a,e] for every j
+void fae_from_rings(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
+                    double cJ, double cK, double *Fae, double *W12);
+// CCSD: Ttau = T2 + t1 (x) t1 and U = T2 + 2 t1 (x) t1
+void ccsd_tau(Ctx *ctx, const double *T, const double *t1, int o, int v, double *Ttau, double *U);
+// traces over m of (WJ - J0) and (WK - K0) at [(m,e),(a,m)] into tJ[a,e], tK[a,e]
+void ring_traces(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
+                 double *tJ, double *tK);
+// CCSD Fae, H1, G2 from the ring traces, and F~ae onto W12's (m = j) entries (kernels.cu)
+void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, const double *tGJ,
+              const double *tGK, const double *t1, const double *c12, const double *Fme, const double *fOV,
+              const double *fVV, int o, int v, bool mvariant, double *Fae, double *H1, double *G2, double *W12);
+// R1 += T1's <ma|fe> terms from the traces of Y[(i,j),(a,m)]
+void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, int o, int v,
+               double *R1);
+// c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e] into c12[0..ov), c12[ov..2ov)
+void ooov_diag_sums(Ctx *ctx, const double *ooov, int o, int v, double *c12);
 // DIIS bookkeeping in one pass: v_out = xn, e_out = xn - x, dots[0] = e.e, dots[1 + k] = olds[k].e
 void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
                 const double *const *olds, double *dots);

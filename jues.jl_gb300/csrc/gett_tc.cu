@@ -798,7 +798,7 @@ template <int NP, bool KFAST>
 __device__ __forceinline__ void pack_block(const double *__restrict__ src, const Mode &rmode, const Mode &kmode,
                                            long long R, long long K, long long Kpad, long long r0, long long k0,
                                            int *__restrict__ rexp, long long rexp_ld, __half *__restrict__ dst,
-                                           long long pstride, long long Kld) {
+                                           long long pstride, long long Kld, double scale = 1.0) {
     __shared__ __align__(16) uint32_t outp[NP][PR][PACK_PITCH];
     __shared__ long long roff[PR], koff[PK];
     __shared__ int rowE[PR];
@@ -823,6 +823,10 @@ __device__ __forceinline__ void pack_block(const double *__restrict__ src, const
             const long long a = roff[row_of(i)], b = koff[2 * pair_of(i) + h];
             x[i][h] = (a >= 0 && b >= 0) ? __ldg(src + a + b) : 0.0;
         }
+    if (scale != 1.0) {   // a power of two: exact
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { x[i][0] *= scale; x[i][1] *= scale; }
+    }
     // row maxima of the exponent field
     if constexpr (KFAST) {
         // a warp's lanes share each of its four rows
@@ -872,14 +876,15 @@ template <int NP, bool KFAST>
 __global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__restrict__ src, Mode rmode, Mode kmode,
                                                          long long R, long long K, long long Rpad,
                                                          long long Kpad, int *__restrict__ rexp,
-                                                         __half *__restrict__ dst) {
+                                                         __half *__restrict__ dst, long long Kld,
+                                                         long long pstride, double scale) {
     // consecutive blocks follow the source's unit-stride index, so the blocks resident at one
     // time read long contiguous runs of it
     // block counts < 2^31 (checked at launch): 32-bit index arithmetic
     const unsigned kblocks = (unsigned)((Kpad + PK - 1) / PK), rblocks = (unsigned)(Rpad / PR);
     const long long r0 = (long long)(KFAST ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
     const long long k0 = (long long)(KFAST ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
-    pack_block<NP, KFAST>(src, rmode, kmode, R, K, Kpad, r0, k0, rexp, Rpad, dst, Rpad * Kpad, Kpad);
+    pack_block<NP, KFAST>(src, rmode, kmode, R, K, Kpad, r0, k0, rexp, Rpad, dst, pstride, Kld, scale);
 }
 
 // Grouped form: many operands (one per problem of a batch) with one 64-wide K block each
@@ -911,15 +916,23 @@ __global__ void __launch_bounds__(256, 6) pack_grouped_kernel(const PackProb *__
                               rows_total * 64, 64);
 }
 
+// Pack rows [0, Rpad) x K [0, Kpad) of one operand into planes of row pitch Kld (plane stride
+// pstride) and the [chunk][row] scales ex (chunk stride Rpad), each value times scale (a power of
+// two); the plain packs have Kld = Kpad and pstride = Rpad Kpad.
 template <int NP>
 void launch_pack(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
-                 long long Rpad, long long Kpad, int *ex, __half *dst) {
+                 long long Rpad, long long Kpad, int *ex, __half *dst, long long Kld = -1, long long pstride = -1,
+                 double scale = 1.0) {
+    if (Kld < 0) Kld = Kpad;
+    if (pstride < 0) pstride = Rpad * Kpad;
     const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     if (km.s0 == 1 && km.d0 > 1)
-        pack_split_kernel<NP, true><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex, dst);
+        pack_split_kernel<NP, true><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex, dst,
+                                                                               Kld, pstride, scale);
     else
-        pack_split_kernel<NP, false><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex, dst);
+        pack_split_kernel<NP, false><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex,
+                                                                                dst, Kld, pstride, scale);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -937,11 +950,14 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     return fn;
 }
 
-CUtensorMap make_map(const __half *base, long long rows_pad, long long kpad, int box_rows, int np) {
+// planes [np][rows_pad][pitch] of FP16 digits, K columns [0, kpad) read (pitch >= kpad)
+CUtensorMap make_map(const __half *base, long long rows_pad, long long kpad, int box_rows, int np,
+                     long long pitch = -1) {
+    if (pitch < 0) pitch = kpad;
     CUtensorMap m;
     std::memset(&m, 0, sizeof(m));
     cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)np};
-    cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
+    cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)rows_pad * pitch * 2};
     cuuint32_t box[3] = {(cuuint32_t)TBK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half *>(base), dims,
@@ -1488,6 +1504,104 @@ __global__ void __launch_bounds__(256) scale_output_kernel(double *C, Mode mC, M
         double *p = C + mode_off(mC, m) + mode_off(nC, n);
         *p = beta == 0.0 ? 0.0 : beta * *p;
     }
+}
+
+// ---------------------------------------------------------------------------------------
+// K-stacked operands.  Several operands with the same rows packed side by side along K into one
+// buffer (each block starting on a scaling-chunk boundary) form one longer contraction:
+// sum_s A_s . B_s^T is one GEMM over the stacked K, so its output tiles are written once and
+// their per-tile cost is paid once.  A view reads any run of adjacent blocks.
+// ---------------------------------------------------------------------------------------
+void StackedPack::ensure(Ctx *ctx, long long rows, long long kcols, int planes) {
+    JUES_REQUIRE(planes == 2 || planes == 3, "stacked packs hold 2 or 3 planes");
+    JUES_REQUIRE(kcols % KCH == 0, "stacked pack width must be a multiple of 128");
+    rows = roundup(rows, TBM);
+    if (rows == rows_pad && kcols == pitch && planes == np && buf.p) return;
+    buf.reset();
+    exps.reset();
+    rows_pad = rows;
+    pitch = kcols;
+    np = planes;
+    buf = DBuf<uint16_t>(ctx, (size_t)np * rows_pad * pitch);
+    exps = DBuf<int>(ctx, (size_t)(pitch / KCH) * rows_pad);
+}
+
+PackedView StackedPack::view(long long k0, long long kcols) const {
+    JUES_REQUIRE(k0 % KCH == 0 && kcols % KCH == 0 && k0 >= 0 && k0 + kcols <= pitch, "stacked view out of range");
+    PackedView v;
+    v.planes = buf.p + k0;
+    v.exps = exps.p + (k0 / KCH) * rows_pad;
+    v.rows_pad = rows_pad;
+    v.kpad = kcols;
+    v.pitch = pitch;
+    v.np = np;
+    return v;
+}
+
+void pack_stacked(Ctx *ctx, StackedPack &sp, long long k0, const double *src, const Mode &rm, const Mode &km,
+                  long long R, long long K, double scale) {
+    const long long kcols = roundup(K, KCH);
+    JUES_REQUIRE(R <= sp.rows_pad && k0 % KCH == 0 && k0 + kcols <= sp.pitch, "operand does not fit its stacked pack");
+    int ak = 0;
+    JUES_REQUIRE(std::frexp(std::fabs(scale), &ak) == 0.5, "stacked pack scale must be a power of two");
+    __half *dst = reinterpret_cast<__half *>(sp.buf.p) + k0;
+    int *ex = sp.exps.p + (k0 / KCH) * sp.rows_pad;
+    Ctx::Scope s(ctx, "pack_split");
+    if (sp.np == 3)
+        launch_pack<3>(ctx, src, rm, km, R, K, sp.rows_pad, kcols, ex, dst, sp.pitch, sp.rows_pad * sp.pitch, scale);
+    else
+        launch_pack<2>(ctx, src, rm, km, R, K, sp.rows_pad, kcols, ex, dst, sp.pitch, sp.rows_pad * sp.pitch, scale);
+}
+
+void gett_tc_views(Ctx *ctx, const PackedView &A, const PackedView &B, long long M, long long N, double alpha,
+                   double beta, double *C, const Mode &mC, const Mode &nC, const double *Cin, const char *name) {
+    if (M <= 0 || N <= 0) return;
+    JUES_REQUIRE(A.np == B.np && A.kpad == B.kpad, "stacked views differ in planes or K");
+    JUES_REQUIRE(M <= A.rows_pad && N <= B.rows_pad, "stacked view has fewer rows than the GEMM");
+    const int np = A.np;
+    const int BN = (np == 2 && B.rows_pad % 128 == 0) ? 128 : 64;
+    const long long Mpad = A.rows_pad, Npad = roundup(N, BN), Kpad = A.kpad;
+    JUES_REQUIRE(Npad <= B.rows_pad, "stacked B view rows not a multiple of the tile width");
+    const __half *pa = reinterpret_cast<const __half *>(A.planes);
+    const __half *pb = reinterpret_cast<const __half *>(B.planes);
+    const CUtensorMap ma = make_map(pa, A.rows_pad, Kpad, TBM, np, A.pitch);
+    const CUtensorMap mb = make_map(pb, B.rows_pad, Kpad, BN, np, B.pitch);
+    TcArgs t;
+    t.M = M;
+    t.N = N;
+    t.kblocks = (int)(Kpad / TBK);
+    t.mtiles = roundup(M, TBM) / TBM;
+    t.alpha = alpha;
+    t.beta = beta;
+    t.C = C;
+    t.Cin = Cin ? Cin : C;
+    t.mC = mC;
+    t.nC = nC;
+    t.flags = ctx->d_flags;
+    t.expA = A.exps;
+    t.expB = B.exps;
+    t.expA_ld = A.rows_pad;
+    t.expB_ld = B.rows_pad;
+    (void)Mpad;
+    const long long tiles = t.mtiles * (Npad / BN);
+    JUES_REQUIRE(tiles < (1LL << 31), "too many output tiles");
+    const int ks0 = choose_ksplit(tiles, t.kblocks, (long long)TBM * BN);
+    if (ks0 > 1) {
+        t.kper = (t.kblocks + ks0 - 1) / ks0;
+        t.kper = (t.kper + TC_KC - 1) / TC_KC * TC_KC;
+        t.ksplit = (t.kblocks + t.kper - 1) / t.kper;
+        t.partial = static_cast<float *>(
+            ctx->splitk_scratch((size_t)t.ksplit * roundup(M, TBM) * Npad * sizeof(float)));
+    }
+    if (np == 3)
+        launch_tc<64, 3, 3>(ctx, ma, mb, t, tiles, name);
+    else if (BN == 128)
+        launch_tc<128, 3, 2>(ctx, ma, mb, t, tiles, name);
+    else
+        launch_tc<64, 4, 2>(ctx, ma, mb, t, tiles, name);
+    if (t.ksplit > 1)
+        splitk_reduce(ctx, t.partial, t.ksplit, roundup(M, TBM) * Npad, roundup(M, TBM), M, N, alpha, beta, C, t.Cin,
+                      mC, nC, name);
 }
 
 void gett_tc_noalloc(Ctx *ctx, const GettArgs &a) {

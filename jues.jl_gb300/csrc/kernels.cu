@@ -222,11 +222,16 @@ __global__ void inv_denominators_kernel(const double *__restrict__ eps, int o, i
     }
 }
 
-// Tn[i,j,a,b] = (L[i,j,a,b] + Z[i,j,a,b] + Z[j,i,b,a]) / D, and the squared step norm.
+// Tn[i,j,a,b] = (L[i,j,a,b] + Z[i,j,a,b] + Z[j,i,b,a] + C[i,j,a,b] + C[j,i,b,a]) / D with the
+// optional rank-one C[i,j,a,b] = t1[i,a] q[b,j] (t1 o x v, q v x o), and the squared step norm.
+__device__ __forceinline__ double rank1_pair(const double *__restrict__ t1, const double *__restrict__ q, int o,
+                                             int v, int i, int j, int a, int b) {
+    return t1[i + (long long)o * a] * q[b + (long long)v * j] + t1[j + (long long)o * b] * q[a + (long long)v * i];
+}
 __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *__restrict__ Z,
                                    const double *__restrict__ invD, int o, int v,
                                    const double *__restrict__ Told, double *__restrict__ Tn,
-                                   double *part) {
+                                   double *part, const double *__restrict__ t1, const double *__restrict__ q) {
     const long long oo = (long long)o * o;
     const long long npair = (long long)v * (v + 1) / 2;
     double acc = 0.0;
@@ -238,11 +243,15 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
             int i = (int)(ij % o), j = (int)(ij / o);
             long long ji = j + (long long)o * i;
             const double inv = invD[ab + ij];   // D is symmetric in (a, b)
-            double x = (L[ab + ij] + Z[ab + ij] + Z[ba + ji]) * inv;
+            double x = L[ab + ij] + Z[ab + ij] + Z[ba + ji];
+            if (t1) x += rank1_pair(t1, q, o, v, i, j, a, b);
+            x *= inv;
             Tn[ab + ij] = x;
             if (Told) { double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
             if (a != b) {
-                double y = (L[ba + ij] + Z[ba + ij] + Z[ab + ji]) * inv;
+                double y = L[ba + ij] + Z[ba + ij] + Z[ab + ji];
+                if (t1) y += rank1_pair(t1, q, o, v, i, j, b, a);
+                y *= inv;
                 Tn[ba + ij] = y;
                 if (Told) { double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
             }
@@ -261,19 +270,83 @@ __global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__r
                                                                const double *__restrict__ Z,
                                                                const double *__restrict__ invD, int o, int v,
                                                                const double *__restrict__ Told,
-                                                               double *__restrict__ Tn, double *part) {
+                                                               double *__restrict__ Tn, double *part,
+                                                               const double *__restrict__ t1,
+                                                               const double *__restrict__ q) {
     extern __shared__ double zs[];   // [2][o][pitch]: zs[0] = Z_ab, zs[1] = Z_ba, element (i, j) at j + pitch i
     const int pitch = o | 1;
     const long long oo = (long long)o * o;
-    const long long npair = (long long)v * (v + 1) / 2;
     const int ooi = o * o;
     double acc = 0.0;
-    (void)npair;
-    {
-        const long long p = blockIdx.x;   // one (a <= b) pair per block: blocks overlap their phases
-        int a, b;
-        pair_ab(p, a, b);
-        const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
+    int a, b;
+    pair_ab(blockIdx.x, a, b);   // one (a <= b) pair per block: resident blocks overlap their phases
+    const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
+    if ((o & 1) == 0) {
+        // even o: element pairs (i, i+1) of one column j as 16-byte accesses; (i, j) advance by
+        // carries (step 2 blockDim.x, i stays even)
+        const int n2 = ooi / 2, step = 2 * blockDim.x, di = step % o, dj = step / o;
+        const double2 *Z2ab = reinterpret_cast<const double2 *>(Z + ab), *Z2ba = reinterpret_cast<const double2 *>(Z + ba);
+        {
+            int i = (2 * threadIdx.x) % o, j = (2 * threadIdx.x) / o;
+#pragma unroll 2
+            for (int k = threadIdx.x; k < n2; k += blockDim.x) {
+                const double2 za = Z2ab[k], zb = Z2ba[k];
+                zs[j + pitch * i] = za.x;
+                zs[j + pitch * (i + 1)] = za.y;
+                zs[o * pitch + j + pitch * i] = zb.x;
+                zs[o * pitch + j + pitch * (i + 1)] = zb.y;
+                i += di; j += dj;
+                if (i >= o) { i -= o; ++j; }
+            }
+        }
+        __syncthreads();
+        const double2 *L2ab = reinterpret_cast<const double2 *>(L + ab), *L2ba = reinterpret_cast<const double2 *>(L + ba);
+        const double2 *D2 = reinterpret_cast<const double2 *>(invD + ab);
+        double2 *T2ab = reinterpret_cast<double2 *>(Tn + ab), *T2ba = reinterpret_cast<double2 *>(Tn + ba);
+        int i = (2 * threadIdx.x) % o, j = (2 * threadIdx.x) / o;
+#pragma unroll 2
+        for (int k = threadIdx.x; k < n2; k += blockDim.x) {
+            const double2 inv = D2[k];   // D is symmetric in (a, b)
+            const double2 l = L2ab[k];
+            double2 x;
+            x.x = l.x + zs[j + pitch * i] + zs[o * pitch + i + pitch * j];
+            x.y = l.y + zs[j + pitch * (i + 1)] + zs[o * pitch + i + 1 + pitch * j];
+            if (t1) {
+                x.x += rank1_pair(t1, q, o, v, i, j, a, b);
+                x.y += rank1_pair(t1, q, o, v, i + 1, j, a, b);
+            }
+            x.x *= inv.x;
+            x.y *= inv.y;
+            T2ab[k] = x;
+            if (Told) {
+                const double2 t = reinterpret_cast<const double2 *>(Told + ab)[k];
+                const double d0 = x.x - t.x, d1 = x.y - t.y;
+                acc = fma(d0, d0, acc);
+                acc = fma(d1, d1, acc);
+            }
+            if (a != b) {
+                const double2 lb = L2ba[k];
+                double2 y;
+                y.x = lb.x + zs[o * pitch + j + pitch * i] + zs[i + pitch * j];
+                y.y = lb.y + zs[o * pitch + j + pitch * (i + 1)] + zs[i + 1 + pitch * j];
+                if (t1) {
+                    y.x += rank1_pair(t1, q, o, v, i, j, b, a);
+                    y.y += rank1_pair(t1, q, o, v, i + 1, j, b, a);
+                }
+                y.x *= inv.x;
+                y.y *= inv.y;
+                T2ba[k] = y;
+                if (Told) {
+                    const double2 t = reinterpret_cast<const double2 *>(Told + ba)[k];
+                    const double d0 = y.x - t.x, d1 = y.y - t.y;
+                    acc = fma(d0, d0, acc);
+                    acc = fma(d1, d1, acc);
+                }
+            }
+            i += di; j += dj;
+            if (i >= o) { i -= o; ++j; }
+        }
+    } else {
         for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
             const int i = ij % o, j = ij / o;
             zs[j + pitch * i] = Z[ab + ij];
@@ -285,12 +358,16 @@ __global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__r
             // Z_ab[i,j] and Z_ba[j,i]; Z_ba[i,j] and Z_ab[j,i]
             const double zab = zs[j + pitch * i], zba_t = zs[o * pitch + i + pitch * j];
             const double inv = invD[ab + ij];   // D is symmetric in (a, b)
-            const double x = (L[ab + ij] + zab + zba_t) * inv;
+            double x = L[ab + ij] + zab + zba_t;
+            if (t1) x += rank1_pair(t1, q, o, v, i, j, a, b);
+            x *= inv;
             Tn[ab + ij] = x;
             if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
             if (a != b) {
                 const double zba = zs[o * pitch + j + pitch * i], zab_t = zs[i + pitch * j];
-                const double y = (L[ba + ij] + zba + zab_t) * inv;
+                double y = L[ba + ij] + zba + zab_t;
+                if (t1) y += rank1_pair(t1, q, o, v, i, j, b, a);
+                y *= inv;
                 Tn[ba + ij] = y;
                 if (Told) { const double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
             }
@@ -346,11 +423,29 @@ struct VecList {
     double c[16];
 };
 
-__global__ void lincomb_kernel(size_t n, int m, VecList vl, double *__restrict__ out) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        double s = 0.0;
-        for (int k = 0; k < m; ++k) s = fma(vl.c[k], vl.p[k][i], s);
-        out[i] = s;
+// out = sum_k c_k p_k with the vector count a template parameter, so every load of an element is
+// in flight at once; pairs of elements as 16-byte loads and stores (the vectors are 16-byte
+// aligned), the odd last element alone.  The sum runs in k order for every element.
+template <int M>
+__global__ void lincomb_kernel(size_t n, VecList vl, double *__restrict__ out) {
+    const size_t n2 = n / 2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
+        double2 x[M];
+#pragma unroll
+        for (int k = 0; k < M; ++k) x[k] = __ldg(reinterpret_cast<const double2 *>(vl.p[k]) + i);
+        double2 r = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int k = 0; k < M; ++k) {
+            r.x = fma(vl.c[k], x[k].x, r.x);
+            r.y = fma(vl.c[k], x[k].y, r.y);
+        }
+        reinterpret_cast<double2 *>(out)[i] = r;
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        double r = 0.0;
+#pragma unroll
+        for (int k = 0; k < M; ++k) r = fma(vl.c[k], vl.p[k][n - 1], r);
+        out[n - 1] = r;
     }
 }
 
@@ -411,6 +506,199 @@ __global__ void wp_fmi_kernel(double *__restrict__ Wp, const double *__restrict_
         else
             Wp[oo * ij + k + (long long)o * j] -= Fmi[k + (long long)o * i];   // m = k, n = j
     }
+}
+
+// Fmi[m,i] = sum_n 2 X[m,n,i,n] - X[m,n,n,i] with X = W' - oooo, W'[(m,n),(i,j)] = oooo + sum_ef
+// oovv[m,n,e,f] T[i,j,e,f]: the Fmi contraction of RCCD.jl:216 (sum_nef oovv[m,n,e,f] T~[i,n,e,f])
+// read off the hole-hole intermediate instead of a GEMM of its own.  One thread per (m, i).
+__global__ void fmi_from_x_kernel(const double *__restrict__ Wp, const double *__restrict__ oooo, int o,
+                                  double *__restrict__ Fmi) {
+    const long long oo = (long long)o * o;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= oo) return;
+    const int m = t % o, i = t / o;
+    double acc = 0.0;
+    for (int n = 0; n < o; ++n) {
+        const long long mn = m + (long long)o * n;
+        const long long d = mn + oo * (i + (long long)o * n), x = mn + oo * (n + (long long)o * i);
+        acc = fma(2.0, Wp[d] - oooo[d], acc);
+        acc -= Wp[x] - oooo[x];
+    }
+    Fmi[t] = acc;
+}
+
+// Fae from the ring intermediates and the Fae term folded into W12.  With t = WJ - J0 and
+// u = WK - K0 (the GEMM parts of WmBeJ and WmBEj, layout [(m,e),(b,j)]), their traces
+// tJ[a,e] = sum_m t[(m,e),(a,m)] and tK[a,e] = sum_m u[(m,e),(a,m)] give
+// Fae[a,e] = -(cJ tJ + cK tK) by the pair symmetry of T2; then W12[(j,e),(a,j)] += Fae[a,e]
+// for every j, so the ring GEMM T[i,m,a,e] W12[(m,e),(b,j)] also yields T[i,j,a,e] Fae[b,e].
+// One thread per (a, e); the (m = j) entries it reads and the ones it updates are the same.
+__global__ void fae_trace_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
+                                 const double *__restrict__ WK, const double *__restrict__ K0, int o, int v,
+                                 double cJ, double cK, double *__restrict__ Fae, double *__restrict__ W12) {
+    const long long ov = (long long)o * v;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)v * v) return;
+    const int e = (int)(t % v), a = (int)(t / v);
+    const long long base = (long long)o * e + ov * a, step = 1 + ov * v;
+    double tj = 0.0, tk = 0.0;
+#pragma unroll 4
+    for (int m = 0; m < o; ++m) {
+        const long long x = base + step * m;
+        tj += WJ[x] - J0[x];
+        tk += WK[x] - K0[x];
+    }
+    const double f = -(cJ * tj + cK * tk);
+    Fae[a + (long long)v * e] = f;
+    if (W12)
+        for (int j = 0; j < o; ++j) W12[base + step * j] += f;
+}
+
+// CCSD sweep inputs from T2 and t1 in one pass: Ttau = T2 + tau and U = T2 + 2 tau with
+// tau[i,j,a,b] = t1[i,a] t1[j,b].  One (a,b) block of o x o per iteration, the two t1 columns
+// in shared memory (2 o doubles, dynamic).
+__global__ void __launch_bounds__(256) ccsd_tau_kernel(const double *__restrict__ T, const double *__restrict__ t1,
+                                                       int o, int v, double *__restrict__ Ttau,
+                                                       double *__restrict__ U) {
+    extern __shared__ double cab[];
+    double *ca = cab, *cb = cab + o;
+    const long long oo = (long long)o * o, vv = (long long)v * v;
+    const int ooi = o * o;
+    for (long long ab = blockIdx.x; ab < vv; ab += gridDim.x) {
+        const int a = (int)(ab % v), b = (int)(ab / v);
+        __syncthreads();
+        for (int k = threadIdx.x; k < 2 * o; k += blockDim.x)
+            cab[k] = k < o ? t1[k + (long long)o * a] : t1[k - o + (long long)o * b];
+        __syncthreads();
+        const long long base = oo * ab;
+        for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
+            const int i = ij % o, j = ij / o;
+            const double t = T[base + ij], tau = ca[i] * cb[j];
+            Ttau[base + ij] = t + tau;
+            U[base + ij] = fma(2.0, tau, t);
+        }
+    }
+}
+
+// Traces over m of the GEMM parts of the CCSD ring intermediates (layout [(m,e),(b,j)]):
+// tJ[a,e] = sum_m (WJ - J0)[(m,e),(a,m)], tK[a,e] = sum_m (WK - K0)[(m,e),(a,m)].  One thread
+// per (a, e).
+__global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
+                                   const double *__restrict__ WK, const double *__restrict__ K0, int o, int v,
+                                   double *__restrict__ tJ, double *__restrict__ tK) {
+    const long long ov = (long long)o * v;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)v * v) return;
+    const int e = (int)(t % v), a = (int)(t / v);
+    const long long base = (long long)o * e + ov * a, step = 1 + ov * v;
+    double tj = 0.0, tk = 0.0;
+#pragma unroll 4
+    for (int m = 0; m < o; ++m) {
+        const long long x = base + step * m;
+        tj += WJ[x] - J0[x];
+        tk += WK[x] - K0[x];
+    }
+    tJ[a + (long long)v * e] = tj;
+    tK[a + (long long)v * e] = tk;
+}
+
+// CCSD Fae and F~ae from the ring intermediates (RCCSD.jl:187-194, or mRCCSD.jl:137-149's t1
+// term).  With the traces tGJ, tGK of the T2 parts of WmBeJ / WmBEj (taken before their t1
+// terms) and tJ, tK of the complete ones (this kernel, after), and the pair symmetry of T2:
+//   H1[a,e] = sum_mf t1[m,f] <ma|ef> = tJ - tGJ + S1,   G2[a,e] = sum_mf t1[m,f] <ma|fe> = tGK - tK + S2,
+// S1[a,e] = sum_n t1[n,a] c1[n,e], S2[a,e] = sum_n t1[n,a] c2[n,e] (the traces of the ooov t1
+// terms, c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e]), and
+//   Fae = 2 G2 - H1' - (tGJ + 2 tGK) + 1/2 t1^T (Fme - fOV) + fVV - 1/2 t1^T fOV
+// (H1' = H1, or H1^T for mRCCSD.jl:140's <me|af>), F~ae = Fae - 1/2 t1^T Fme.  Writes Fae, H1, G2
+// (the T1 equation's tau corrections) and adds F~ae[a,e] to W12[(j,e),(a,j)] for every j, where
+// the first ring GEMM turns it into the T2[i,j,a,e] F~ae[b,e] term.  One thread per (a, e).
+__global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
+                                const double *__restrict__ WK, const double *__restrict__ K0,
+                                const double *__restrict__ tGJ, const double *__restrict__ tGK,
+                                const double *__restrict__ t1, const double *__restrict__ c12,
+                                const double *__restrict__ Fme, const double *__restrict__ fOV,
+                                const double *__restrict__ fVV, int o, int v, int mvariant,
+                                double *__restrict__ Fae, double *__restrict__ H1, double *__restrict__ G2,
+                                double *__restrict__ W12) {
+    const long long ov = (long long)o * v;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)v * v) return;
+    const int e = (int)(t % v), a = (int)(t / v);
+    const long long step = 1 + ov * v;
+    const long long base = (long long)o * e + ov * a;
+    const double *c1 = c12, *c2 = c12 + ov;
+    double tj = 0.0, tk = 0.0;
+    for (int m = 0; m < o; ++m) {
+        const long long x = base + step * m;
+        tj += WJ[x] - J0[x];
+        tk += WK[x] - K0[x];
+    }
+    double s1 = 0.0, s2 = 0.0, tf = 0.0, tfo = 0.0;
+    for (int n = 0; n < o; ++n) {
+        const double ta = t1[n + (long long)o * a];
+        s1 = fma(ta, c1[n + (long long)o * e], s1);
+        s2 = fma(ta, c2[n + (long long)o * e], s2);
+        tf = fma(ta, Fme[n + (long long)o * e], tf);
+        if (fOV) tfo = fma(ta, fOV[n + (long long)o * e], tfo);
+    }
+    const long long ae = a + (long long)v * e;
+    const double h1 = tj - tGJ[ae] + s1, g2 = tGK[ae] - tk + s2;
+    double h1x = h1;
+    if (mvariant) {
+        // H1[e,a]: the WJ trace at [(m,a),(e,m)] and S1[e,a]
+        const long long base2 = (long long)o * a + ov * e, ea = e + (long long)v * a;
+        double tj2 = 0.0, s12 = 0.0;
+        for (int m = 0; m < o; ++m) tj2 += WJ[base2 + step * m] - J0[base2 + step * m];
+        for (int n = 0; n < o; ++n) s12 = fma(t1[n + (long long)o * e], c1[n + (long long)o * a], s12);
+        h1x = tj2 - tGJ[ea] + s12;
+    }
+    double ft = 2.0 * g2 - h1x - (tGJ[ae] + 2.0 * tGK[ae]) - tfo;   // F~ae
+    if (fVV) ft += fVV[ae];
+    Fae[ae] = fma(0.5, tf, ft);
+    H1[ae] = h1;
+    G2[ae] = g2;
+    for (int j = 0; j < o; ++j) W12[base + step * j] += ft;
+}
+
+// T1's <ma|fe> terms from Y[(i,j),(a,m)] = sum_ef Ttau[i,j,e,f] <ma|fe> (the Wabef t1
+// intermediate, RCCSD.jl:256-257 / mRCCSD.jl:210-211):
+//   R1[i,a] += 2 (sum_m Y[(i,m),(a,m)] - sum_e t1[i,e] G2[a,e]) - (sum_m Y[(m,i),(a,m)] - sum_f t1[i,f] H1[a,f])
+// (the tau parts of Ttau removed through G2 and H1).  One thread per (i, a).
+__global__ void t1_ytrace_kernel(const double *__restrict__ Y, const double *__restrict__ t1,
+                                 const double *__restrict__ G2, const double *__restrict__ H1, int o, int v,
+                                 double *__restrict__ R1) {
+    const long long oo = (long long)o * o;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)o * v) return;
+    const int i = (int)(t % o), a = (int)(t / o);
+    double y1 = 0.0, y2 = 0.0;
+    for (int m = 0; m < o; ++m) {
+        const long long col = oo * (a + (long long)v * m);
+        y1 += Y[i + (long long)o * m + col];
+        y2 += Y[m + (long long)o * i + col];
+    }
+    double g = 0.0, h = 0.0;
+    for (int e = 0; e < v; ++e) {
+        const double te = t1[i + (long long)o * e];
+        g = fma(te, G2[a + (long long)v * e], g);
+        h = fma(te, H1[a + (long long)v * e], h);
+    }
+    R1[t] += 2.0 * (y1 - g) - (y2 - h);
+}
+
+// c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e] (ooov column-major o x o x o x v)
+__global__ void ooov_diag_sums_kernel(const double *__restrict__ ooov, int o, int v, double *__restrict__ c12) {
+    const long long oo = (long long)o * o, ooo = oo * o, ov = (long long)o * v;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= ov) return;
+    const int n = (int)(t % o), e = (int)(t / o);
+    double s1 = 0.0, s2 = 0.0;
+    for (int m = 0; m < o; ++m) {
+        s1 += ooov[n + (long long)o * m + oo * m + ooo * e];
+        s2 += ooov[m + (long long)o * n + oo * m + ooo * e];
+    }
+    c12[t] = s1;
+    c12[ov + t] = s2;
 }
 
 __global__ void t1_finalize_kernel(double *__restrict__ t1n, const double *__restrict__ eps, int o, int v,
@@ -598,7 +886,8 @@ void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out) {
 }
 
 double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
-                   const double *Told, double *Tn) {
+                   const double *Told, double *Tn, const double *t1, const double *q) {
+    JUES_REQUIRE(!t1 == !q, "t2_finalize: t1 and q come together");
     long long npair = (long long)v * (v + 1) / 2;
     int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
     {
@@ -614,9 +903,10 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
                 attr_set.fetch_or(bit);
             }
             nb = (int)npair;
-            t2_finalize_smem_kernel<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
+            t2_finalize_smem_kernel<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red,
+                                                                             t1, q);
         } else {
-            t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red);
+            t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red, t1, q);
         }
         JUES_CHECK_CUDA(cudaGetLastError());
     }
@@ -693,12 +983,81 @@ void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o) {
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
+void fmi_from_x(Ctx *ctx, const double *Wp, const double *oooo, int o, double *Fmi) {
+    Ctx::Scope s(ctx, "fmi_trace");
+    const long long n = (long long)o * o;
+    fmi_from_x_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(Wp, oooo, o, Fmi);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void fae_from_rings(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
+                    double cJ, double cK, double *Fae, double *W12) {
+    Ctx::Scope s(ctx, "fae_trace");
+    const long long n = (long long)v * v;
+    fae_trace_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, cJ, cK, Fae, W12);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void ccsd_tau(Ctx *ctx, const double *T, const double *t1, int o, int v, double *Ttau, double *U) {
+    JUES_REQUIRE(o <= 2048, "ccsd_tau: nocc <= 2048");
+    Ctx::Scope s(ctx, "ccsd_tau");
+    const long long vv = (long long)v * v;
+    ccsd_tau_kernel<<<(unsigned)std::min<long long>(vv, 152LL * 8), 256, 2 * o * sizeof(double), ctx->stream>>>(
+        T, t1, o, v, Ttau, U);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void ring_traces(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
+                 double *tJ, double *tK) {
+    Ctx::Scope s(ctx, "fae_trace");
+    const long long n = (long long)v * v;
+    ring_traces_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, tJ, tK);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, const double *tGJ,
+              const double *tGK, const double *t1, const double *c12, const double *Fme, const double *fOV,
+              const double *fVV, int o, int v, bool mvariant, double *Fae, double *H1, double *G2, double *W12) {
+    Ctx::Scope s(ctx, "fae_trace");
+    const long long n = (long long)v * v;
+    ccsd_fae_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(WJ, J0, WK, K0, tGJ, tGK, t1, c12, Fme,
+                                                                          fOV, fVV, o, v, mvariant ? 1 : 0, Fae,
+                                                                          H1, G2, W12);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, int o, int v,
+               double *R1) {
+    Ctx::Scope s(ctx, "ccsd_t1");
+    const long long n = (long long)o * v;
+    t1_ytrace_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(Y, t1, G2, H1, o, v, R1);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void ooov_diag_sums(Ctx *ctx, const double *ooov, int o, int v, double *c12) {
+    Ctx::Scope s(ctx, "ooov_diag_sums");
+    const long long n = (long long)o * v;
+    ooov_diag_sums_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(ooov, o, v, c12);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
 void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double *c, double *out) {
     JUES_REQUIRE(m >= 1 && m <= 16, "lincomb supports 1..16 vectors");
     VecList vl;
     for (int k = 0; k < m; ++k) { vl.p[k] = vecs[k]; vl.c[k] = c[k]; }
+    bool aligned = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    for (int k = 0; k < m; ++k) aligned = aligned && (reinterpret_cast<uintptr_t>(vecs[k]) & 15) == 0;
+    JUES_REQUIRE(aligned, "lincomb: vectors must be 16-byte aligned");
     Ctx::Scope s(ctx, "lincomb");
-    lincomb_kernel<<<grid_for((long long)n), 256, 0, ctx->stream>>>(n, m, vl, out);
+    const unsigned grid = grid_for((long long)(n / 2 + 1));
+    switch (m) {
+#define JUES_LINCOMB(K) \
+    case K: lincomb_kernel<K><<<grid, 256, 0, ctx->stream>>>(n, vl, out); break;
+        JUES_LINCOMB(1) JUES_LINCOMB(2) JUES_LINCOMB(3) JUES_LINCOMB(4) JUES_LINCOMB(5) JUES_LINCOMB(6)
+        JUES_LINCOMB(7) JUES_LINCOMB(8) JUES_LINCOMB(9) JUES_LINCOMB(10) JUES_LINCOMB(11) JUES_LINCOMB(12)
+        JUES_LINCOMB(13) JUES_LINCOMB(14) JUES_LINCOMB(15) JUES_LINCOMB(16)
+#undef JUES_LINCOMB
+    }
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 

@@ -350,3 +350,36 @@ def test_rccd_default_split_s200_converged_within_one_microhartree(lib, s200):
                            return_log=True)
     assert len(log) < 60 and all(r[4] == JUES_PREC_SPLIT for r in log)
     assert abs(e - ref) < 1e-6, (e, ref, len(log))
+
+
+@pytest.mark.parametrize("method,name", [(0, "S25"), (0, "S100"), (1, "S25"), (1, "S100")])
+def test_one_split_sweep_against_fp64_sweep(lib, method, name):
+    # One sweep in split precision and one in FP64 from the same amplitudes (two FP64 sweeps from
+    # the MP2 guess, so T2 is pair-symmetric and t1 nonzero) on the same FP64 integrals.  The
+    # split sweep runs its ring contractions K-stacked (two GEMMs of K = 2 ov); its amplitudes
+    # must agree with the FP64 sweep's to the split arithmetic's ~1e-6 of max|T| and the energy
+    # to 1e-8 Eh, where any misplaced term would be >= 1e-3.
+    from juesgpu.CoupledCluster import CCSession
+    w = make_named(name).wfn()
+    kw = dict(guess="mp2", diis=False, r_conv=0.0, maxit=10, transform_precision="fp64")
+    ref = CCSession(method, w, precision="fp64", **kw)
+    ses = CCSession(method, w, precision="split_bf16", **kw)
+    ses.set_precision("fp64")
+    ref.iterate(2)
+    ses.iterate(2)
+    t1a, Ta = ref.amplitudes()
+    t1b, Tb = ses.amplitudes()
+    assert np.array_equal(Ta, Tb)
+    ref.iterate(1)
+    ses.set_precision("split_bf16")
+    ses.iterate(1)
+    t1a, Ta = ref.amplitudes()
+    t1b, Tb = ses.amplitudes()
+    scale = np.abs(Ta).max()
+    assert np.abs(Tb - Ta).max() < 3e-6 * scale, np.abs(Tb - Ta).max() / scale
+    if method == 1:
+        # t1 is a small sum of larger cancelling terms: its bar is relative to max|T2|
+        assert np.abs(t1b - t1a).max() < 3e-6 * scale, np.abs(t1b - t1a).max() / scale
+    assert abs(ses.energy() - ref.energy()) < 1e-8
+    ref.close()
+    ses.close()
