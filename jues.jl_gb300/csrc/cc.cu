@@ -71,6 +71,39 @@ DBuf<double> view_of(double *p, size_t n) {
 }  // namespace
 
 // ---------------------------------------------------------------------------------------
+// The ladders in split precision on K-stacked packs.  With ko = roundup(o^2, 128) and
+// kv = roundup(v^2, 128):  X = oovv . Tl^T (Tl = T2, or T2 + tau for CCSD) reads Tl from the
+// second block of stackLA; after W' is complete, one GEMM of K = ko + kv gives
+// L = oovv + W'^T . Tl + Tl . vvvv^T (the hole-hole and particle-particle ladders).
+// ---------------------------------------------------------------------------------------
+static void ladder_stacks_x(CCState *s, const double *Tl, const char *name) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, vv = v * v;
+    const long long ko = (oo + 127) / 128 * 128, kv = (vv + 127) / 128 * 128;
+    if (!s->stackLB.buf.p) {
+        s->stackLB.ensure(ctx, vv, ko + kv, 2);
+        pack_stacked(ctx, s->stackLB, ko, s->vvvv.p, plain(1), plain(vv), vv, vv, 1.0);   // vvvv[ab, ef]
+        s->stackXW.ensure(ctx, oo, kv, 2);
+        pack_stacked(ctx, s->stackXW, 0, s->oovv.p, plain(1), plain(oo), oo, vv, 1.0);    // oovv[mn, ef]
+    }
+    s->stackLA.ensure(ctx, oo, ko + kv, 2);
+    pack_stacked(ctx, s->stackLA, ko, Tl, plain(1), plain(oo), oo, vv, 1.0);              // Tl[ij, ef]
+    // W' = oooo + X
+    gett_tc_views(ctx, s->stackXW.view(0, kv), s->stackLA.view(ko, kv), oo, oo, 1.0, 1.0, s->Wp.p, plain(1),
+                  plain(oo), s->oooo.p, name);
+}
+
+static void ladder_stacks_l(CCState *s, const double *Tl, const char *name) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, vv = v * v;
+    const long long ko = (oo + 127) / 128 * 128, kv = (vv + 127) / 128 * 128;
+    pack_stacked(ctx, s->stackLA, 0, s->Wp.p, plain(oo), plain(1), oo, oo, 1.0);          // W'[mn, ij] as (ij, mn)
+    pack_stacked(ctx, s->stackLB, 0, Tl, plain(oo), plain(1), vv, oo, 1.0);               // Tl[mn, ab] as (ab, mn)
+    gett_tc_views(ctx, s->stackLA.view(0, ko + kv), s->stackLB.view(0, ko + kv), oo, vv, 1.0, 1.0, s->L.p,
+                  plain(1), plain(oo), s->oovv.p, name);
+}
+
+// ---------------------------------------------------------------------------------------
 // The ring contractions in split precision, on K-stacked packs (gett_tc_views).  With the
 // block width kb = roundup(ov, 128) and T2 read in the ring GEMMs' two layouts,
 //   R1 = T2[i,m,a,e] (rows (i,a), K (m,e)) and R23 = T2[m,i,a,e] (the same rows, m unit-stride),
@@ -142,19 +175,28 @@ double ccd_sweep(CCState *s, int prec) {
     s->cache_operands = is_split(prec);
     const double *W = s->oovv.p;
 
+    // In split precision the ladders and the ring contractions run on K-stacked packs (two planes).
+    const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;
     // W'[mn,ij] = oooo[mn,ij] + X[mn,ij], X = sum_ef oovv[mn,ef] T[ij,ef]  (Wmnij + the Wabef T-part)
-    G(s, prec, "ccd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), T, plain(oo), plain(1), 1.0, s->Wp.p,
-      plain(1), plain(oo), s->oooo.p);
+    if (stacked)
+        ladder_stacks_x(s, T, "ccd_x");
+    else
+        G(s, prec, "ccd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), T, plain(oo), plain(1), 1.0, s->Wp.p,
+          plain(1), plain(oo), s->oooo.p);
     // Fmi[m,i] = sum_nef oovv[m,n,e,f] T~[i,n,e,f] = sum_n 2 X[mn,in] - X[mn,ni]      (RCCD.jl:216)
     fmi_from_x(ctx, s->Wp.p, s->oooo.p, (int)o, s->Fmi.p);
     // - T[i,m,a,b] Fmi[m,j] - T[m,j,a,b] Fmi[m,i] (RCCD.jl:244) as hole-hole ladder terms:
     // W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i]
     wp_fmi(ctx, s->Wp.p, s->Fmi.p, (int)o);
     // L = oovv + (W')^T.T + T.vvvv^T                                     (RCCD.jl:243-246)
-    G(s, prec, "ccd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), T, plain(1), plain(oo),
-      1.0, s->L.p, plain(1), plain(oo), W);
-    G(s, prec, "ccd_pp_ladder", oo, vv, vv, 1.0, T, plain(1), plain(oo), s->vvvv.p, plain(vv), plain(1),
-      1.0, s->L.p, plain(1), plain(oo), nullptr, false, true);
+    if (stacked) {
+        ladder_stacks_l(s, T, "ccd_pp_ladder");
+    } else {
+        G(s, prec, "ccd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), T, plain(1), plain(oo),
+          1.0, s->L.p, plain(1), plain(oo), W);
+        G(s, prec, "ccd_pp_ladder", oo, vv, vv, 1.0, T, plain(1), plain(oo), s->vvvv.p, plain(vv), plain(1),
+          1.0, s->L.p, plain(1), plain(oo), nullptr, false, true);
+    }
 
     // Ring intermediates in (me),(bj) layout, their columns taken in (j,b) order.  With the pair
     // symmetry T[i,j,a,b] = T[j,i,b,a] and oovvT = 2 oovv[m,n,e,f] - oovv[n,m,e,f]:
@@ -165,8 +207,6 @@ double ccd_sweep(CCState *s, int prec) {
     // so T enters as B in the two layouts the ring GEMMs below read it as A (one pack each) and
     // no T~ is formed.  DF-RCCD.jl:239-242 reads WmBeJ's last term as oovv[m,n,e,f] T[n,j,f,b];
     // then the first term's weights are oovv instead of oovvT.
-    // In split precision the two WmBeJ GEMMs and the first two ring GEMMs run K-stacked.
-    const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;   // two planes
     const Mode jb = mode2(o, ov * v, ov);   // column (j,b) of a [(m,e),(b,j)] array
     if (stacked) {
         ring_stacks_begin(s, T);
@@ -475,7 +515,17 @@ double cc_total_energy(CCState *s) {
     // term), one dot product with weights formed once
     if (s->method == 0 && s->oovvT.p)
         return dot(s->ctx, (size_t)s->o * s->o * s->v * s->v, s->T.p, s->oovvT.p);
-    double e = cc_energy(s->ctx, s->oovv.p, s->T.p, s->method == 1 ? s->t1.p : nullptr, s->o, s->v);
+    double e;
+    if (s->method == 1 && s->oovvT.p) {
+        // CCSD: sum oovv (2X - X^T) with X = T2 + t1 (x) t1 = T2 . oovvT + sum_ia t1[i,a] F[i,a],
+        // F[i,a] = sum_jb oovvT[i,j,a,b] t1[j,b] (one GEMV into the Fme work array)
+        const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v;
+        G(s, JUES_PREC_FP64, "ccenergy", ov, 1, ov, 1.0, s->oovvT.p, mode2(o, 1, oo), mode2(o, o, oov), s->t1.p,
+          plain(1), plain(0), 0.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
+        e = dot(s->ctx, (size_t)(oo * v * v), s->T.p, s->oovvT.p) + dot(s->ctx, (size_t)ov, s->t1.p, s->Fme.p);
+    } else {
+        e = cc_energy(s->ctx, s->oovv.p, s->T.p, s->method == 1 ? s->t1.p : nullptr, s->o, s->v);
+    }
     if (s->fock && s->method == 1) e += 2.0 * dot(s->ctx, (size_t)s->o * s->v, s->fOV.p, s->t1.p);   // AutoRCCSD.jl:43
     return e;
 }
@@ -696,9 +746,14 @@ double ccsd_sweep(CCState *s, int prec) {
     // Fme = sum_nf oovvT[m,n,e,f] t1[n,f] (RCCSD.jl:204-210)
     G(s, JUES_PREC_FP64, "ccsd_fme", ov, 1, ov, 1.0, s->oovvT.p, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
       plain(0), 0.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
+    // In split precision the ladders, Y and the ring contractions run on K-stacked packs.
+    const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;   // two planes
     // W' = oooo + X, X = sum_ef oovv[mn,ef] Ttau[ij,ef] (Wmnij and Wabef's T2 + tau parts)
-    G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
-      plain(1), plain(oo), s->oooo.p, true, true);
+    if (stacked)
+        ladder_stacks_x(s, Ttau, "ccsd_x");
+    else
+        G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
+          plain(1), plain(oo), s->oooo.p, true, true);
     // Fmi (RCCSD.jl:195-203): sum_nef oovv[m,n,e,f] (2 Ts[i,n,e,f] - Ts[n,i,e,f]), Ts = T2 + tau/2,
     // = the trace of X less 1/2 Fme[m,e] t1[i,e]; then the ooov t1 terms
     fmi_from_x(ctx, s->Wp.p, s->oooo.p, (int)o, s->Fmi.p);
@@ -727,13 +782,16 @@ double ccsd_sweep(CCState *s, int prec) {
       s->Fmt.p, plain(1), plain(o));
     wp_fmi(ctx, s->Wp.p, s->Fmt.p, (int)o);
     // L = oovv + W'^T Ttau + Ttau vvvv^T  (Wabef's t1 parts go through Y below)
-    G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
-      1.0, s->L.p, plain(1), plain(oo), W, false, true);
-    G(s, prec, "ccsd_pp_ladder", oo, vv, vv, 1.0, Ttau, plain(1), plain(oo), s->vvvv.p, plain(vv),
-      plain(1), 1.0, s->L.p, plain(1), plain(oo), nullptr, true, true);
+    if (stacked) {
+        ladder_stacks_l(s, Ttau, "ccsd_pp_ladder");
+    } else {
+        G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
+          1.0, s->L.p, plain(1), plain(oo), W, false, true);
+        G(s, prec, "ccsd_pp_ladder", oo, vv, vv, 1.0, Ttau, plain(1), plain(oo), s->vvvv.p, plain(vv),
+          plain(1), 1.0, s->L.p, plain(1), plain(oo), nullptr, true, true);
+    }
 
     // ring intermediates (RCCSD.jl:229-247), layout [(m,e),(b,j)], columns taken in (j,b) order
-    const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;   // two planes
     const Mode jb = mode2(o, ov * v, ov);
     if (stacked) {
         ring_stacks_begin(s, U);
@@ -765,8 +823,19 @@ double ccsd_sweep(CCState *s, int prec) {
 
     // Y[ij,(a,m)] = sum_ef Ttau[i,j,e,f] <am|ef> (<am|ef> = ovvv[m,a,f,e])
     double *Y = s->aux2.p;
-    G(s, prec, "ccsd_y", oo, ov, vv, 1.0, Ttau, plain(1), plain(oo), ovvv, mode2(v, ovv, ov), mode2(v, o, 1),
-      0.0, Y, plain(1), plain(oo), nullptr, true, true);
+    if (stacked) {
+        // Ttau[ij,ef] from the ladder stack; ovvv as (a,m) x (e,f), packed once
+        const long long ko = (oo + 127) / 128 * 128, kv = (vv + 127) / 128 * 128;
+        if (!s->stackY.buf.p) {
+            s->stackY.ensure(ctx, ov, kv, 2);
+            pack_stacked(ctx, s->stackY, 0, ovvv, mode2(v, o, 1), mode2(v, ovv, ov), ov, vv, 1.0);
+        }
+        gett_tc_views(ctx, s->stackLA.view(ko, kv), s->stackY.view(0, kv), oo, ov, 1.0, 0.0, Y, plain(1), plain(oo),
+                      nullptr, "ccsd_y");
+    } else {
+        G(s, prec, "ccsd_y", oo, ov, vv, 1.0, Ttau, plain(1), plain(oo), ovvv, mode2(v, ovv, ov), mode2(v, o, 1),
+          0.0, Y, plain(1), plain(oo), nullptr, true, true);
+    }
 
     // T1 (RCCSD.jl:248-259) into t1n
     double *R1 = s->t1n.p;
@@ -789,6 +858,22 @@ double ccsd_sweep(CCState *s, int prec) {
     // the <ma|fe> terms from Y
     t1_ytrace(ctx, Y, t1, G2, H1, (int)o, (int)v, R1);
 
+    // Z's t1 terms with t1 on b, by their (i,a)<->(j,b) images all of the form
+    // -sum_m Q[i,j,a,m] t1[m,b], with Q (in place of Y, layout [(i,j),(a,m)]) =
+    //   Y[i,j,a,m]                                 (Wabef's t1 parts)
+    // + Y1[j,m,i,a], Y1[i,m,j,b] = sum_e t1[i,e] <mj|eb>   (- tau[i,m,e,a] <mb|ej>, imaged)
+    // + Y2[i,m,a,j], Y2[i,m,a,j] = sum_e t1[i,e] <ma|je>   (- tau[i,m,e,b] <am|ej>)
+    // + <mi|ja> = ooov[m,i,j,a]                            (- t1[m,a] <mb|ij>, imaged)
+    G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo), mode3(o, o, 1, o, oov), 1.0, Y,
+      plain(o), mode3(o, o, oov, 1, oo), nullptr, false, true);
+    G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov), plain(1), 1.0, Y, plain(1),
+      mode3(o, v, oov, oo, o), nullptr, false, true);
+    {
+        // box (i, j, a, m): ooov[m,i,j,a] at m + o i + oo j + ooo a; Q[i,j,a,m] at i + o j + oo a + oov m
+        Perm4 p{{o, o, v, o}, {o, oo, ooo, 1}, {1, o, oo, oov}};
+        permute4(ctx, p, 1.0, ooov, 1.0, Y);
+    }
+
     // Z (RCCSD.jl:264-284, one member of each (i,a)<->(j,b) pair)
     double *Z = s->Z.p;
     // + T2[i,m,a,e] (2 WmBeJ + WmBEj + [m = j] F~ae)[m,b,e,j] - T2[m,i,a,e] WmBeJ[m,b,e,j]
@@ -803,25 +888,12 @@ double ccsd_sweep(CCState *s, int prec) {
         G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->WK.p, plain(1),
           plain(ov), 1.0, Z, mode2(o, 1, oov), mode2(v, oo, o), nullptr, true, false);
     }
-    // Wabef's t1 parts: Z[i,j,a,b] -= sum_m Y[ij,a,m] t1[m,b]
+    // Z[i,j,a,b] -= sum_m Q[i,j,a,m] t1[m,b]: Wabef's t1 parts and the tau and ooov t1 terms
     G(s, prec, "ccsd_y_t1", oov, v, o, -1.0, Y, plain(1), plain(oov), t1, plain(1), plain(o), 1.0, Z,
       plain(1), plain(oov));
-    // - tau[i,m,e,a] <mb|ej>: Y1[i,m,j,b] = sum_e t1[i,e] oovv[m,j,e,b]; Z -= sum_m t1[m,a] Y1[i,m,j,b]
-    G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo),
-      mode3(o, o, 1, o, oov), 0.0, Y, plain(1), plain(o), nullptr, false, true);
-    G(s, prec, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, o, 1, oo, ooo), plain(o), t1,
-      plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo));
-    // - tau[i,m,e,b] <am|ej>: Y2[i,m,a,j] = sum_e t1[i,e] ovov[m,a,j,e]; Z -= sum_m Y2 t1[m,b]
-    G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov),
-      plain(1), 0.0, Y, plain(1), plain(o), nullptr, false, true);
-    G(s, prec, "ccsd_z_tau", oov, v, o, -1.0, Y, mode3(o, v, 1, oo, oov), plain(o), t1,
-      plain(1), plain(o), 1.0, Z, mode3(o, v, 1, oo, o), plain(oov));
     // + t1[i,e] <ab|ej> = t1[i,e] ovvv[j,a,b,e]
     G(s, prec, "ccsd_z_ovvv", o, ovv, v, 1.0, t1, plain(1), plain(o), ovvv, plain(ovv), plain(1), 1.0, Z,
       plain(1), plain(o), nullptr, false, true);
-    // - t1[m,a] <mb|ij> = t1[m,a] ooov[m,j,i,b]
-    G(s, prec, "ccsd_z_ooov", oov, v, o, -1.0, ooov, mode3(o, o, oo, o, ooo), plain(1), t1,
-      plain(1), plain(o), 1.0, Z, mode3(o, o, 1, o, oov), plain(oo), nullptr, true, false);
 
     if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia
     // q[b,j] = sum_m t1[m,b] F~mi[m,j]: the hole-hole ladder's tau[i,m,a,b] F~mi[m,j] terms, undone

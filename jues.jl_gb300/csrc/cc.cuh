@@ -33,6 +33,10 @@ struct CCState {
     // (CCD) or (1/2 oovvT, -1/2 oovv) (CCSD); stackT: T2[m,i,a,e] | T2[i,m,a,e] (| U[m,i,a,e],
     // CCSD); stackR: -WJ | W12; stackK: WK
     StackedPack stackW, stackT, stackR, stackK;
+    // split precision: the two ladders as one GEMM, L = oovv + [W'^T | T] . [T ; vvvv]^T over
+    // K = (m,n) then (e,f): stackLA = [W'^T | T] (rows (i,j)), stackLB = [T | vvvv] (rows (a,b),
+    // vvvv packed once); stackXW = oovv (rows (m,n), K (e,f)) for X, stackY = ovvv (CCSD's Y)
+    StackedPack stackLA, stackLB, stackXW, stackY;
     // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
     std::vector<DBuf<double>> dv, de;
     std::vector<std::vector<double>> gram;   // gram[k][l] = e_k . e_l, k,l in insertion order

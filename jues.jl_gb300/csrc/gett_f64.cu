@@ -288,6 +288,77 @@ __global__ void __launch_bounds__(256, NN == 1 ? 3 : 2) gett_f64_skinny(GroupPro
     }
 }
 
+// skinny GEMM (N <= NN <= 8) whose rows, not K, are the unit-stride index of A: one thread per
+// output row, so a warp's loads of one K position are 32 consecutive doubles; blockIdx.y takes
+// K positions [y kper, (y + 1) kper) (four independent positions in flight per thread) and writes
+// its partial sums to part[y][n][m] for the split-K reduction (kper = K: one part)
+template <int NN>
+__global__ void __launch_bounds__(256) gett_f64_rows(GroupProblem g, long long kper, double *__restrict__ part) {
+    const long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (m >= g.M) return;
+    const long long k0 = blockIdx.y * kper, k1 = min(g.K, k0 + kper);
+    const long long om = mode_off(g.mA, m);
+    long long onb[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) onb[j] = j < g.N ? mode_off(g.nB, j) : 0;
+    double acc[NN];
+#pragma unroll
+    for (int j = 0; j < NN; ++j) acc[j] = 0.0;
+    constexpr int U = 4;
+    ModeIter ia[U], ib[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        ia[u].init(g.kA, k0 + u);
+        ib[u].init(g.kB, k0 + u);
+    }
+    for (long long k = k0; k < k1; k += U) {
+        double a[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) a[u] = k + u < k1 ? __ldg(g.A + om + ia[u].off) : 0.0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (k + u < k1) {
+                const long long ok = ib[u].off;
+#pragma unroll
+                for (int j = 0; j < NN; ++j)
+                    if (j < g.N) acc[j] = fma(a[u], __ldg(g.B + ok + onb[j]), acc[j]);
+            }
+            ia[u].step(g.kA, U);
+            ib[u].step(g.kB, U);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NN; ++j)
+        if (j < g.N) part[(blockIdx.y * g.N + j) * g.M + m] = acc[j];
+}
+
+// small GEMM (M N <= 2^16 outputs, K <= 8192): one warp per output element, its lanes over K,
+// so that even a single-tile problem spreads over the whole GPU instead of one CTA
+__global__ void __launch_bounds__(256) gett_f64_small(GroupProblem g) {
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= g.M * g.N) return;
+    const long long m = w % g.M, n = w / g.M;
+    const long long oa = mode_off(g.mA, m), ob = mode_off(g.nB, n);
+    ModeIter ia, ib;
+    ia.init(g.kA, lane);
+    ib.init(g.kB, lane);
+    double acc = 0.0;
+    for (long long k = lane; k < g.K; k += 32) {
+        acc = fma(__ldg(g.A + oa + ia.off), __ldg(g.B + ob + ib.off), acc);
+        ia.step(g.kA, 32);
+        ib.step(g.kB, 32);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
+    if (lane == 0) {
+        const long long off = mode_off(g.mC, m) + mode_off(g.nC, n);
+        double r = g.alpha * acc;
+        if (g.beta != 0.0) r = fma(g.beta, g.Cin[off], r);
+        g.C[off] = r;
+    }
+}
+
 }  // namespace
 
 GroupProblem to_problem(const GettArgs &a) {
@@ -306,6 +377,35 @@ GroupProblem to_problem(const GettArgs &a) {
 void gett_f64(Ctx *ctx, const GettArgs &a, const char *name) {
     if (a.M <= 0 || a.N <= 0) return;
     GroupProblem g = to_problem(a);
+    if (a.N > 8 && a.M * a.N <= (1LL << 16) && a.K <= 8192) {
+        Ctx::Scope s(ctx, name);
+        gett_f64_small<<<(unsigned)((a.M * a.N * 32 + 255) / 256), 256, 0, ctx->stream>>>(g);
+        JUES_CHECK_CUDA(cudaGetLastError());
+        return;
+    }
+    const bool k_unit = a.kA.s0 == 1 && a.kA.d0 > 1, rows_unit = a.mA.s0 == 1 && a.mA.d0 > 1;
+    if (a.N <= 8 && rows_unit && !k_unit && a.M >= 256) {
+        // thread per row, K split over blockIdx.y so that about eight blocks run per SM
+        const long long rb = (a.M + 255) / 256;
+        long long ks = std::max<long long>(1, std::min<long long>((152LL * 8 + rb - 1) / rb, a.K / 64));
+        ks = std::min<long long>(ks, 65535);
+        long long kper = (a.K + ks - 1) / ks;
+        kper = (kper + 3) / 4 * 4;
+        ks = (a.K + kper - 1) / kper;
+        JUES_REQUIRE(rb < (1LL << 31), "GEMM too large for one launch");
+        double *ws = static_cast<double *>(ctx->splitk_scratch((size_t)(ks * a.M * a.N) * sizeof(double)));
+        {
+            Ctx::Scope s(ctx, name);
+            const dim3 grid((unsigned)rb, (unsigned)ks);
+            if (a.N == 1)
+                gett_f64_rows<1><<<grid, 256, 0, ctx->stream>>>(g, kper, ws);
+            else
+                gett_f64_rows<8><<<grid, 256, 0, ctx->stream>>>(g, kper, ws);
+            JUES_CHECK_CUDA(cudaGetLastError());
+        }
+        splitk_reduce(ctx, ws, (int)ks, a.M * a.N, a.M, a.M, a.N, a.alpha, a.beta, a.C, g.Cin, a.mC, a.nC, name);
+        return;
+    }
     if (a.N <= 8) {
         long long blocks = (a.M * 32 + 255) / 256;
         JUES_REQUIRE(blocks < (1LL << 31), "GEMM too large for one launch");

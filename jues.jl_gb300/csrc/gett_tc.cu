@@ -1593,6 +1593,14 @@ void gett_tc_views(Ctx *ctx, const PackedView &A, const PackedView &B, long long
         t.partial = static_cast<float *>(
             ctx->splitk_scratch((size_t)t.ksplit * roundup(M, TBM) * Npad * sizeof(float)));
     }
+    // C = Cin + alpha AB into a dense column-major C: copy Cin over first and accumulate in place
+    const bool disjoint = t.Cin + M * N <= t.C || t.C + M * N <= t.Cin;
+    if (t.ksplit <= 1 && beta == 1.0 && t.Cin != t.C && disjoint && mC.d0 == MODE_BIG && mC.s0 == 1 &&
+        nC.d0 == MODE_BIG && nC.s0 == M) {
+        JUES_CHECK_CUDA(cudaMemcpyAsync(C, t.Cin, (size_t)(M * N) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                        ctx->stream));
+        t.Cin = t.C;
+    }
     if (np == 3)
         launch_tc<64, 3, 3>(ctx, ma, mb, t, tiles, name);
     else if (BN == 128)

@@ -21,6 +21,13 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// warp-wide sum, valid in every lane
+__device__ __forceinline__ double warp_allsum(double v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
 // block-wide sum; result valid in thread 0
 __device__ __forceinline__ double block_sum(double v) {
     __shared__ double s[32];
@@ -266,7 +273,8 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
 // Z[:,:,a,b] and Z[:,:,b,a] are contiguous o x o blocks, loaded coalesced into shared memory on
 // an odd row pitch (conflict-free transposed reads), so every global access is unit-stride.
 // Dynamic shared memory 2 o pitch doubles (o <= 64).
-__global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__restrict__ L,
+template <bool RANK1>
+__global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(const double *__restrict__ L,
                                                                const double *__restrict__ Z,
                                                                const double *__restrict__ invD, int o, int v,
                                                                const double *__restrict__ Told,
@@ -281,72 +289,7 @@ __global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__r
     int a, b;
     pair_ab(blockIdx.x, a, b);   // one (a <= b) pair per block: resident blocks overlap their phases
     const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
-    if ((o & 1) == 0) {
-        // even o: element pairs (i, i+1) of one column j as 16-byte accesses; (i, j) advance by
-        // carries (step 2 blockDim.x, i stays even)
-        const int n2 = ooi / 2, step = 2 * blockDim.x, di = step % o, dj = step / o;
-        const double2 *Z2ab = reinterpret_cast<const double2 *>(Z + ab), *Z2ba = reinterpret_cast<const double2 *>(Z + ba);
-        {
-            int i = (2 * threadIdx.x) % o, j = (2 * threadIdx.x) / o;
-#pragma unroll 2
-            for (int k = threadIdx.x; k < n2; k += blockDim.x) {
-                const double2 za = Z2ab[k], zb = Z2ba[k];
-                zs[j + pitch * i] = za.x;
-                zs[j + pitch * (i + 1)] = za.y;
-                zs[o * pitch + j + pitch * i] = zb.x;
-                zs[o * pitch + j + pitch * (i + 1)] = zb.y;
-                i += di; j += dj;
-                if (i >= o) { i -= o; ++j; }
-            }
-        }
-        __syncthreads();
-        const double2 *L2ab = reinterpret_cast<const double2 *>(L + ab), *L2ba = reinterpret_cast<const double2 *>(L + ba);
-        const double2 *D2 = reinterpret_cast<const double2 *>(invD + ab);
-        double2 *T2ab = reinterpret_cast<double2 *>(Tn + ab), *T2ba = reinterpret_cast<double2 *>(Tn + ba);
-        int i = (2 * threadIdx.x) % o, j = (2 * threadIdx.x) / o;
-#pragma unroll 2
-        for (int k = threadIdx.x; k < n2; k += blockDim.x) {
-            const double2 inv = D2[k];   // D is symmetric in (a, b)
-            const double2 l = L2ab[k];
-            double2 x;
-            x.x = l.x + zs[j + pitch * i] + zs[o * pitch + i + pitch * j];
-            x.y = l.y + zs[j + pitch * (i + 1)] + zs[o * pitch + i + 1 + pitch * j];
-            if (t1) {
-                x.x += rank1_pair(t1, q, o, v, i, j, a, b);
-                x.y += rank1_pair(t1, q, o, v, i + 1, j, a, b);
-            }
-            x.x *= inv.x;
-            x.y *= inv.y;
-            T2ab[k] = x;
-            if (Told) {
-                const double2 t = reinterpret_cast<const double2 *>(Told + ab)[k];
-                const double d0 = x.x - t.x, d1 = x.y - t.y;
-                acc = fma(d0, d0, acc);
-                acc = fma(d1, d1, acc);
-            }
-            if (a != b) {
-                const double2 lb = L2ba[k];
-                double2 y;
-                y.x = lb.x + zs[o * pitch + j + pitch * i] + zs[i + pitch * j];
-                y.y = lb.y + zs[o * pitch + j + pitch * (i + 1)] + zs[i + 1 + pitch * j];
-                if (t1) {
-                    y.x += rank1_pair(t1, q, o, v, i, j, b, a);
-                    y.y += rank1_pair(t1, q, o, v, i + 1, j, b, a);
-                }
-                y.x *= inv.x;
-                y.y *= inv.y;
-                T2ba[k] = y;
-                if (Told) {
-                    const double2 t = reinterpret_cast<const double2 *>(Told + ba)[k];
-                    const double d0 = y.x - t.x, d1 = y.y - t.y;
-                    acc = fma(d0, d0, acc);
-                    acc = fma(d1, d1, acc);
-                }
-            }
-            i += di; j += dj;
-            if (i >= o) { i -= o; ++j; }
-        }
-    } else {
+    {
         for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
             const int i = ij % o, j = ij / o;
             zs[j + pitch * i] = Z[ab + ij];
@@ -359,14 +302,14 @@ __global__ void __launch_bounds__(256) t2_finalize_smem_kernel(const double *__r
             const double zab = zs[j + pitch * i], zba_t = zs[o * pitch + i + pitch * j];
             const double inv = invD[ab + ij];   // D is symmetric in (a, b)
             double x = L[ab + ij] + zab + zba_t;
-            if (t1) x += rank1_pair(t1, q, o, v, i, j, a, b);
+            if (RANK1) x += rank1_pair(t1, q, o, v, i, j, a, b);
             x *= inv;
             Tn[ab + ij] = x;
             if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
             if (a != b) {
                 const double zba = zs[o * pitch + j + pitch * i], zab_t = zs[i + pitch * j];
                 double y = L[ba + ij] + zba + zab_t;
-                if (t1) y += rank1_pair(t1, q, o, v, i, j, b, a);
+                if (RANK1) y += rank1_pair(t1, q, o, v, i, j, b, a);
                 y *= inv;
                 Tn[ba + ij] = y;
                 if (Told) { const double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
@@ -532,26 +475,27 @@ __global__ void fmi_from_x_kernel(const double *__restrict__ Wp, const double *_
 // tJ[a,e] = sum_m t[(m,e),(a,m)] and tK[a,e] = sum_m u[(m,e),(a,m)] give
 // Fae[a,e] = -(cJ tJ + cK tK) by the pair symmetry of T2; then W12[(j,e),(a,j)] += Fae[a,e]
 // for every j, so the ring GEMM T[i,m,a,e] W12[(m,e),(b,j)] also yields T[i,j,a,e] Fae[b,e].
-// One thread per (a, e); the (m = j) entries it reads and the ones it updates are the same.
+// One warp per (a, e), its lanes over m; the (m = j) entries it reads and the ones it updates
+// are the same.
 __global__ void fae_trace_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
                                  const double *__restrict__ WK, const double *__restrict__ K0, int o, int v,
                                  double cJ, double cK, double *__restrict__ Fae, double *__restrict__ W12) {
     const long long ov = (long long)o * v;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (t >= (long long)v * v) return;
     const int e = (int)(t % v), a = (int)(t / v);
     const long long base = (long long)o * e + ov * a, step = 1 + ov * v;
     double tj = 0.0, tk = 0.0;
-#pragma unroll 4
-    for (int m = 0; m < o; ++m) {
+    for (int m = lane; m < o; m += 32) {
         const long long x = base + step * m;
         tj += WJ[x] - J0[x];
         tk += WK[x] - K0[x];
     }
-    const double f = -(cJ * tj + cK * tk);
-    Fae[a + (long long)v * e] = f;
+    const double f = -(cJ * warp_allsum(tj) + cK * warp_allsum(tk));
+    if (lane == 0) Fae[a + (long long)v * e] = f;
     if (W12)
-        for (int j = 0; j < o; ++j) W12[base + step * j] += f;
+        for (int j = lane; j < o; j += 32) W12[base + step * j] += f;
 }
 
 // CCSD sweep inputs from T2 and t1 in one pass: Ttau = T2 + tau and U = T2 + 2 tau with
@@ -582,24 +526,28 @@ __global__ void __launch_bounds__(256) ccsd_tau_kernel(const double *__restrict_
 
 // Traces over m of the GEMM parts of the CCSD ring intermediates (layout [(m,e),(b,j)]):
 // tJ[a,e] = sum_m (WJ - J0)[(m,e),(a,m)], tK[a,e] = sum_m (WK - K0)[(m,e),(a,m)].  One thread
-// per (a, e).
+// warp per (a, e), its lanes over m.
 __global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
                                    const double *__restrict__ WK, const double *__restrict__ K0, int o, int v,
                                    double *__restrict__ tJ, double *__restrict__ tK) {
     const long long ov = (long long)o * v;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (t >= (long long)v * v) return;
     const int e = (int)(t % v), a = (int)(t / v);
     const long long base = (long long)o * e + ov * a, step = 1 + ov * v;
     double tj = 0.0, tk = 0.0;
-#pragma unroll 4
-    for (int m = 0; m < o; ++m) {
+    for (int m = lane; m < o; m += 32) {
         const long long x = base + step * m;
         tj += WJ[x] - J0[x];
         tk += WK[x] - K0[x];
     }
-    tJ[a + (long long)v * e] = tj;
-    tK[a + (long long)v * e] = tk;
+    tj = warp_allsum(tj);
+    tk = warp_allsum(tk);
+    if (lane == 0) {
+        tJ[a + (long long)v * e] = tj;
+        tK[a + (long long)v * e] = tk;
+    }
 }
 
 // CCSD Fae and F~ae from the ring intermediates (RCCSD.jl:187-194, or mRCCSD.jl:137-149's t1
@@ -611,7 +559,8 @@ __global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *
 //   Fae = 2 G2 - H1' - (tGJ + 2 tGK) + 1/2 t1^T (Fme - fOV) + fVV - 1/2 t1^T fOV
 // (H1' = H1, or H1^T for mRCCSD.jl:140's <me|af>), F~ae = Fae - 1/2 t1^T Fme.  Writes Fae, H1, G2
 // (the T1 equation's tau corrections) and adds F~ae[a,e] to W12[(j,e),(a,j)] for every j, where
-// the first ring GEMM turns it into the T2[i,j,a,e] F~ae[b,e] term.  One thread per (a, e).
+// the first ring GEMM turns it into the T2[i,j,a,e] F~ae[b,e] term.  One warp per (a, e), its
+// lanes over m and n.
 __global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
                                 const double *__restrict__ WK, const double *__restrict__ K0,
                                 const double *__restrict__ tGJ, const double *__restrict__ tGK,
@@ -621,43 +570,44 @@ __global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__r
                                 double *__restrict__ Fae, double *__restrict__ H1, double *__restrict__ G2,
                                 double *__restrict__ W12) {
     const long long ov = (long long)o * v;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (t >= (long long)v * v) return;
     const int e = (int)(t % v), a = (int)(t / v);
     const long long step = 1 + ov * v;
     const long long base = (long long)o * e + ov * a;
     const double *c1 = c12, *c2 = c12 + ov;
-    double tj = 0.0, tk = 0.0;
-    for (int m = 0; m < o; ++m) {
+    double tj = 0.0, tk = 0.0, s1 = 0.0, s2 = 0.0, tf = 0.0, tfo = 0.0, tj2 = 0.0, s12 = 0.0;
+    const long long base2 = (long long)o * a + ov * e;
+    for (int m = lane; m < o; m += 32) {
         const long long x = base + step * m;
         tj += WJ[x] - J0[x];
         tk += WK[x] - K0[x];
+        const double ta = t1[m + (long long)o * a];
+        s1 = fma(ta, c1[m + (long long)o * e], s1);
+        s2 = fma(ta, c2[m + (long long)o * e], s2);
+        tf = fma(ta, Fme[m + (long long)o * e], tf);
+        if (fOV) tfo = fma(ta, fOV[m + (long long)o * e], tfo);
+        if (mvariant) {
+            // H1[e,a]: the WJ trace at [(m,a),(e,m)] and S1[e,a]
+            tj2 += WJ[base2 + step * m] - J0[base2 + step * m];
+            s12 = fma(t1[m + (long long)o * e], c1[m + (long long)o * a], s12);
+        }
     }
-    double s1 = 0.0, s2 = 0.0, tf = 0.0, tfo = 0.0;
-    for (int n = 0; n < o; ++n) {
-        const double ta = t1[n + (long long)o * a];
-        s1 = fma(ta, c1[n + (long long)o * e], s1);
-        s2 = fma(ta, c2[n + (long long)o * e], s2);
-        tf = fma(ta, Fme[n + (long long)o * e], tf);
-        if (fOV) tfo = fma(ta, fOV[n + (long long)o * e], tfo);
-    }
+    tj = warp_allsum(tj); tk = warp_allsum(tk); s1 = warp_allsum(s1); s2 = warp_allsum(s2);
+    tf = warp_allsum(tf); tfo = warp_allsum(tfo);
+    if (mvariant) { tj2 = warp_allsum(tj2); s12 = warp_allsum(s12); }
     const long long ae = a + (long long)v * e;
     const double h1 = tj - tGJ[ae] + s1, g2 = tGK[ae] - tk + s2;
-    double h1x = h1;
-    if (mvariant) {
-        // H1[e,a]: the WJ trace at [(m,a),(e,m)] and S1[e,a]
-        const long long base2 = (long long)o * a + ov * e, ea = e + (long long)v * a;
-        double tj2 = 0.0, s12 = 0.0;
-        for (int m = 0; m < o; ++m) tj2 += WJ[base2 + step * m] - J0[base2 + step * m];
-        for (int n = 0; n < o; ++n) s12 = fma(t1[n + (long long)o * e], c1[n + (long long)o * a], s12);
-        h1x = tj2 - tGJ[ea] + s12;
-    }
+    const double h1x = mvariant ? tj2 - tGJ[e + (long long)v * a] + s12 : h1;
     double ft = 2.0 * g2 - h1x - (tGJ[ae] + 2.0 * tGK[ae]) - tfo;   // F~ae
     if (fVV) ft += fVV[ae];
-    Fae[ae] = fma(0.5, tf, ft);
-    H1[ae] = h1;
-    G2[ae] = g2;
-    for (int j = 0; j < o; ++j) W12[base + step * j] += ft;
+    if (lane == 0) {
+        Fae[ae] = fma(0.5, tf, ft);
+        H1[ae] = h1;
+        G2[ae] = g2;
+    }
+    for (int j = lane; j < o; j += 32) W12[base + step * j] += ft;
 }
 
 // T1's <ma|fe> terms from Y[(i,j),(a,m)] = sum_ef Ttau[i,j,e,f] <ma|fe> (the Wabef t1
@@ -895,16 +845,24 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
         // one block per pair; the step norm's partials (one per block) must fit the reduction scratch
         if (o <= 64 && npair <= 65536 - 64) {
             const size_t smem = (size_t)2 * o * (o | 1) * sizeof(double);
+            // the rank-one term is a template parameter: without it the kernel fits 32 registers
+            // and eight blocks per SM
             static std::atomic<unsigned long long> attr_set{0};
             const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
             if (smem > 48 * 1024 && (!bit || !(attr_set.load() & bit))) {
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel,
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
                 attr_set.fetch_or(bit);
             }
             nb = (int)npair;
-            t2_finalize_smem_kernel<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red,
-                                                                             t1, q);
+            if (t1)
+                t2_finalize_smem_kernel<true><<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn,
+                                                                                   ctx->d_red, t1, q);
+            else
+                t2_finalize_smem_kernel<false><<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn,
+                                                                                    ctx->d_red, nullptr, nullptr);
         } else {
             t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red, t1, q);
         }
@@ -994,7 +952,8 @@ void fae_from_rings(Ctx *ctx, const double *WJ, const double *J0, const double *
                     double cJ, double cK, double *Fae, double *W12) {
     Ctx::Scope s(ctx, "fae_trace");
     const long long n = (long long)v * v;
-    fae_trace_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, cJ, cK, Fae, W12);
+    fae_trace_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, cJ, cK, Fae,
+                                                                               W12);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -1011,7 +970,7 @@ void ring_traces(Ctx *ctx, const double *WJ, const double *J0, const double *WK,
                  double *tJ, double *tK) {
     Ctx::Scope s(ctx, "fae_trace");
     const long long n = (long long)v * v;
-    ring_traces_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, tJ, tK);
+    ring_traces_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, tJ, tK);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -1020,7 +979,7 @@ void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, co
               const double *fVV, int o, int v, bool mvariant, double *Fae, double *H1, double *G2, double *W12) {
     Ctx::Scope s(ctx, "fae_trace");
     const long long n = (long long)v * v;
-    ccsd_fae_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(WJ, J0, WK, K0, tGJ, tGK, t1, c12, Fme,
+    ccsd_fae_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, J0, WK, K0, tGJ, tGK, t1, c12, Fme,
                                                                           fOV, fVV, o, v, mvariant ? 1 : 0, Fae,
                                                                           H1, G2, W12);
     JUES_CHECK_CUDA(cudaGetLastError());

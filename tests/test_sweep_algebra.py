@@ -118,7 +118,8 @@ def ccsd_device_form(blocks, t1, T, variant="jl", fock=None):
     Fme from oovvT; Fmi from the trace of X = oovv . Ttau^T; the T2 parts of WmBeJ / WmBEj as
     three GEMMs on T2 and U = T2 + 2 tau; Fae, H1, G2 from the traces of WJ and WK before and
     after their t1 terms; T1's <ma|fe> terms from the traces of Y; F~ae in the first ring GEMM,
-    F~mi in the hole-hole ladder with the rank-one correction t1[i,a] q[b,j] in the finalisation.
+    F~mi in the hole-hole ladder with the rank-one correction t1[i,a] q[b,j] in the finalisation;
+    Z's t1 terms with t1 on b (Wabef's, the two tau terms, the ooov term) as one -Q . t1.
     """
     oooo, ooov, oovv, ovov, ovvv, vvvv = blocks
     o, v = t1.shape
@@ -168,10 +169,12 @@ def ccsd_device_form(blocks, t1, T, variant="jl", fock=None):
           - E("mnae,mnie->ia", T, ooovT))
     R1 += (2 * (np.einsum("imam->ia", Y) - E("ie,ae->ia", t1, G2))
            - (np.einsum("miam->ia", Y) - E("if,af->ia", t1, H1)))        # t1_ytrace
+    # Q[i,j,a,m] = Y + Y1[j,m,i,a] + Y2[i,m,a,j] + ooov[m,i,j,a] (the t1-on-b terms, imaged)
+    Y1 = E("ie,mjeb->imjb", t1, oovv)
+    Y2 = E("ie,maje->imaj", t1, ovov)
+    Q = Y + Y1.transpose(2, 0, 3, 1) + Y2.transpose(0, 3, 2, 1) + ooov.transpose(1, 2, 3, 0)
     Z = (E("imae,mbej->ijab", T, W12) - E("miae,mbej->ijab", T, WJ) + E("mibe,maej->ijab", T, WK)
-         - E("ijam,mb->ijab", Y, t1)
-         - E("ie,ma,mjeb->ijab", t1, t1, oovv) - E("ie,mb,maje->ijab", t1, t1, ovov)
-         + E("ie,jabe->ijab", t1, ovvv) - E("ma,mjib->ijab", t1, ooov))
+         - E("ijam,mb->ijab", Q, t1) + E("ie,jabe->ijab", t1, ovvv))
     if fock is not None:
         R1 = R1 + fOV
     q = E("mb,mj->bj", t1, Fmt)
