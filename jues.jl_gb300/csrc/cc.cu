@@ -291,9 +291,9 @@ static void diis_reset(CCState *s) {
     s->gram.clear();
 }
 
-// x = vector fed into the sweep, xn = sweep output (both length len, device); on return x holds
-// the extrapolated vector.
-static void diis_step(CCState *s, double *x, const double *xn, size_t len, double *ee = nullptr) {
+// the slot of the next (amplitude, error) pair, the oldest evicted when full; olds = the stored
+// errors that stay, in insertion order
+static int diis_begin(CCState *s, size_t len, std::vector<const double *> &olds) {
     Ctx *ctx = s->ctx;
     const int cap = std::max(1, s->opts.diis_size - 1);
     if ((int)s->dv.size() < cap) {
@@ -313,12 +313,17 @@ static void diis_step(CCState *s, double *x, const double *xn, size_t len, doubl
         s->dv[slot] = DBuf<double>(ctx, len);
         s->de[slot] = DBuf<double>(ctx, len);
     }
-    // the new pair and its overlaps with the stored errors, in one pass
+    olds.resize(s->dorder.size());
+    for (size_t k = 0; k < s->dorder.size(); ++k) olds[k] = s->de[s->dorder[k]].p;
+    return slot;
+}
+
+// the slot's pair is stored and dots = [e.e, olds_k.e]: extend the Gram matrix, solve, and
+// extrapolate into x
+static void diis_finish(CCState *s, double *x, int slot, size_t len, const std::vector<double> &dots,
+                        double *ee) {
+    Ctx *ctx = s->ctx;
     const int m = (int)s->dorder.size() + 1;
-    std::vector<const double *> olds(m - 1);
-    for (int k = 0; k < m - 1; ++k) olds[k] = s->de[s->dorder[k]].p;
-    std::vector<double> dots(m);
-    diis_error(ctx, len, xn, x, s->dv[slot].p, s->de[slot].p, m - 1, olds.data(), dots.data());
     s->dorder.push_back(slot);
     std::vector<double> row(m);
     for (int k = 0; k < m - 1; ++k) row[k] = dots[1 + k];
@@ -336,12 +341,23 @@ static void diis_step(CCState *s, double *x, const double *xn, size_t len, doubl
         for (int l = 0; l < m; ++l) B[k * nb + l] = mx > 0 ? s->gram[k][l] / mx : 0.0;
     rhs[m] = -1.0;
     if (mx == 0.0 || !solve_small(B, rhs, nb, c)) {
-        d2d(ctx, x, xn, len);   // degenerate subspace: plain update
+        d2d(ctx, x, s->dv[slot].p, len);   // degenerate subspace: plain update
         return;
     }
     std::vector<const double *> vecs(m);
     for (int k = 0; k < m; ++k) vecs[k] = s->dv[s->dorder[k]].p;
     lincomb(ctx, len, m, vecs.data(), c.data(), x);
+}
+
+// x = vector fed into the sweep, xn = sweep output (both length len, device); on return x holds
+// the extrapolated vector and *ee = |xn - x|^2.
+static void diis_step(CCState *s, double *x, const double *xn, size_t len, double *ee = nullptr) {
+    std::vector<const double *> olds;
+    const int slot = diis_begin(s, len, olds);
+    // the new pair and its overlaps with the stored errors, in one pass
+    std::vector<double> dots(olds.size() + 1);
+    diis_error(s->ctx, len, xn, x, s->dv[slot].p, s->de[slot].p, (int)olds.size(), olds.data(), dots.data());
+    diis_finish(s, x, slot, len, dots, ee);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -601,7 +617,9 @@ static void cc_one(CCState *s, int prec) {
             diis_step(s, s->T.p, s->Tn.p, t2n, &ee);
             if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
         } else {
-            diis_step(s, s->X.p, s->Xn.p, s->xoff + t2n);
+            double ee = 0.0;
+            diis_step(s, s->X.p, s->Xn.p, s->xoff + t2n, &ee);
+            if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
         }
     } else {
         std::swap(s->T, s->Tn);
@@ -899,9 +917,13 @@ double ccsd_sweep(CCState *s, int prec) {
     // q[b,j] = sum_m t1[m,b] F~mi[m,j]: the hole-hole ladder's tau[i,m,a,b] F~mi[m,j] terms, undone
     G(s, JUES_PREC_FP64, "ccsd_q", v, o, o, 1.0, t1, plain(o), plain(1), s->Fmt.p, plain(1), plain(o), 0.0, q,
       plain(1), plain(v));
-    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p, t1, q);
+    // with DIIS the step norm comes from its error vector over [t1 | T2] (the same squared sum), so
+    // the finalisation skips it unless the per-block norms are wanted (AutoRCCSD's rms)
+    const bool norms = !s->opts.diis || s->auto_rms;
+    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, norms ? T : nullptr, s->Tn.p, t1, q);
     // t1n = R1 / D_ia and its step norm
-    const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, t1);
+    const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, norms ? t1 : nullptr);
+    if (!norms) return -1.0;
     s->r1sq = r1;
     s->r2sq = r2;
     return r2 + r1;

@@ -35,7 +35,8 @@ struct CCState {
     StackedPack stackW, stackT, stackR, stackK;
     // split precision: the two ladders as one GEMM, L = oovv + [W'^T | T] . [T ; vvvv]^T over
     // K = (m,n) then (e,f): stackLA = [W'^T | T] (rows (i,j)), stackLB = [T | vvvv] (rows (a,b),
-    // vvvv packed once); stackXW = oovv (rows (m,n), K (e,f)) for X, stackY = ovvv (CCSD's Y)
+    // vvvv packed once); stackXW = oovv (rows (m,n), K (e,f)) for X; stackY = ovvv as (a,m) x (e,f)
+    // for CCSD's Y
     StackedPack stackLA, stackLB, stackXW, stackY;
     // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
     std::vector<DBuf<double>> dv, de;

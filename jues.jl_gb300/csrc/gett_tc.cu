@@ -877,14 +877,14 @@ __global__ void __launch_bounds__(256, 6) pack_split_kernel(const double *__rest
                                                          long long R, long long K, long long Rpad,
                                                          long long Kpad, int *__restrict__ rexp,
                                                          __half *__restrict__ dst, long long Kld,
-                                                         long long pstride, double scale) {
+                                                         long long pstride, double scale, long long rexp_ld) {
     // consecutive blocks follow the source's unit-stride index, so the blocks resident at one
     // time read long contiguous runs of it
     // block counts < 2^31 (checked at launch): 32-bit index arithmetic
     const unsigned kblocks = (unsigned)((Kpad + PK - 1) / PK), rblocks = (unsigned)(Rpad / PR);
     const long long r0 = (long long)(KFAST ? blockIdx.x / kblocks : blockIdx.x % rblocks) * PR;
     const long long k0 = (long long)(KFAST ? blockIdx.x % kblocks : blockIdx.x / rblocks) * PK;
-    pack_block<NP, KFAST>(src, rmode, kmode, R, K, Kpad, r0, k0, rexp, Rpad, dst, pstride, Kld, scale);
+    pack_block<NP, KFAST>(src, rmode, kmode, R, K, Kpad, r0, k0, rexp, rexp_ld, dst, pstride, Kld, scale);
 }
 
 // Grouped form: many operands (one per problem of a batch) with one 64-wide K block each
@@ -922,17 +922,18 @@ __global__ void __launch_bounds__(256, 6) pack_grouped_kernel(const PackProb *__
 template <int NP>
 void launch_pack(Ctx *ctx, const double *src, const Mode &rm, const Mode &km, long long R, long long K,
                  long long Rpad, long long Kpad, int *ex, __half *dst, long long Kld = -1, long long pstride = -1,
-                 double scale = 1.0) {
+                 double scale = 1.0, long long rexp_ld = -1) {
     if (Kld < 0) Kld = Kpad;
     if (pstride < 0) pstride = Rpad * Kpad;
+    if (rexp_ld < 0) rexp_ld = Rpad;
     const long long blocks = (Rpad / PR) * ((Kpad + PK - 1) / PK);
     JUES_REQUIRE(blocks < (1LL << 31), "operand too large to pack in one launch");
     if (km.s0 == 1 && km.d0 > 1)
         pack_split_kernel<NP, true><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex, dst,
-                                                                               Kld, pstride, scale);
+                                                                               Kld, pstride, scale, rexp_ld);
     else
         pack_split_kernel<NP, false><<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rm, km, R, K, Rpad, Kpad, ex,
-                                                                                dst, Kld, pstride, scale);
+                                                                                dst, Kld, pstride, scale, rexp_ld);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 

@@ -21,6 +21,12 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// up to 16 vectors and coefficients as one kernel argument
+struct VecList {
+    const double *p[16];
+    double c[16];
+};
+
 // warp-wide sum, valid in every lane
 __device__ __forceinline__ double warp_allsum(double v) {
 #pragma unroll
@@ -282,6 +288,7 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
                                                                const double *__restrict__ t1,
                                                                const double *__restrict__ q) {
     extern __shared__ double zs[];   // [2][o][pitch]: zs[0] = Z_ab, zs[1] = Z_ba, element (i, j) at j + pitch i
+    // RANK1: then t1[:,a], t1[:,b], q[a,:], q[b,:] (o each)
     const int pitch = o | 1;
     const long long oo = (long long)o * o;
     const int ooi = o * o;
@@ -289,6 +296,13 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
     int a, b;
     pair_ab(blockIdx.x, a, b);   // one (a <= b) pair per block: resident blocks overlap their phases
     const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
+    double *r1v = zs + 2 * o * pitch;
+    if (RANK1)
+        for (int k = threadIdx.x; k < 4 * o; k += blockDim.x) {
+            const int w = k / o, i = k % o;
+            r1v[k] = w == 0 ? t1[i + (long long)o * a] : w == 1 ? t1[i + (long long)o * b]
+                   : w == 2 ? q[a + (long long)v * i] : q[b + (long long)v * i];
+        }
     {
         for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
             const int i = ij % o, j = ij / o;
@@ -302,14 +316,15 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             const double zab = zs[j + pitch * i], zba_t = zs[o * pitch + i + pitch * j];
             const double inv = invD[ab + ij];   // D is symmetric in (a, b)
             double x = L[ab + ij] + zab + zba_t;
-            if (RANK1) x += rank1_pair(t1, q, o, v, i, j, a, b);
+            // C[i,j,a,b] + C[j,i,b,a] = t1[i,a] q[b,j] + t1[j,b] q[a,i]
+            if (RANK1) x += r1v[i] * r1v[3 * o + j] + r1v[o + j] * r1v[2 * o + i];
             x *= inv;
             Tn[ab + ij] = x;
             if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
             if (a != b) {
                 const double zba = zs[o * pitch + j + pitch * i], zab_t = zs[i + pitch * j];
                 double y = L[ba + ij] + zba + zab_t;
-                if (RANK1) y += rank1_pair(t1, q, o, v, i, j, b, a);
+                if (RANK1) y += r1v[o + i] * r1v[2 * o + j] + r1v[j] * r1v[3 * o + i];
                 y *= inv;
                 Tn[ba + ij] = y;
                 if (Told) { const double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
@@ -319,6 +334,7 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
     acc = block_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
+
 
 // T~[i,j,a,b] = 2 T[i,j,a,b] - T[j,i,a,b], one (a,b) block per iteration with its transpose
 // through shared memory (odd row pitch), every global access unit-stride
@@ -361,10 +377,6 @@ __global__ void t_tilde_kernel(const double *__restrict__ T, int o, int v, doubl
     }
 }
 
-struct VecList {
-    const double *p[16];
-    double c[16];
-};
 
 // out = sum_k c_k p_k with the vector count a template parameter, so every load of an element is
 // in flight at once; pairs of elements as 16-byte loads and stores (the vectors are 16-byte
@@ -453,21 +465,24 @@ __global__ void wp_fmi_kernel(double *__restrict__ Wp, const double *__restrict_
 
 // Fmi[m,i] = sum_n 2 X[m,n,i,n] - X[m,n,n,i] with X = W' - oooo, W'[(m,n),(i,j)] = oooo + sum_ef
 // oovv[m,n,e,f] T[i,j,e,f]: the Fmi contraction of RCCD.jl:216 (sum_nef oovv[m,n,e,f] T~[i,n,e,f])
-// read off the hole-hole intermediate instead of a GEMM of its own.  One thread per (m, i).
+// read off the hole-hole intermediate instead of a GEMM of its own.  One warp per (m, i), its
+// lanes over n.
 __global__ void fmi_from_x_kernel(const double *__restrict__ Wp, const double *__restrict__ oooo, int o,
                                   double *__restrict__ Fmi) {
     const long long oo = (long long)o * o;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (t >= oo) return;
-    const int m = t % o, i = t / o;
+    const int m = (int)(t % o), i = (int)(t / o);
     double acc = 0.0;
-    for (int n = 0; n < o; ++n) {
+    for (int n = lane; n < o; n += 32) {
         const long long mn = m + (long long)o * n;
         const long long d = mn + oo * (i + (long long)o * n), x = mn + oo * (n + (long long)o * i);
         acc = fma(2.0, Wp[d] - oooo[d], acc);
         acc -= Wp[x] - oooo[x];
     }
-    Fmi[t] = acc;
+    acc = warp_allsum(acc);
+    if (lane == 0) Fmi[t] = acc;
 }
 
 // Fae from the ring intermediates and the Fae term folded into W12.  With t = WJ - J0 and
@@ -499,28 +514,17 @@ __global__ void fae_trace_kernel(const double *__restrict__ WJ, const double *__
 }
 
 // CCSD sweep inputs from T2 and t1 in one pass: Ttau = T2 + tau and U = T2 + 2 tau with
-// tau[i,j,a,b] = t1[i,a] t1[j,b].  One (a,b) block of o x o per iteration, the two t1 columns
-// in shared memory (2 o doubles, dynamic).
+// tau[i,j,a,b] = t1[i,a] t1[j,b]; an elementwise grid-stride pass (32-bit indices, t1 from L1).
 __global__ void __launch_bounds__(256) ccsd_tau_kernel(const double *__restrict__ T, const double *__restrict__ t1,
-                                                       int o, int v, double *__restrict__ Ttau,
+                                                       unsigned o, unsigned v, unsigned n, double *__restrict__ Ttau,
                                                        double *__restrict__ U) {
-    extern __shared__ double cab[];
-    double *ca = cab, *cb = cab + o;
-    const long long oo = (long long)o * o, vv = (long long)v * v;
-    const int ooi = o * o;
-    for (long long ab = blockIdx.x; ab < vv; ab += gridDim.x) {
-        const int a = (int)(ab % v), b = (int)(ab / v);
-        __syncthreads();
-        for (int k = threadIdx.x; k < 2 * o; k += blockDim.x)
-            cab[k] = k < o ? t1[k + (long long)o * a] : t1[k - o + (long long)o * b];
-        __syncthreads();
-        const long long base = oo * ab;
-        for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
-            const int i = ij % o, j = ij / o;
-            const double t = T[base + ij], tau = ca[i] * cb[j];
-            Ttau[base + ij] = t + tau;
-            U[base + ij] = fma(2.0, tau, t);
-        }
+    const unsigned oo = o * o;
+    for (unsigned x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        const unsigned ij = x % oo, ab = x / oo;
+        const unsigned i = ij % o, j = ij / o, a = ab % v, b = ab / v;
+        const double t = T[x], tau = __ldg(t1 + i + o * a) * __ldg(t1 + j + o * b);
+        Ttau[x] = t + tau;
+        U[x] = fma(2.0, tau, t);
     }
 }
 
@@ -844,7 +848,7 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
         Ctx::Scope s(ctx, "t2_finalize");
         // one block per pair; the step norm's partials (one per block) must fit the reduction scratch
         if (o <= 64 && npair <= 65536 - 64) {
-            const size_t smem = (size_t)2 * o * (o | 1) * sizeof(double);
+            const size_t smem = ((size_t)2 * o * (o | 1) + (t1 ? 4 * o : 0)) * sizeof(double);
             // the rank-one term is a template parameter: without it the kernel fits 32 registers
             // and eight blocks per SM
             static std::atomic<unsigned long long> attr_set{0};
@@ -853,7 +857,8 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
                 JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
                 JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (2 * 64 * 65 + 4 * 64) * 8));
                 attr_set.fetch_or(bit);
             }
             nb = (int)npair;
@@ -870,6 +875,7 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
     }
     return Told ? finish_reduce(ctx, nb) : 0.0;
 }
+
 
 double t1_finalize(Ctx *ctx, double *t1n, const double *eps, int o, int v, const double *t1old) {
     {
@@ -944,7 +950,7 @@ void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o) {
 void fmi_from_x(Ctx *ctx, const double *Wp, const double *oooo, int o, double *Fmi) {
     Ctx::Scope s(ctx, "fmi_trace");
     const long long n = (long long)o * o;
-    fmi_from_x_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(Wp, oooo, o, Fmi);
+    fmi_from_x_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(Wp, oooo, o, Fmi);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -958,11 +964,10 @@ void fae_from_rings(Ctx *ctx, const double *WJ, const double *J0, const double *
 }
 
 void ccsd_tau(Ctx *ctx, const double *T, const double *t1, int o, int v, double *Ttau, double *U) {
-    JUES_REQUIRE(o <= 2048, "ccsd_tau: nocc <= 2048");
+    const long long n = (long long)o * o * v * v;
+    JUES_REQUIRE(n < (1LL << 31), "ccsd_tau: o^2 v^2 must be below 2^31");
     Ctx::Scope s(ctx, "ccsd_tau");
-    const long long vv = (long long)v * v;
-    ccsd_tau_kernel<<<(unsigned)std::min<long long>(vv, 152LL * 8), 256, 2 * o * sizeof(double), ctx->stream>>>(
-        T, t1, o, v, Ttau, U);
+    ccsd_tau_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(T, t1, (unsigned)o, (unsigned)v, (unsigned)n, Ttau, U);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
