@@ -419,8 +419,12 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         Perm4 p{{o, o, o, v}, {o, 1, oo, oo * o}, {1, o, oo, oo * o}};
         permute4(ctx, p, 1.0, s->ooov.p, 0.0, sw.p);
         axpby(ctx, n3, 2.0, s->ooov.p, -1.0, sw.p, s->ooovT.p);
-        s->c12 = DBuf<double>(ctx, (size_t)(2 * ov));
+        s->c12 = DBuf<double>(ctx, (size_t)(3 * ov));
         ooov_diag_sums(ctx, s->ooov.p, o, v, s->c12.p);
+        // box (i, j, a, m): ooov[m,i,j,a] at m + o i + oo j + ooo a; ooovQ[i,j,a,m] at i + o j + oo a + oov m
+        s->ooovQ = DBuf<double>(ctx, n3);
+        Perm4 q{{o, o, v, o}, {o, oo, oo * o, 1}, {1, o, oo, oo * v}};
+        permute4(ctx, q, 1.0, s->ooov.p, 0.0, s->ooovQ.p);
     }
     s->invD = DBuf<double>(ctx, t2n);
     inv_denominators(ctx, s->eps.p, o, v, s->invD.p);
@@ -848,11 +852,11 @@ double ccsd_sweep(CCState *s, int prec) {
             s->stackY.ensure(ctx, ov, kv, 2);
             pack_stacked(ctx, s->stackY, 0, ovvv, mode2(v, o, 1), mode2(v, ovv, ov), ov, vv, 1.0);
         }
-        gett_tc_views(ctx, s->stackLA.view(ko, kv), s->stackY.view(0, kv), oo, ov, 1.0, 0.0, Y, plain(1), plain(oo),
-                      nullptr, "ccsd_y");
+        gett_tc_views(ctx, s->stackLA.view(ko, kv), s->stackY.view(0, kv), oo, ov, 1.0, 1.0, Y, plain(1), plain(oo),
+                      s->ooovQ.p, "ccsd_y");
     } else {
         G(s, prec, "ccsd_y", oo, ov, vv, 1.0, Ttau, plain(1), plain(oo), ovvv, mode2(v, ovv, ov), mode2(v, o, 1),
-          0.0, Y, plain(1), plain(oo), nullptr, true, true);
+          1.0, Y, plain(1), plain(oo), s->ooovQ.p, true, true);
     }
 
     // T1 (RCCSD.jl:248-259) into t1n
@@ -873,24 +877,19 @@ double ccsd_sweep(CCState *s, int prec) {
     // - sum_mne T2[m,n,a,e] (2 <mn|ie> - <nm|ie>)
     G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, s->ooovT.p, plain(oo), mode2(oo, 1, ooo), T,
       mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o), nullptr, true, false);
-    // the <ma|fe> terms from Y
-    t1_ytrace(ctx, Y, t1, G2, H1, (int)o, (int)v, R1);
+    // the <ma|fe> terms from Y (its ooov seed's traces, c2 and c3, taken off)
+    t1_ytrace(ctx, Y, t1, G2, H1, s->c12.p, (int)o, (int)v, R1);
 
     // Z's t1 terms with t1 on b, by their (i,a)<->(j,b) images all of the form
     // -sum_m Q[i,j,a,m] t1[m,b], with Q (in place of Y, layout [(i,j),(a,m)]) =
     //   Y[i,j,a,m]                                 (Wabef's t1 parts)
+    // + <mi|ja> = ooov[m,i,j,a]                            (- t1[m,a] <mb|ij>, imaged; Y's seed)
     // + Y1[j,m,i,a], Y1[i,m,j,b] = sum_e t1[i,e] <mj|eb>   (- tau[i,m,e,a] <mb|ej>, imaged)
     // + Y2[i,m,a,j], Y2[i,m,a,j] = sum_e t1[i,e] <ma|je>   (- tau[i,m,e,b] <am|ej>)
-    // + <mi|ja> = ooov[m,i,j,a]                            (- t1[m,a] <mb|ij>, imaged)
     G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), W, plain(oo), mode3(o, o, 1, o, oov), 1.0, Y,
       plain(o), mode3(o, o, oov, 1, oo), nullptr, false, true);
     G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov), plain(1), 1.0, Y, plain(1),
       mode3(o, v, oov, oo, o), nullptr, false, true);
-    {
-        // box (i, j, a, m): ooov[m,i,j,a] at m + o i + oo j + ooo a; Q[i,j,a,m] at i + o j + oo a + oov m
-        Perm4 p{{o, o, v, o}, {o, oo, ooo, 1}, {1, o, oo, oov}};
-        permute4(ctx, p, 1.0, ooov, 1.0, Y);
-    }
 
     // Z (RCCSD.jl:264-284, one member of each (i,a)<->(j,b) pair)
     double *Z = s->Z.p;

@@ -17,7 +17,8 @@ struct CCState {
     DBuf<double> invD;           // 1 / D[i,j,a,b], formed once
     DBuf<double> oovvT;          // 2 oovv[i,j,a,b] - oovv[j,i,a,b], formed once (CCD energy weights,
                                  // ring and Fme weights)
-    DBuf<double> ooovT, c12;     // CCSD: 2 ooov[m,n,i,e] - ooov[n,m,i,e]; the ooov diagonal sums c1, c2
+    DBuf<double> ooovT, c12;     // CCSD: 2 ooov[m,n,i,e] - ooov[n,m,i,e]; the ooov diagonal sums c1, c2, c3
+    DBuf<double> ooovQ;          // CCSD: ooov[m,i,j,a] at [(i,j),(a,m)], the seed of Y
     DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;

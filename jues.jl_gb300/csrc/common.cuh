@@ -310,10 +310,12 @@ void ring_traces(Ctx *ctx, const double *WJ, const double *J0, const double *WK,
 void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, const double *tGJ,
               const double *tGK, const double *t1, const double *c12, const double *Fme, const double *fOV,
               const double *fVV, int o, int v, bool mvariant, double *Fae, double *H1, double *G2, double *W12);
-// R1 += T1's <ma|fe> terms from the traces of Y[(i,j),(a,m)]
-void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, int o, int v,
-               double *R1);
-// c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e] into c12[0..ov), c12[ov..2ov)
+// R1 += T1's <ma|fe> terms from the traces of Y[(i,j),(a,m)], which carries the ooov seed
+// ooov[m,i,j,a] (its traces c2, c3 from c123 are taken off)
+void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, const double *c123,
+               int o, int v, double *R1);
+// c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e], c3[n,e] = sum_m ooov[m,m,n,e] into
+// c12[0..ov), [ov..2ov), [2ov..3ov)
 void ooov_diag_sums(Ctx *ctx, const double *ooov, int o, int v, double *c12);
 // DIIS bookkeeping in one pass: v_out = xn, e_out = xn - x, dots[0] = e.e, dots[1 + k] = olds[k].e
 void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,

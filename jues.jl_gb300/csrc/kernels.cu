@@ -619,8 +619,8 @@ __global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__r
 //   R1[i,a] += 2 (sum_m Y[(i,m),(a,m)] - sum_e t1[i,e] G2[a,e]) - (sum_m Y[(m,i),(a,m)] - sum_f t1[i,f] H1[a,f])
 // (the tau parts of Ttau removed through G2 and H1).  One thread per (i, a).
 __global__ void t1_ytrace_kernel(const double *__restrict__ Y, const double *__restrict__ t1,
-                                 const double *__restrict__ G2, const double *__restrict__ H1, int o, int v,
-                                 double *__restrict__ R1) {
+                                 const double *__restrict__ G2, const double *__restrict__ H1,
+                                 const double *__restrict__ c123, int o, int v, double *__restrict__ R1) {
     const long long oo = (long long)o * o;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)o * v) return;
@@ -631,6 +631,10 @@ __global__ void t1_ytrace_kernel(const double *__restrict__ Y, const double *__r
         y1 += Y[i + (long long)o * m + col];
         y2 += Y[m + (long long)o * i + col];
     }
+    // Y carries its ooov seed Q0[i,j,a,m] = ooov[m,i,j,a], whose traces are c2[i,a] and c3[i,a]
+    const long long ov = (long long)o * v;
+    y1 -= c123[ov + t];
+    y2 -= c123[2 * ov + t];
     double g = 0.0, h = 0.0;
     for (int e = 0; e < v; ++e) {
         const double te = t1[i + (long long)o * e];
@@ -640,19 +644,22 @@ __global__ void t1_ytrace_kernel(const double *__restrict__ Y, const double *__r
     R1[t] += 2.0 * (y1 - g) - (y2 - h);
 }
 
-// c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e] (ooov column-major o x o x o x v)
+// c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e], c3[n,e] = sum_m ooov[m,m,n,e]
+// (ooov column-major o x o x o x v)
 __global__ void ooov_diag_sums_kernel(const double *__restrict__ ooov, int o, int v, double *__restrict__ c12) {
     const long long oo = (long long)o * o, ooo = oo * o, ov = (long long)o * v;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= ov) return;
     const int n = (int)(t % o), e = (int)(t / o);
-    double s1 = 0.0, s2 = 0.0;
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
     for (int m = 0; m < o; ++m) {
         s1 += ooov[n + (long long)o * m + oo * m + ooo * e];
         s2 += ooov[m + (long long)o * n + oo * m + ooo * e];
+        s3 += ooov[m + (long long)o * m + oo * n + ooo * e];
     }
     c12[t] = s1;
     c12[ov + t] = s2;
+    c12[2 * ov + t] = s3;
 }
 
 __global__ void t1_finalize_kernel(double *__restrict__ t1n, const double *__restrict__ eps, int o, int v,
@@ -990,11 +997,11 @@ void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, co
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
-void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, int o, int v,
-               double *R1) {
+void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, const double *c123,
+               int o, int v, double *R1) {
     Ctx::Scope s(ctx, "ccsd_t1");
     const long long n = (long long)o * v;
-    t1_ytrace_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(Y, t1, G2, H1, o, v, R1);
+    t1_ytrace_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(Y, t1, G2, H1, c123, o, v, R1);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 

@@ -162,17 +162,20 @@ def ccsd_device_form(blocks, t1, T, variant="jl", fock=None):
     Fae = Ft + 0.5 * E("ma,me->ae", t1, Fme)
     for j in range(o):
         W12[j, :, :, j] += Ft
-    Y = E("ijef,mafe->ijam", Ttau, ovvv)                                # ccsd_y
+    # ccsd_y, seeded with ooov[m,i,j,a] at [(i,j),(a,m)]
+    Y = E("ijef,mafe->ijam", Ttau, ovvv) + ooov.transpose(1, 2, 3, 0)
+    c2 = np.einsum("mima->ia", ooov)                                    # the seed's two traces
+    c3 = np.einsum("mmia->ia", ooov)
     R1 = (E("ie,ae->ia", t1, Fae) - E("ma,mi->ia", t1, Fmi)
           + 2 * E("me,imae->ia", Fme, T) - E("me,miae->ia", Fme, T)
           + 2 * E("me,imae->ia", t1, oovv) - E("me,maie->ia", t1, ovov)
           - E("mnae,mnie->ia", T, ooovT))
-    R1 += (2 * (np.einsum("imam->ia", Y) - E("ie,ae->ia", t1, G2))
-           - (np.einsum("miam->ia", Y) - E("if,af->ia", t1, H1)))        # t1_ytrace
-    # Q[i,j,a,m] = Y + Y1[j,m,i,a] + Y2[i,m,a,j] + ooov[m,i,j,a] (the t1-on-b terms, imaged)
+    R1 += (2 * (np.einsum("imam->ia", Y) - c2 - E("ie,ae->ia", t1, G2))
+           - (np.einsum("miam->ia", Y) - c3 - E("if,af->ia", t1, H1)))   # t1_ytrace
+    # Q[i,j,a,m] = Y (with its ooov seed) + Y1[j,m,i,a] + Y2[i,m,a,j] (the t1-on-b terms, imaged)
     Y1 = E("ie,mjeb->imjb", t1, oovv)
     Y2 = E("ie,maje->imaj", t1, ovov)
-    Q = Y + Y1.transpose(2, 0, 3, 1) + Y2.transpose(0, 3, 2, 1) + ooov.transpose(1, 2, 3, 0)
+    Q = Y + Y1.transpose(2, 0, 3, 1) + Y2.transpose(0, 3, 2, 1)
     Z = (E("imae,mbej->ijab", T, W12) - E("miae,mbej->ijab", T, WJ) + E("mibe,maej->ijab", T, WK)
          - E("ijam,mb->ijab", Q, t1) + E("ie,jabe->ijab", t1, ovvv))
     if fock is not None:
