@@ -122,42 +122,49 @@ static void ring_stacks_begin(CCState *s, const double *U) {
     if (!s->stackW.buf.p) {
         s->stackW.ensure(ctx, ov, 3 * kb, 2);
         const double *wt = (s->reference_df_wmbej ? s->oovv.p : s->oovvT.p);
-        // CCD [-1/2 oovv | 1/2 oovvT | 1/2 oovv'], CCSD [1/2 oovvT | -1/2 oovv | 1/2 oovv']:
-        // rows (m,e), K (n,f)
-        pack_stacked(ctx, s->stackW, ccsd ? kb : 0, s->oovv.p, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, -0.5);
-        pack_stacked(ctx, s->stackW, ccsd ? 0 : kb, wt, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, 0.5);
+        // [-1/2 oovv | 1/2 oovvT | 1/2 oovv']: rows (m,e), K (n,f)
+        pack_stacked(ctx, s->stackW, 0, s->oovv.p, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, -0.5);
+        pack_stacked(ctx, s->stackW, kb, wt, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, 0.5);
         pack_stacked(ctx, s->stackW, 2 * kb, s->oovv.p, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 0.5);
     }
-    s->stackT.ensure(ctx, ov, (ccsd ? 3 : 2) * kb, 2);
-    pack_stacked(ctx, s->stackT, 0, s->T.p, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 1.0);    // R23
+    // CCD [R23 | R1]; CCSD [U23 | R1 | R23 | t1] (t1 as one column of a 128-wide block)
+    s->stackT.ensure(ctx, ov, ccsd ? 3 * kb + 128 : 2 * kb, 2);
+    pack_stacked(ctx, s->stackT, 0, U, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 1.0);        // U23 (CCD: R23)
     pack_stacked(ctx, s->stackT, kb, s->T.p, mode2(o, 1, oo), mode2(o, o, oov), ov, ov, 1.0);   // R1
-    if (ccsd) pack_stacked(ctx, s->stackT, 2 * kb, U, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 1.0);
+    if (ccsd) {
+        pack_stacked(ctx, s->stackT, 2 * kb, s->T.p, mode2(o, o, oo), mode2(o, 1, oov), ov, ov, 1.0);   // R23
+        pack_stacked(ctx, s->stackT, 3 * kb, s->t1.p, plain(1), plain(1), ov, 1, 1.0);                  // t1
+    }
     const Mode jb = mode2(o, ov * v, ov);
     d2d(ctx, s->WJ.p, s->ovvoJ.p, (size_t)(ov * ov));
     d2d(ctx, s->WK.p, s->ovovK.p, (size_t)(ov * ov));
-    // CCD: [R23 | R1] against [-1/2 oovv | 1/2 oovvT]; CCSD: [R1 | U23] against [1/2 oovvT | -1/2 oovv]
-    gett_tc_views(ctx, s->stackW.view(0, 2 * kb), s->stackT.view(ccsd ? kb : 0, 2 * kb), ov, ov, 1.0, 1.0, s->WJ.p,
-                  plain(1), jb, nullptr, ccsd ? "ccsd_wj" : "ccd_wj");
-    gett_tc_views(ctx, s->stackW.view(2 * kb, kb), s->stackT.view(ccsd ? 2 * kb : 0, kb), ov, ov, 1.0, 1.0, s->WK.p,
-                  plain(1), jb, nullptr, ccsd ? "ccsd_wk" : "ccd_wk");
+    // [U23 | R1] against [-1/2 oovv | 1/2 oovvT]; U23 against 1/2 oovv[n,m,e,f]
+    gett_tc_views(ctx, s->stackW.view(0, 2 * kb), s->stackT.view(0, 2 * kb), ov, ov, 1.0, 1.0, s->WJ.p, plain(1), jb,
+                  nullptr, ccsd ? "ccsd_wj" : "ccd_wj");
+    gett_tc_views(ctx, s->stackW.view(2 * kb, kb), s->stackT.view(0, kb), ov, ov, 1.0, 1.0, s->WK.p, plain(1), jb,
+                  nullptr, ccsd ? "ccsd_wk" : "ccd_wk");
 }
 
-// Z = [R23 | R1] . [-WJ ; W12] (beta 0), then Z += R23 . WK
-static void ring_stacks_z(CCState *s) {
+// Z = [R23 | R1] . [-WJ ; W12] (beta 0), then Z += R23 . WK.  CCSD also carries the rank-one
+// t1[i,a] q[b,j] (the hole-hole ladder's tau F~mi terms, undone) as a third K block:
+// Z = [R1 | R23 | t1] . [W12 ; -WJ ; q].
+static void ring_stacks_z(CCState *s, const double *q) {
     Ctx *ctx = s->ctx;
     const long long o = s->o, v = s->v, oo = o * o, ov = o * v, oov = oo * v;
     const long long kb = (ov + 127) / 128 * 128;
     const bool ccsd = s->method == 1;
-    s->stackR.ensure(ctx, ov, 2 * kb, 2);
-    pack_stacked(ctx, s->stackR, 0, s->WJ.p, plain(ov), plain(1), ov, ov, -1.0);
-    pack_stacked(ctx, s->stackR, kb, s->W12.p, plain(ov), plain(1), ov, ov, 1.0);
+    s->stackR.ensure(ctx, ov, ccsd ? 2 * kb + 128 : 2 * kb, 2);
+    pack_stacked(ctx, s->stackR, ccsd ? kb : 0, s->WJ.p, plain(ov), plain(1), ov, ov, -1.0);
+    pack_stacked(ctx, s->stackR, ccsd ? 0 : kb, s->W12.p, plain(ov), plain(1), ov, ov, 1.0);
+    if (ccsd) pack_stacked(ctx, s->stackR, 2 * kb, q, plain(1), plain(1), ov, 1, 1.0);
     s->stackK.ensure(ctx, ov, kb, 2);
     pack_stacked(ctx, s->stackK, 0, s->WK.p, plain(ov), plain(1), ov, ov, 1.0);
     const char *name = ccsd ? "ccsd_ring" : "ccd_ring";
-    gett_tc_views(ctx, s->stackT.view(0, 2 * kb), s->stackR.view(0, 2 * kb), ov, ov, 1.0, 0.0, s->Z.p,
+    const long long kz = ccsd ? 2 * kb + 128 : 2 * kb;
+    gett_tc_views(ctx, s->stackT.view(ccsd ? kb : 0, kz), s->stackR.view(0, kz), ov, ov, 1.0, 0.0, s->Z.p,
                   mode2(o, 1, oo), mode2(v, oov, o), nullptr, name);
-    gett_tc_views(ctx, s->stackT.view(0, kb), s->stackK.view(0, kb), ov, ov, 1.0, 1.0, s->Z.p, mode2(o, 1, oov),
-                  mode2(v, oo, o), nullptr, name);
+    gett_tc_views(ctx, s->stackT.view(ccsd ? 2 * kb : 0, kb), s->stackK.view(0, kb), ov, ov, 1.0, 1.0, s->Z.p,
+                  mode2(o, 1, oov), mode2(v, oo, o), nullptr, name);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -232,7 +239,7 @@ double ccd_sweep(CCState *s, int prec) {
     // Z: the terms of RCCD.jl:243-254 whose (i,a)<->(j,b) images are added by t2_finalize
     double *Z = s->Z.p;
     if (stacked) {
-        ring_stacks_z(s);
+        ring_stacks_z(s, nullptr);
     } else {
         // + T[i,m,a,e] (2WmBeJ + WmBEj + [m = j] Fae)[m,b,e,j]
         G(s, prec, "ccd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
@@ -891,12 +898,18 @@ double ccsd_sweep(CCState *s, int prec) {
     G(s, prec, "ccsd_z_tau", o, oov, v, 1.0, t1, plain(1), plain(o), ovov, plain(oov), plain(1), 1.0, Y, plain(1),
       mode3(o, v, oov, oo, o), nullptr, false, true);
 
+    // q[b,j] = sum_m t1[m,b] F~mi[m,j]: the hole-hole ladder's tau[i,m,a,b] F~mi[m,j] terms, undone by
+    // the rank-one t1[i,a] q[b,j] (and its image): a K block of the stacked ring GEMM, or a term of
+    // the finalisation
+    G(s, JUES_PREC_FP64, "ccsd_q", v, o, o, 1.0, t1, plain(o), plain(1), s->Fmt.p, plain(1), plain(o), 0.0, q,
+      plain(1), plain(v));
+
     // Z (RCCSD.jl:264-284, one member of each (i,a)<->(j,b) pair)
     double *Z = s->Z.p;
     // + T2[i,m,a,e] (2 WmBeJ + WmBEj + [m = j] F~ae)[m,b,e,j] - T2[m,i,a,e] WmBeJ[m,b,e,j]
     // + T2[m,i,b,e] WmBEj[m,a,e,j]
     if (stacked) {
-        ring_stacks_z(s);
+        ring_stacks_z(s, q);
     } else {
         G(s, prec, "ccsd_ring", ov, ov, ov, 1.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->W12.p, plain(1),
           plain(ov), 0.0, Z, mode2(o, 1, oo), mode2(v, oov, o), nullptr, true, false);
@@ -913,13 +926,11 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(1), plain(o), nullptr, false, true);
 
     if (s->fock) axpby(ctx, (size_t)ov, 1.0, s->fOV.p, 1.0, R1, R1);   // + f_ia
-    // q[b,j] = sum_m t1[m,b] F~mi[m,j]: the hole-hole ladder's tau[i,m,a,b] F~mi[m,j] terms, undone
-    G(s, JUES_PREC_FP64, "ccsd_q", v, o, o, 1.0, t1, plain(o), plain(1), s->Fmt.p, plain(1), plain(o), 0.0, q,
-      plain(1), plain(v));
     // with DIIS the step norm comes from its error vector over [t1 | T2] (the same squared sum), so
     // the finalisation skips it unless the per-block norms are wanted (AutoRCCSD's rms)
     const bool norms = !s->opts.diis || s->auto_rms;
-    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, norms ? T : nullptr, s->Tn.p, t1, q);
+    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, norms ? T : nullptr, s->Tn.p,
+                            stacked ? nullptr : t1, stacked ? nullptr : q);
     // t1n = R1 / D_ia and its step norm
     const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, norms ? t1 : nullptr);
     if (!norms) return -1.0;
