@@ -432,6 +432,12 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         s->ooovQ = DBuf<double>(ctx, n3);
         Perm4 q{{o, o, v, o}, {o, oo, oo * o, 1}, {1, o, oo, oo * v}};
         permute4(ctx, q, 1.0, s->ooov.p, 0.0, s->ooovQ.p);
+        // M1[(i,a),(m,e)] = 2 oovv[i,m,a,e] - ovov[m,a,i,e], box (i, a, m, e)
+        s->M1 = DBuf<double>(ctx, (size_t)(ov * ov));
+        Perm4 p1{{o, v, o, v}, {1, oo, o, oo * v}, {1, o, ov, ov * o}};
+        permute4(ctx, p1, 2.0, s->oovv.p, 0.0, s->M1.p);
+        Perm4 p2{{o, v, o, v}, {ov, o, 1, ov * o}, {1, o, ov, ov * o}};
+        permute4(ctx, p2, -1.0, s->ovov.p, 1.0, s->M1.p);
     }
     s->invD = DBuf<double>(ctx, t2n);
     inv_denominators(ctx, s->eps.p, o, v, s->invD.p);
@@ -872,15 +878,11 @@ double ccsd_sweep(CCState *s, int prec) {
       0.0, R1, plain(1), plain(o));
     G(s, prec, "ccsd_t1", o, v, o, -1.0, s->Fmi.p, plain(o), plain(1), t1, plain(1), plain(o),
       1.0, R1, plain(1), plain(o));
-    // Fme[m,e] (2 T2[i,m,a,e] - T2[m,i,a,e])
-    G(s, prec, "ccsd_t1", ov, 1, ov, 2.0, T, mode2(o, 1, oo), mode2(o, o, oov), s->Fme.p,
-      plain(1), plain(0), 1.0, R1, plain(1), plain(0));
-    G(s, prec, "ccsd_t1", ov, 1, ov, -1.0, T, mode2(o, o, oo), mode2(o, 1, oov), s->Fme.p,
-      plain(1), plain(0), 1.0, R1, plain(1), plain(0));
-    G(s, prec, "ccsd_t1", ov, 1, ov, 2.0, W, mode2(o, 1, oo), mode2(o, o, oov), t1, plain(1),
-      plain(0), 1.0, R1, plain(1), plain(0), nullptr, true, false);
-    G(s, prec, "ccsd_t1", ov, 1, ov, -1.0, ovov, mode2(o, ov, o), mode2(o, 1, oov), t1,
-      plain(1), plain(0), 1.0, R1, plain(1), plain(0), nullptr, true, false);
+    // Fme[m,e] (2 T2[i,m,a,e] - T2[m,i,a,e]), one read of T2
+    t1_fme(ctx, T, s->Fme.p, (int)o, (int)v, R1);
+    // t1[m,e] (2 <im|ae> - <ma|ie>) through M1, formed once
+    G(s, prec, "ccsd_t1", ov, 1, ov, 1.0, s->M1.p, plain(1), plain(ov), t1, plain(1), plain(0), 1.0, R1, plain(1),
+      plain(0), nullptr, true, false);
     // - sum_mne T2[m,n,a,e] (2 <mn|ie> - <nm|ie>)
     G(s, prec, "ccsd_t1_ooov", o, v, oov, -1.0, s->ooovT.p, plain(oo), mode2(oo, 1, ooo), T,
       mode2(oo, 1, oov), plain(oo), 1.0, R1, plain(1), plain(o), nullptr, true, false);

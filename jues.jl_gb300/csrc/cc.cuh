@@ -19,6 +19,7 @@ struct CCState {
                                  // ring and Fme weights)
     DBuf<double> ooovT, c12;     // CCSD: 2 ooov[m,n,i,e] - ooov[n,m,i,e]; the ooov diagonal sums c1, c2, c3
     DBuf<double> ooovQ;          // CCSD: ooov[m,i,j,a] at [(i,j),(a,m)], the seed of Y
+    DBuf<double> M1;             // CCSD: 2 oovv[i,m,a,e] - ovov[m,a,i,e] at [(i,a),(m,e)] (T1's t1 terms)
     DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;

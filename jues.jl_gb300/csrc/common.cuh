@@ -314,6 +314,8 @@ void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, co
 // ooov[m,i,j,a] (its traces c2, c3 from c123 are taken off)
 void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, const double *H1, const double *c123,
                int o, int v, double *R1);
+// R1[i,a] += sum_{m,e} (2 T2[i,m,a,e] - T2[m,i,a,e]) Fme[m,e] (one read of T2; o <= 64)
+void t1_fme(Ctx *ctx, const double *T, const double *Fme, int o, int v, double *R1);
 // c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e], c3[n,e] = sum_m ooov[m,m,n,e] into
 // c12[0..ov), [ov..2ov), [2ov..3ov)
 void ooov_diag_sums(Ctx *ctx, const double *ooov, int o, int v, double *c12);

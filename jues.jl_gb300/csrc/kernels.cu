@@ -644,6 +644,45 @@ __global__ void t1_ytrace_kernel(const double *__restrict__ Y, const double *__r
     R1[t] += 2.0 * (y1 - g) - (y2 - h);
 }
 
+// T1's Fme term, R1[i,a] += sum_{m,e} (2 T2[i,m,a,e] - T2[m,i,a,e]) Fme[m,e], in one read of T2: block
+// (a, chunk) takes the o x o blocks T2[:,:,a,e] of its e range through shared memory (odd pitch for
+// the transposed reads) and writes its per-i sums to part[chunk][i + o a]; o <= 64.
+constexpr int T1FME_CHUNK = 8;
+__global__ void __launch_bounds__(256) t1_fme_kernel(const double *__restrict__ T, const double *__restrict__ Fme,
+                                                     int o, int v, double *__restrict__ part) {
+    extern __shared__ double tile[];   // [o][pitch], element (i, m) of the block at i + pitch m
+    const int pitch = o | 1, ooi = o * o;
+    const int a = blockIdx.x, chunk = blockIdx.y;
+    const long long oo = (long long)o * o;
+    // thread (i, g): row i, quarter g of the m range (o <= 64: four groups of 64 threads)
+    const int i = threadIdx.x & 63, g = threadIdx.x >> 6;
+    double acc = 0.0;
+    const int e0 = chunk * T1FME_CHUNK, e1 = min(v, e0 + T1FME_CHUNK);
+    for (int e = e0; e < e1; ++e) {
+        const double *blk = T + oo * (a + (long long)v * e);
+        __syncthreads();
+        for (int im = threadIdx.x; im < ooi; im += blockDim.x) tile[(im % o) + pitch * (im / o)] = blk[im];
+        __syncthreads();
+        if (i < o)
+            for (int m = g; m < o; m += 4)
+                acc = fma(2.0 * tile[i + pitch * m] - tile[m + pitch * i], Fme[m + (long long)o * e], acc);
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (g == 0 && i < o)
+        part[(long long)chunk * o * v + i + (long long)o * a] = red[i] + red[i + 64] + red[i + 128] + red[i + 192];
+}
+
+// R1[x] += sum over chunks of part[chunk][x], in chunk order
+__global__ void t1_fme_reduce_kernel(const double *__restrict__ part, int nchunk, long long n, double *__restrict__ R1) {
+    const long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    double s = 0.0;
+    for (int c = 0; c < nchunk; ++c) s += part[c * n + x];
+    R1[x] += s;
+}
+
 // c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e], c3[n,e] = sum_m ooov[m,m,n,e]
 // (ooov column-major o x o x o x v)
 __global__ void ooov_diag_sums_kernel(const double *__restrict__ ooov, int o, int v, double *__restrict__ c12) {
@@ -1002,6 +1041,19 @@ void t1_ytrace(Ctx *ctx, const double *Y, const double *t1, const double *G2, co
     Ctx::Scope s(ctx, "ccsd_t1");
     const long long n = (long long)o * v;
     t1_ytrace_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(Y, t1, G2, H1, c123, o, v, R1);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void t1_fme(Ctx *ctx, const double *T, const double *Fme, int o, int v, double *R1) {
+    JUES_REQUIRE(o <= 64, "t1_fme: nocc <= 64");
+    const int nchunk = (v + T1FME_CHUNK - 1) / T1FME_CHUNK;
+    const long long n = (long long)o * v;
+    double *part = static_cast<double *>(ctx->splitk_scratch((size_t)nchunk * n * sizeof(double)));
+    Ctx::Scope s(ctx, "ccsd_t1");
+    t1_fme_kernel<<<dim3((unsigned)v, (unsigned)nchunk), 256, (size_t)o * (o | 1) * sizeof(double), ctx->stream>>>(
+        T, Fme, o, v, part);
+    t1_fme_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(part, nchunk, n, R1);
+    ctx->count_launch();
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
