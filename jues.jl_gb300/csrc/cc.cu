@@ -233,7 +233,7 @@ double ccd_sweep(CCState *s, int prec) {
     // GEMM parts of WJ and WK at [(m,e),(a,m)]: -(tJ + 2 tK), or -2(tJ + tK) in the DF-RCCD.jl
     // form; then W12[(j,e),(b,j)] += Fae[b,e], so that the first ring GEMM also gives the
     // T[i,j,a,e] Fae[b,e] term of RCCD.jl:243
-    fae_from_rings(ctx, s->WJ.p, s->ovvoJ.p, s->WK.p, s->ovovK.p, (int)o, (int)v, s->reference_df_wmbej ? 2.0 : 1.0,
+    fae_from_rings(ctx, s->WJ.p, s->tr0.p, s->WK.p, s->tr0.p + vv, (int)o, (int)v, s->reference_df_wmbej ? 2.0 : 1.0,
                    2.0, s->Fae.p, s->W12.p);
 
     // Z: the terms of RCCD.jl:243-254 whose (i,a)<->(j,b) images are added by t2_finalize
@@ -416,6 +416,8 @@ static CCState *cc_finish(std::unique_ptr<CCState> s) {
         Perm4 q{{o, v, v, o}, {1, ov * o, o, ov}, {1, o, ov, ov * v}};
         permute4(ctx, q, -1.0, s->ovov.p, 0.0, s->ovovK.p);
     }
+    s->tr0 = DBuf<double>(ctx, (size_t)(2 * vv));
+    ring_traces(ctx, s->ovvoJ.p, nullptr, s->ovovK.p, nullptr, o, v, s->tr0.p, s->tr0.p + vv);
     s->oovvT = DBuf<double>(ctx, t2n);
     t_tilde(ctx, s->oovv.p, o, v, s->oovvT.p);
     if (method == 1) {
@@ -840,7 +842,7 @@ double ccsd_sweep(CCState *s, int prec) {
         G(s, prec, "ccsd_wk", ov, ov, ov, 0.5, W, mode2(o, o, oo), mode2(o, 1, oov), U, mode2(o, 1, oov),
           mode2(o, o, oo), 1.0, s->WK.p, plain(1), jb, nullptr, true, true);
     }
-    ring_traces(ctx, s->WJ.p, s->ovvoJ.p, s->WK.p, s->ovovK.p, (int)o, (int)v, tGJ, tGK);
+    ring_traces(ctx, s->WJ.p, s->tr0.p, s->WK.p, s->tr0.p + vv, (int)o, (int)v, tGJ, tGK);
     // the t1 terms: WJ += t1[j,f] <mb|ef> - t1[n,b] <mn|ej>, WK += -t1[j,f] <mb|fe> + t1[n,b] <nm|ej>
     G(s, prec, "ccsd_wj_t1", ovv, o, v, 1.0, ovvv, mode3(o, v, 1, ov, o), plain(ovv), t1,
       plain(o), plain(1), 1.0, s->WJ.p, mode3(o, v, 1, o, ov), plain(ovv), nullptr, true, false);
@@ -852,7 +854,7 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(1), plain(o), 1.0, s->WK.p, mode3(o, v, 1, o, ovv), plain(ov), nullptr, true, false);
     axpby(ctx, (size_t)(ov * ov), 2.0, s->WJ.p, 1.0, s->WK.p, s->W12.p);
     // Fae (the exchange t1 term as RCCSD.jl:190 or mRCCSD.jl:140), H1, G2; W12 += [m = j] F~ae
-    ccsd_fae(ctx, s->WJ.p, s->ovvoJ.p, s->WK.p, s->ovovK.p, tGJ, tGK, t1, s->c12.p, s->Fme.p,
+    ccsd_fae(ctx, s->WJ.p, s->tr0.p, s->WK.p, s->tr0.p + vv, tGJ, tGK, t1, s->c12.p, s->Fme.p,
              s->fock ? s->fOV.p : nullptr, s->fock ? s->fVV.p : nullptr, (int)o, (int)v,
              s->opts.ccsd_fae == JUES_CCSD_FAE_MRCCSD, s->Fae.p, H1, G2, s->W12.p);
 

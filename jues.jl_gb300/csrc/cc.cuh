@@ -21,6 +21,7 @@ struct CCState {
     DBuf<double> ooovQ;          // CCSD: ooov[m,i,j,a] at [(i,j),(a,m)], the seed of Y
     DBuf<double> M1;             // CCSD: 2 oovv[i,m,a,e] - ovov[m,a,i,e] at [(i,a),(m,e)] (T1's t1 terms)
     DBuf<double> ovvoJ, ovovK;   // ring-intermediate seeds in (me),(bj) layout
+    DBuf<double> tr0;            // their traces sum_m [(m,e),(a,m)], v x v each (trJ0 | trK0)
     // amplitudes and work arrays
     DBuf<double> T, Tn, Tt, Z, L, Wp, WJ, WK, W12, Fae, Fmi;
     DBuf<double> t1, t1n, Fme, U, Fmt;      // CCSD: U = T2 + 2 tau, Fmt = F~mi

@@ -297,17 +297,17 @@ void lincomb(Ctx *ctx, size_t n, int m, const double *const *vecs, const double 
 void wp_fmi(Ctx *ctx, double *Wp, const double *Fmi, int o);
 // Fmi[m,i] = sum_n 2 X[m,n,i,n] - X[m,n,n,i], X = Wp - oooo (o^4 arrays [(m,n),(i,j)])
 void fmi_from_x(Ctx *ctx, const double *Wp, const double *oooo, int o, double *Fmi);
-// Fae[a,e] = -(cJ tr(WJ - J0) + cK tr(WK - K0))[a,e], traces over m of [(m,e),(a,m)]; when W12 is
-// given, W12[(j,e),(a,j)] += Fae[a,e] for every j
-void fae_from_rings(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
-                    double cJ, double cK, double *Fae, double *W12);
+// Fae[a,e] = -(cJ (tr WJ - trJ0) + cK (tr WK - trK0))[a,e], traces over m of [(m,e),(a,m)] (trJ0, trK0:
+// the seeds' traces); when W12 is given, W12[(j,e),(a,j)] += Fae[a,e] for every j
+void fae_from_rings(Ctx *ctx, const double *WJ, const double *trJ0, const double *WK, const double *trK0, int o,
+                    int v, double cJ, double cK, double *Fae, double *W12);
 // CCSD: Ttau = T2 + t1 (x) t1 and U = T2 + 2 t1 (x) t1
 void ccsd_tau(Ctx *ctx, const double *T, const double *t1, int o, int v, double *Ttau, double *U);
-// traces over m of (WJ - J0) and (WK - K0) at [(m,e),(a,m)] into tJ[a,e], tK[a,e]
-void ring_traces(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
+// traces over m of WJ and WK at [(m,e),(a,m)] less trJ0, trK0 (null: nothing) into tJ[a,e], tK[a,e]
+void ring_traces(Ctx *ctx, const double *WJ, const double *trJ0, const double *WK, const double *trK0, int o, int v,
                  double *tJ, double *tK);
 // CCSD Fae, H1, G2 from the ring traces, and F~ae onto W12's (m = j) entries (kernels.cu)
-void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, const double *tGJ,
+void ccsd_fae(Ctx *ctx, const double *WJ, const double *trJ0, const double *WK, const double *trK0, const double *tGJ,
               const double *tGK, const double *t1, const double *c12, const double *Fme, const double *fOV,
               const double *fVV, int o, int v, bool mvariant, double *Fae, double *H1, double *G2, double *W12);
 // R1 += T1's <ma|fe> terms from the traces of Y[(i,j),(a,m)], which carries the ooov seed

@@ -487,13 +487,14 @@ __global__ void fmi_from_x_kernel(const double *__restrict__ Wp, const double *_
 
 // Fae from the ring intermediates and the Fae term folded into W12.  With t = WJ - J0 and
 // u = WK - K0 (the GEMM parts of WmBeJ and WmBEj, layout [(m,e),(b,j)]), their traces
-// tJ[a,e] = sum_m t[(m,e),(a,m)] and tK[a,e] = sum_m u[(m,e),(a,m)] give
+// tJ[a,e] = sum_m t[(m,e),(a,m)] and tK[a,e] = sum_m u[(m,e),(a,m)] (the seeds' traces trJ0, trK0
+// formed once) give
 // Fae[a,e] = -(cJ tJ + cK tK) by the pair symmetry of T2; then W12[(j,e),(a,j)] += Fae[a,e]
 // for every j, so the ring GEMM T[i,m,a,e] W12[(m,e),(b,j)] also yields T[i,j,a,e] Fae[b,e].
 // One warp per (a, e), its lanes over m; the (m = j) entries it reads and the ones it updates
 // are the same.
-__global__ void fae_trace_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
-                                 const double *__restrict__ WK, const double *__restrict__ K0, int o, int v,
+__global__ void fae_trace_kernel(const double *__restrict__ WJ, const double *__restrict__ trJ0,
+                                 const double *__restrict__ WK, const double *__restrict__ trK0, int o, int v,
                                  double cJ, double cK, double *__restrict__ Fae, double *__restrict__ W12) {
     const long long ov = (long long)o * v;
     const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -504,10 +505,11 @@ __global__ void fae_trace_kernel(const double *__restrict__ WJ, const double *__
     double tj = 0.0, tk = 0.0;
     for (int m = lane; m < o; m += 32) {
         const long long x = base + step * m;
-        tj += WJ[x] - J0[x];
-        tk += WK[x] - K0[x];
+        tj += WJ[x];
+        tk += WK[x];
     }
-    const double f = -(cJ * warp_allsum(tj) + cK * warp_allsum(tk));
+    const long long ae = a + (long long)v * e;
+    const double f = -(cJ * (warp_allsum(tj) - trJ0[ae]) + cK * (warp_allsum(tk) - trK0[ae]));
     if (lane == 0) Fae[a + (long long)v * e] = f;
     if (W12)
         for (int j = lane; j < o; j += 32) W12[base + step * j] += f;
@@ -528,11 +530,12 @@ __global__ void __launch_bounds__(256) ccsd_tau_kernel(const double *__restrict_
     }
 }
 
-// Traces over m of the GEMM parts of the CCSD ring intermediates (layout [(m,e),(b,j)]):
-// tJ[a,e] = sum_m (WJ - J0)[(m,e),(a,m)], tK[a,e] = sum_m (WK - K0)[(m,e),(a,m)].  One thread
+// Traces over m of the GEMM parts of the ring intermediates (layout [(m,e),(b,j)]):
+// tJ[a,e] = sum_m WJ[(m,e),(a,m)] - trJ0[a,e], tK likewise (null trJ0, trK0: the plain traces,
+// which is how the seeds' traces are formed once).  One thread
 // warp per (a, e), its lanes over m.
-__global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
-                                   const double *__restrict__ WK, const double *__restrict__ K0, int o, int v,
+__global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *__restrict__ trJ0,
+                                   const double *__restrict__ WK, const double *__restrict__ trK0, int o, int v,
                                    double *__restrict__ tJ, double *__restrict__ tK) {
     const long long ov = (long long)o * v;
     const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -543,14 +546,15 @@ __global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *
     double tj = 0.0, tk = 0.0;
     for (int m = lane; m < o; m += 32) {
         const long long x = base + step * m;
-        tj += WJ[x] - J0[x];
-        tk += WK[x] - K0[x];
+        tj += WJ[x];
+        tk += WK[x];
     }
     tj = warp_allsum(tj);
     tk = warp_allsum(tk);
+    const long long ae = a + (long long)v * e;
     if (lane == 0) {
-        tJ[a + (long long)v * e] = tj;
-        tK[a + (long long)v * e] = tk;
+        tJ[ae] = tj - (trJ0 ? trJ0[ae] : 0.0);
+        tK[ae] = tk - (trK0 ? trK0[ae] : 0.0);
     }
 }
 
@@ -565,8 +569,8 @@ __global__ void ring_traces_kernel(const double *__restrict__ WJ, const double *
 // (the T1 equation's tau corrections) and adds F~ae[a,e] to W12[(j,e),(a,j)] for every j, where
 // the first ring GEMM turns it into the T2[i,j,a,e] F~ae[b,e] term.  One warp per (a, e), its
 // lanes over m and n.
-__global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__restrict__ J0,
-                                const double *__restrict__ WK, const double *__restrict__ K0,
+__global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__restrict__ trJ0,
+                                const double *__restrict__ WK, const double *__restrict__ trK0,
                                 const double *__restrict__ tGJ, const double *__restrict__ tGK,
                                 const double *__restrict__ t1, const double *__restrict__ c12,
                                 const double *__restrict__ Fme, const double *__restrict__ fOV,
@@ -585,8 +589,8 @@ __global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__r
     const long long base2 = (long long)o * a + ov * e;
     for (int m = lane; m < o; m += 32) {
         const long long x = base + step * m;
-        tj += WJ[x] - J0[x];
-        tk += WK[x] - K0[x];
+        tj += WJ[x];
+        tk += WK[x];
         const double ta = t1[m + (long long)o * a];
         s1 = fma(ta, c1[m + (long long)o * e], s1);
         s2 = fma(ta, c2[m + (long long)o * e], s2);
@@ -594,14 +598,14 @@ __global__ void ccsd_fae_kernel(const double *__restrict__ WJ, const double *__r
         if (fOV) tfo = fma(ta, fOV[m + (long long)o * e], tfo);
         if (mvariant) {
             // H1[e,a]: the WJ trace at [(m,a),(e,m)] and S1[e,a]
-            tj2 += WJ[base2 + step * m] - J0[base2 + step * m];
+            tj2 += WJ[base2 + step * m];
             s12 = fma(t1[m + (long long)o * e], c1[m + (long long)o * a], s12);
         }
     }
-    tj = warp_allsum(tj); tk = warp_allsum(tk); s1 = warp_allsum(s1); s2 = warp_allsum(s2);
+    const long long ae = a + (long long)v * e, ea = e + (long long)v * a;
+    tj = warp_allsum(tj) - trJ0[ae]; tk = warp_allsum(tk) - trK0[ae]; s1 = warp_allsum(s1); s2 = warp_allsum(s2);
     tf = warp_allsum(tf); tfo = warp_allsum(tfo);
-    if (mvariant) { tj2 = warp_allsum(tj2); s12 = warp_allsum(s12); }
-    const long long ae = a + (long long)v * e;
+    if (mvariant) { tj2 = warp_allsum(tj2) - trJ0[ea]; s12 = warp_allsum(s12); }
     const double h1 = tj - tGJ[ae] + s1, g2 = tGK[ae] - tk + s2;
     const double h1x = mvariant ? tj2 - tGJ[e + (long long)v * a] + s12 : h1;
     double ft = 2.0 * g2 - h1x - (tGJ[ae] + 2.0 * tGK[ae]) - tfo;   // F~ae
@@ -1000,11 +1004,11 @@ void fmi_from_x(Ctx *ctx, const double *Wp, const double *oooo, int o, double *F
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
-void fae_from_rings(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
-                    double cJ, double cK, double *Fae, double *W12) {
+void fae_from_rings(Ctx *ctx, const double *WJ, const double *trJ0, const double *WK, const double *trK0, int o,
+                    int v, double cJ, double cK, double *Fae, double *W12) {
     Ctx::Scope s(ctx, "fae_trace");
     const long long n = (long long)v * v;
-    fae_trace_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, cJ, cK, Fae,
+    fae_trace_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, trJ0, WK, trK0, o, v, cJ, cK, Fae,
                                                                                W12);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
@@ -1017,20 +1021,20 @@ void ccsd_tau(Ctx *ctx, const double *T, const double *t1, int o, int v, double 
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
-void ring_traces(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, int o, int v,
+void ring_traces(Ctx *ctx, const double *WJ, const double *trJ0, const double *WK, const double *trK0, int o, int v,
                  double *tJ, double *tK) {
     Ctx::Scope s(ctx, "fae_trace");
     const long long n = (long long)v * v;
-    ring_traces_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, J0, WK, K0, o, v, tJ, tK);
+    ring_traces_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, trJ0, WK, trK0, o, v, tJ, tK);
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
-void ccsd_fae(Ctx *ctx, const double *WJ, const double *J0, const double *WK, const double *K0, const double *tGJ,
+void ccsd_fae(Ctx *ctx, const double *WJ, const double *trJ0, const double *WK, const double *trK0, const double *tGJ,
               const double *tGK, const double *t1, const double *c12, const double *Fme, const double *fOV,
               const double *fVV, int o, int v, bool mvariant, double *Fae, double *H1, double *G2, double *W12) {
     Ctx::Scope s(ctx, "fae_trace");
     const long long n = (long long)v * v;
-    ccsd_fae_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, J0, WK, K0, tGJ, tGK, t1, c12, Fme,
+    ccsd_fae_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, ctx->stream>>>(WJ, trJ0, WK, trK0, tGJ, tGK, t1, c12, Fme,
                                                                           fOV, fVV, o, v, mvariant ? 1 : 0, Fae,
                                                                           H1, G2, W12);
     JUES_CHECK_CUDA(cudaGetLastError());
