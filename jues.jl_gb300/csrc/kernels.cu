@@ -655,6 +655,7 @@ constexpr int T1FME_CHUNK = 8;
 __global__ void __launch_bounds__(256) t1_fme_kernel(const double *__restrict__ T, const double *__restrict__ Fme,
                                                      int o, int v, double *__restrict__ part) {
     extern __shared__ double tile[];   // [o][pitch], element (i, m) of the block at i + pitch m
+    __shared__ double fm[64];          // Fme[:, e]
     const int pitch = o | 1, ooi = o * o;
     const int a = blockIdx.x, chunk = blockIdx.y;
     const long long oo = (long long)o * o;
@@ -666,10 +667,10 @@ __global__ void __launch_bounds__(256) t1_fme_kernel(const double *__restrict__ 
         const double *blk = T + oo * (a + (long long)v * e);
         __syncthreads();
         for (int im = threadIdx.x; im < ooi; im += blockDim.x) tile[(im % o) + pitch * (im / o)] = blk[im];
+        if (threadIdx.x < o) fm[threadIdx.x] = Fme[threadIdx.x + (long long)o * e];
         __syncthreads();
         if (i < o)
-            for (int m = g; m < o; m += 4)
-                acc = fma(2.0 * tile[i + pitch * m] - tile[m + pitch * i], Fme[m + (long long)o * e], acc);
+            for (int m = g; m < o; m += 4) acc = fma(2.0 * tile[i + pitch * m] - tile[m + pitch * i], fm[m], acc);
     }
     __shared__ double red[256];
     red[threadIdx.x] = acc;
