@@ -55,6 +55,31 @@ def ccd_exec_flops(o, v):
     return 2 * o**2 * v**4 + 12 * o**3 * v**3 + 4 * o**4 * v**2 + 4 * o**2 * v**3 + 2 * o**3 * v**2
 
 
+def folds(o, v):
+    """Whether the split sweeps run the folded ladders (nocc <= 64 and nvir <= 361)."""
+    return o <= 64 and v * (v + 1) // 2 <= 65536 - 64
+
+
+def ccd_split_gemm_flops(o, v):
+    """One product's flops per CCD split sweep of each tcgen05 GEMM scope (3 products run): X and
+    the ladders folded over the pairs (i <= j), (a <= b) when folds(o, v), and the K-stacked rings."""
+    ov = float(o * v)
+    if folds(o, v):
+        np_, nq = o * (o + 1) / 2.0, v * (v + 1) / 2.0
+        x, lad = 2 * 2.0 * o * o * np_ * nq, 2 * 2.0 * np_ * nq * (np_ + nq)
+    else:
+        x, lad = 2.0 * o**4 * v**2, 2.0 * o**2 * v**2 * (o**2 + v**2)
+    return {"ccd_x": x, "ccd_pp_ladder": lad, "ccd_wj": 4 * ov**3, "ccd_wk": 2 * ov**3, "ccd_ring": 6 * ov**3}
+
+
+def ladder_launch_flops(o, v):
+    """Executed (3-product) flops of one ladder GEMM launch: one folded sign, or the whole ladder."""
+    if folds(o, v):
+        np_, nq = o * (o + 1) / 2.0, v * (v + 1) / 2.0
+        return 3 * 2.0 * np_ * nq * (np_ + nq)
+    return 3 * 2.0 * o**2 * v**2 * (v**2 + o**2)
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -394,7 +419,7 @@ def run_ccsd_measure(shape, gao, system, local, steps=3, fp64_steps=1):
     ses.close()
     pk, pk_kind = peaks()
     peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
-    pp_exec = 3 * 2.0 * o**2 * v**2 * (v**2 + o**2)   # both ladders, K-stacked in one launch
+    pp_exec = ladder_launch_flops(o, v)   # both ladders, K-stacked, one folded sign per launch
     pp_s = (pp_ms / pp_n / 1e3) if pp_n else None
     out = {"workload": f"rccsd_{shape.lower()}_split", "nbf": system.nbf, "nocc": o, "nvir": v,
            "s_per_iter": s_iter, "steps": len(lg), "fp64_s_per_iter": fp64,
@@ -457,9 +482,15 @@ def run_gpu(args):
     pp_n -= ctx.profile("ccd_pp_ladder.reduce")[1]      # split-K reductions are not GEMM launches
     ring_ms, ring_n = ctx.profile("ccd_ring")
     pack_ms, pack_n = ctx.profile("pack_split")
+    gemm = {}   # the tcgen05 GEMM launches of the sweep by scope (split-K reductions taken out)
+    for g in ccd_split_gemm_flops(o, vir):
+        g_ms, g_n = ctx.profile(g)
+        r_ms, r_n = ctx.profile(g + ".reduce")
+        gemm[g] = (g_ms - r_ms, g_n - r_n)
     other_ms = {k: sum(ctx.profile(p)[0] for p in ps) / args.steps
                 for k, ps in (("fae_fmi", ("fmi_trace", "fae_trace", "wp_fmi")),
                               ("x", ("ccd_x",)),
+                              ("fold", ("pair_fold", "pair_unfold")),
                               ("wj_wk", ("ccd_wj", "ccd_wk")),
                               ("t2_finalize", ("t2_finalize",)),
                               ("t_tilde_axpby", ("t_tilde", "axpby")),
@@ -573,12 +604,21 @@ def run_gpu(args):
     if rank != 0:
         return
     pk, pk_kind = peaks()
-    # three products; the launch runs both ladders K-stacked: [W'^T | T] . [T ; vvvv]^T
-    pp_flops_exec = 3 * 2.0 * o**2 * vir**2 * (vir**2 + o**2)
-    pp_avg_s = (pp_ms / pp_n / 1e3) if pp_n else None
-    achieved = pp_flops_exec / pp_avg_s / 1e12 if pp_avg_s else None
+    # the dominant kernel: gett_tc_kernel<128,3,2,2>, every split GEMM launch of the sweep (three
+    # products each); achieved = executed flops over all its launches / their summed duration
     peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
-    traffic = load_traffic().get(f"ccd_pp_ladder_{name.lower()}")
+    gflops = ccd_split_gemm_flops(o, vir)
+    g_s = sum(ms for ms, _ in gemm.values()) / 1e3
+    g_n = sum(n_ for _, n_ in gemm.values())
+    g_flops = 3 * sum(gflops.values()) * args.steps
+    achieved = g_flops / g_s / 1e12 if g_s > 0 else None
+    per_gemm = {g: {"ms_per_sweep": ms / args.steps, "launches_per_sweep": n_ / args.steps,
+                    "tflops_executed": 3 * gflops[g] * args.steps / (ms / 1e3) / 1e12 if ms > 0 else None,
+                    "frac": 3 * gflops[g] * args.steps / (ms / 1e3) / 1e12 / peak if ms > 0 else None}
+                for g, (ms, n_) in gemm.items()}
+    pp_flops_exec = ladder_launch_flops(o, vir)
+    pp_avg_s = (pp_ms / pp_n / 1e3) if pp_n else None
+    traffic = load_traffic().get(f"ccd_gemms_{name.lower()}")
     cpu = None
     if not args.skip_cpu and ws == 1:
         sw = cpu_pipeline(system)
@@ -592,11 +632,11 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * s_per_iter, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": SPLIT_DTYPE, "data": "synthetic",
         "config": {"workload": f"rccd_{name.lower()}_split", "nbf": n, "nocc": o, "nvir": vir, "naux": naux,
-                   "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (packed vvvv 2.6 GB)",
+                   "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (packed folded vvvv 1.4 GB, T2 0.33 GB)",
                    "guess": "mp2", "diis": 6, "precision": "split (JUES_PREC_SPLIT)"},
         "replica_sweeps_per_s": ws / s_per_iter,
         "tflops_reference_flops": ccd_ref_flops(o, vir) / s_per_iter / 1e12,
-        "tflops_executed_tensor": 3 * ccd_exec_flops(o, vir) / s_per_iter / 1e12,
+        "tflops_executed_tensor": 3 * sum(ccd_split_gemm_flops(o, vir).values()) / s_per_iter / 1e12,
         "fp64_s_per_iter": fp64,
         "fp64_tflops_executed": (fp64_exec / fp64 / 1e12) if fp64 else None,
         "fp64_frac_of_spec": (fp64_exec / fp64 / 1e12 / FP64_SPEC_TFLOPS) if fp64 else None,
@@ -609,11 +649,18 @@ def run_gpu(args):
         "wall_s_timed": wall, "setup_s": setup_s,
         "kernels_ms_per_step": {"pp_ladder": pp_ms / args.steps, "ring": ring_ms / args.steps,
                                 "pack_split": pack_ms / args.steps, **other_ms},
-        "roofline": {"bound": "tensor", "kernel": "ccd_pp_ladder (tcgen05 split GEMM, 3 products; hole-hole and particle ladders K-stacked)",
+        "roofline": {"bound": "tensor",
+                     "kernel": "gett_tc_kernel<128,3,2,2>, every tcgen05 split GEMM launch of the sweep (3 products): "
+                               "X and the hole-hole + particle ladders folded over (i<=j), (a<=b), WmBeJ and the "
+                               "rings K-stacked, WmBEj, the third ring",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": f"{pk_kind} bf16 sustained",
-                     "flops_per_launch": pp_flops_exec, "launch_ms": 1e3 * pp_avg_s if pp_avg_s else None,
+                     "flops_per_launch": (g_flops / g_n) if g_n else None,
+                     "launch_ms": (1e3 * g_s / g_n) if g_n else None, "launches_per_sweep": g_n / args.steps,
+                     "per_gemm": per_gemm,
+                     "ladder_launch": {"flops": pp_flops_exec, "ms": 1e3 * pp_avg_s if pp_avg_s else None,
+                                       "frac": (pp_flops_exec / pp_avg_s / 1e12 / peak) if pp_avg_s else None},
                      "traffic": traffic},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
         "rccsd": ccsd, "batch": batch, "pT": pT, "df_rccd": df,

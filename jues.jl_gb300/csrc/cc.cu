@@ -104,6 +104,109 @@ static void ladder_stacks_l(CCState *s, const double *Tl, const char *name) {
 }
 
 // ---------------------------------------------------------------------------------------
+// The folded ladders (split precision, nocc <= 64).  The ladders' output is pair-symmetric,
+// L[i,j,a,b] = L[j,i,b,a], like Tl (T2, or T2 + tau for CCSD).  For p = (i <= j), q = (a <= b)
+// and s = +-1, L_s[p,q] = 1/2 (L[i,j,a,b] + s L[i,j,b,a]) is s-symmetric in (i,j) too, so
+//   L[i,j,a,b] = L+[p,q] + sgn L-[p,q]   (sgn = +1 for i < j, -1 for i > j; L- = 0 for i = j or a = b),
+// and every contraction over a pair (e,f) with an s-symmetric factor A_s[.,(e,f)] = Tl[.,e,f] +
+// s Tl[.,f,e] runs over e <= f only: sum_ef g[ef] A_s[ef] / 2 = sum_{e<=f} A_s[ef] w_s[ef] with the
+// weight w_s[ef] = 1/2 (g[ef] + s g[fe]), 1/4 g[ee] on the diagonal (pair_fold).  So
+//   X_s   = Xw_s . A_s^T                       (K = the nq pairs (e <= f))
+//   L_s   = O_s + [C_s | A_s] . [A_s^T | B_s]^T  (K = np pairs (m <= n), then the nq pairs (e <= f))
+// with C_s the fold of W'[mn,ij] over (m,n) (hole-hole ladder), B_s that of vvvv (particle
+// ladder), O_s = 1/2 oovv folded over (a,b): two GEMMs of M = np, N = nq, K = np + nq in place
+// of one of M = o^2, N = v^2, K = o^2 + v^2, about a quarter of its work; X likewise halves.
+// ---------------------------------------------------------------------------------------
+static void pair_begin(CCState *s) {
+    if (s->stackPB[0].buf.p) return;
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, vv = v * v, ov = o * v;
+    const long long np = o * (o + 1) / 2, nq = v * (v + 1) / 2;
+    const long long kp = (np + 127) / 128 * 128, kq = (nq + 127) / 128 * 128;
+    {
+        // B_s[(a<=b), (e<=f)] from vvvv[ab,ef] (rows a + v b, K e + v f)
+        DBuf<double> tmp(ctx, (size_t)(2 * nq * nq));
+        pair_fold(ctx, s->vvvv.p, nq, true, 0, 1, v, (int)v, vv, vv * v, 0.5, true, tmp.p);
+        for (int k = 0; k < 2; ++k) {
+            s->stackPB[k].ensure(ctx, nq, kp + kq, 2);
+            pack_stacked(ctx, s->stackPB[k], kp, tmp.p + k * nq * nq, plain(1), plain(nq), nq, nq, 1.0);
+        }
+    }
+    {
+        // Xw_s[mn, (e<=f)] from oovv[mn,ef]
+        DBuf<double> tmp(ctx, (size_t)(2 * oo * nq));
+        pair_fold(ctx, s->oovv.p, oo, false, oo, 1, 0, (int)v, oo, oo * v, 0.5, true, tmp.p);
+        for (int k = 0; k < 2; ++k) {
+            s->stackPX[k].ensure(ctx, oo, kq, 2);
+            pack_stacked(ctx, s->stackPX[k], 0, tmp.p + k * oo * nq, plain(1), plain(oo), oo, nq, 1.0);
+        }
+    }
+    if (s->method == 1) {
+        // Yw_s[(a,m), (e<=f)] from <am|ef> = ovvv[m,a,f,e] (row a + v m at a o + m, K at e ovv + f ov)
+        DBuf<double> tmp(ctx, (size_t)(2 * ov * nq));
+        pair_fold(ctx, s->ovvv.p, ov, false, v, o, 1, (int)v, ov * v, ov, 0.5, true, tmp.p);
+        for (int k = 0; k < 2; ++k) {
+            s->stackPY[k].ensure(ctx, ov, kq, 2);
+            pack_stacked(ctx, s->stackPY[k], 0, tmp.p + k * ov * nq, plain(1), plain(ov), ov, nq, 1.0);
+        }
+        s->Ypm = DBuf<double>(ctx, (size_t)(2 * np * ov));
+    }
+    // O_s[(i<=j), (a<=b)] = 1/2 (oovv[ij,ab] + s oovv[ij,ba])
+    s->Opm = DBuf<double>(ctx, (size_t)(2 * np * nq));
+    pair_fold(ctx, s->oovv.p, np, true, 0, 1, o, (int)v, oo, oo * v, 0.5, false, s->Opm.p);
+    s->Apm = DBuf<double>(ctx, (size_t)(2 * np * nq));
+    s->Lpm = DBuf<double>(ctx, (size_t)(2 * np * nq));
+    s->Cpm = DBuf<double>(ctx, (size_t)(2 * np * np));
+    s->Xpm = DBuf<double>(ctx, (size_t)(2 * oo * np));
+    for (int k = 0; k < 2; ++k) s->stackPA[k].ensure(ctx, np, kp + kq, 2);
+}
+
+// A_s from Tl, then W' = oooo + X: X[mn,ij] = X+[mn,p] + sgn X-[mn,p]
+static void pair_x(CCState *s, const double *Tl, const char *name) {
+    Ctx *ctx = s->ctx;
+    pair_begin(s);
+    const long long o = s->o, v = s->v, oo = o * o;
+    const long long np = o * (o + 1) / 2, nq = v * (v + 1) / 2;
+    const long long kp = (np + 127) / 128 * 128, kq = (nq + 127) / 128 * 128;
+    // A_s[(i<=j), (e<=f)] = Tl[i,j,e,f] + s Tl[i,j,f,e]
+    pair_fold(ctx, Tl, np, true, 0, 1, o, (int)v, oo, oo * v, 1.0, false, s->Apm.p);
+    for (int k = 0; k < 2; ++k) {
+        pack_stacked(ctx, s->stackPA[k], kp, s->Apm.p + k * np * nq, plain(1), plain(np), np, nq, 1.0);
+        gett_tc_views(ctx, s->stackPX[k].view(0, kq), s->stackPA[k].view(kp, kq), oo, np, 1.0, 0.0,
+                      s->Xpm.p + k * oo * np, plain(1), plain(oo), nullptr, name);
+    }
+    pair_unfold(ctx, s->Xpm.p, oo * np, s->oooo.p, (int)o, oo, oo, 1, oo, 1, false, s->Wp.p);
+}
+
+// L_s = O_s + C_s . A_s + A_s . B_s^T, C_s the fold of the finished W'
+static void pair_l(CCState *s, const char *name) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o;
+    const long long np = o * (o + 1) / 2, nq = v * (v + 1) / 2;
+    const long long kp = (np + 127) / 128 * 128, kq = (nq + 127) / 128 * 128;
+    // C_s[(i<=j), (m<=n)] from W'[mn,ij] (at m + o n + o^2 (i + o j))
+    pair_fold(ctx, s->Wp.p, np, true, 0, oo, oo * o, (int)o, 1, o, 0.5, true, s->Cpm.p);
+    for (int k = 0; k < 2; ++k) {
+        pack_stacked(ctx, s->stackPA[k], 0, s->Cpm.p + k * np * np, plain(1), plain(np), np, np, 1.0);
+        pack_stacked(ctx, s->stackPB[k], 0, s->Apm.p + k * np * nq, plain(np), plain(1), nq, np, 1.0);
+        gett_tc_views(ctx, s->stackPA[k].view(0, kp + kq), s->stackPB[k].view(0, kp + kq), np, nq, 1.0, 1.0,
+                      s->Lpm.p + k * np * nq, plain(1), plain(np), s->Opm.p + k * np * nq, name);
+    }
+}
+
+// CCSD: Y[ij,(a,m)] = ooovQ + Y+[p,(a,m)] + sgn Y-[p,(a,m)], Y_s = A_s . Yw_s^T
+static void pair_y(CCState *s, double *Y, const char *name) {
+    Ctx *ctx = s->ctx;
+    const long long o = s->o, v = s->v, oo = o * o, ov = o * v;
+    const long long np = o * (o + 1) / 2, nq = v * (v + 1) / 2;
+    const long long kp = (np + 127) / 128 * 128, kq = (nq + 127) / 128 * 128;
+    for (int k = 0; k < 2; ++k)
+        gett_tc_views(ctx, s->stackPA[k].view(kp, kq), s->stackPY[k].view(0, kq), np, ov, 1.0, 0.0,
+                      s->Ypm.p + k * np * ov, plain(1), plain(np), nullptr, name);
+    pair_unfold(ctx, s->Ypm.p, np * ov, s->ooovQ.p, (int)o, ov, 1, oo, 1, np, true, Y);
+}
+
+// ---------------------------------------------------------------------------------------
 // The ring contractions in split precision, on K-stacked packs (gett_tc_views).  With the
 // block width kb = roundup(ov, 128) and T2 read in the ring GEMMs' two layouts,
 //   R1 = T2[i,m,a,e] (rows (i,a), K (m,e)) and R23 = T2[m,i,a,e] (the same rows, m unit-stride),
@@ -184,8 +287,11 @@ double ccd_sweep(CCState *s, int prec) {
 
     // In split precision the ladders and the ring contractions run on K-stacked packs (two planes).
     const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;
+    const bool pairl = stacked && t2_finalize_folds((int)o, (int)v);   // the folded ladders
     // W'[mn,ij] = oooo[mn,ij] + X[mn,ij], X = sum_ef oovv[mn,ef] T[ij,ef]  (Wmnij + the Wabef T-part)
-    if (stacked)
+    if (pairl)
+        pair_x(s, T, "ccd_x");
+    else if (stacked)
         ladder_stacks_x(s, T, "ccd_x");
     else
         G(s, prec, "ccd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), T, plain(oo), plain(1), 1.0, s->Wp.p,
@@ -196,7 +302,9 @@ double ccd_sweep(CCState *s, int prec) {
     // W'[(m,n),(i,j)] -= [m = i] Fmi[n,j] + [n = j] Fmi[m,i]
     wp_fmi(ctx, s->Wp.p, s->Fmi.p, (int)o);
     // L = oovv + (W')^T.T + T.vvvv^T                                     (RCCD.jl:243-246)
-    if (stacked) {
+    if (pairl) {
+        pair_l(s, "ccd_pp_ladder");
+    } else if (stacked) {
         ladder_stacks_l(s, T, "ccd_pp_ladder");
     } else {
         G(s, prec, "ccd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), T, plain(1), plain(oo),
@@ -255,11 +363,12 @@ double ccd_sweep(CCState *s, int prec) {
     s->cache_operands = false;
     // with DIIS the step norm comes from its error vector (the same |Tn - T|^2), so the
     // finalisation skips it: two of its five FP64 operations per element
+    const double *Lf = pairl ? s->Lpm.p : s->L.p;
     if (s->opts.diis) {
-        t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, nullptr, s->Tn.p);
+        t2_finalize(ctx, Lf, Z, s->invD.p, (int)o, (int)v, nullptr, s->Tn.p, nullptr, nullptr, pairl);
         return -1.0;
     }
-    return t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p);
+    return t2_finalize(ctx, Lf, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p, nullptr, nullptr, pairl);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -785,8 +894,11 @@ double ccsd_sweep(CCState *s, int prec) {
       plain(0), 0.0, s->Fme.p, plain(1), plain(0), nullptr, true, false);
     // In split precision the ladders, Y and the ring contractions run on K-stacked packs.
     const bool stacked = prec == JUES_PREC_SPLIT || prec == JUES_PREC_SPLIT2;   // two planes
+    const bool pairl = stacked && t2_finalize_folds((int)o, (int)v);             // the folded ladders
     // W' = oooo + X, X = sum_ef oovv[mn,ef] Ttau[ij,ef] (Wmnij and Wabef's T2 + tau parts)
-    if (stacked)
+    if (pairl)
+        pair_x(s, Ttau, "ccsd_x");
+    else if (stacked)
         ladder_stacks_x(s, Ttau, "ccsd_x");
     else
         G(s, prec, "ccsd_x", oo, oo, vv, 1.0, W, plain(1), plain(oo), Ttau, plain(oo), plain(1), 1.0, s->Wp.p,
@@ -819,7 +931,9 @@ double ccsd_sweep(CCState *s, int prec) {
       s->Fmt.p, plain(1), plain(o));
     wp_fmi(ctx, s->Wp.p, s->Fmt.p, (int)o);
     // L = oovv + W'^T Ttau + Ttau vvvv^T  (Wabef's t1 parts go through Y below)
-    if (stacked) {
+    if (pairl) {
+        pair_l(s, "ccsd_pp_ladder");
+    } else if (stacked) {
         ladder_stacks_l(s, Ttau, "ccsd_pp_ladder");
     } else {
         G(s, prec, "ccsd_hh_ladder", oo, vv, oo, 1.0, s->Wp.p, plain(oo), plain(1), Ttau, plain(1), plain(oo),
@@ -860,7 +974,9 @@ double ccsd_sweep(CCState *s, int prec) {
 
     // Y[ij,(a,m)] = sum_ef Ttau[i,j,e,f] <am|ef> (<am|ef> = ovvv[m,a,f,e])
     double *Y = s->aux2.p;
-    if (stacked) {
+    if (pairl) {
+        pair_y(s, Y, "ccsd_y");
+    } else if (stacked) {
         // Ttau[ij,ef] from the ladder stack; ovvv as (a,m) x (e,f), packed once
         const long long ko = (oo + 127) / 128 * 128, kv = (vv + 127) / 128 * 128;
         if (!s->stackY.buf.p) {
@@ -933,8 +1049,8 @@ double ccsd_sweep(CCState *s, int prec) {
     // with DIIS the step norm comes from its error vector over [t1 | T2] (the same squared sum), so
     // the finalisation skips it unless the per-block norms are wanted (AutoRCCSD's rms)
     const bool norms = !s->opts.diis || s->auto_rms;
-    double r2 = t2_finalize(ctx, s->L.p, Z, s->invD.p, (int)o, (int)v, norms ? T : nullptr, s->Tn.p,
-                            stacked ? nullptr : t1, stacked ? nullptr : q);
+    double r2 = t2_finalize(ctx, pairl ? s->Lpm.p : s->L.p, Z, s->invD.p, (int)o, (int)v, norms ? T : nullptr,
+                            s->Tn.p, stacked ? nullptr : t1, stacked ? nullptr : q, pairl);
     // t1n = R1 / D_ia and its step norm
     const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, norms ? t1 : nullptr);
     if (!norms) return -1.0;

@@ -41,6 +41,20 @@ struct CCState {
     // vvvv packed once); stackXW = oovv (rows (m,n), K (e,f)) for X; stackY = ovvv as (a,m) x (e,f)
     // for CCSD's Y
     StackedPack stackLA, stackLB, stackXW, stackY;
+    // split precision with nocc <= 64 (t2_finalize_folds): the same contractions folded by the pair
+    // symmetry over occupied pairs p = (i <= j) (np of them) and virtual pairs q = (a <= b) (nq),
+    // sign s = +1 (index 0) and -1 (index 1):
+    //   A_s[p,q(e,f)] = Tl[i,j,e,f] + s Tl[i,j,f,e]                     (Apm, per sweep)
+    //   X_s[mn,p]  = sum_q Xw_s[mn,q] A_s[p,q]                            (X = X+ + sgn X-)
+    //   L_s[p,q]   = O_s[p,q] + sum_p' C_s[p,p'] A_s[p',q] + sum_q' A_s[p,q'] B_s[q,q']
+    //   Y_s[p,am]  = sum_q A_s[p,q] Yw_s[am,q]                            (CCSD)
+    // with the weights B_s (vvvv), Xw_s (oovv), Yw_s (ovvv) and C_s (W', per sweep) folded over
+    // their contracted pair at 1/2 (1/4 on its diagonal), and O_s = 1/2 oovv folded over (a, b).
+    // stackPA[s] = [C_s | A_s] (rows p), stackPB[s] = [A_s^T | B_s] (rows q, B_s packed once),
+    // stackPX[s] = Xw_s (rows (m,n)), stackPY[s] = Yw_s (rows (a,m)).
+    bool pairl = false;
+    DBuf<double> Apm, Cpm, Lpm, Opm, Xpm, Ypm;
+    StackedPack stackPA[2], stackPB[2], stackPX[2], stackPY[2];
     // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
     std::vector<DBuf<double>> dv, de;
     std::vector<std::vector<double>> gram;   // gram[k][l] = e_k . e_l, k,l in insertion order

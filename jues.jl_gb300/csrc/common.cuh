@@ -282,7 +282,17 @@ double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t
 // with C[i,j,a,b] = t1[i,a] q[b,j] when t1 and q (v x o) are given; returns ||Tn - Told||^2 if
 // Told != nullptr.  Writes Tn.
 double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
-                   const double *Told, double *Tn, const double *t1 = nullptr, const double *q = nullptr);
+                   const double *Told, double *Tn, const double *t1 = nullptr, const double *q = nullptr,
+                   bool pairl = false);
+// whether t2_finalize takes folded ladders (pairl) at these sizes
+bool t2_finalize_folds(int o, int v);
+// folding of a pair-symmetric contraction over an index pair (e <= f) of extent d (kernels.cu,
+// pair_fold_kernel): out = [out+ | out-], each R x d(d+1)/2
+void pair_fold(Ctx *ctx, const double *src, long long R, bool rowpair, long long rd, long long rs0, long long rs1,
+               int d, long long ke, long long kf, double scale, bool diag_half, double *out);
+// the inverse over an occupied pair (i <= j) (pair_unfold_kernel)
+void pair_unfold(Ctx *ctx, const double *P, long long npc, const double *base, int o, long long C, long long sij,
+                 long long sc, long long tp, long long tc, bool ijfast, double *out);
 // invD[i,j,a,b] = 1 / (e_i + e_j - e_a - e_b)
 void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out);
 // t1n[i,a] /= (e_i - e_a) in place; returns ||t1n - t1old||^2

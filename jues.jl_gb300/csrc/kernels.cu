@@ -278,8 +278,13 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
 // pair (a <= b) (one pair per block, so resident blocks overlap their load and compute phases);
 // Z[:,:,a,b] and Z[:,:,b,a] are contiguous o x o blocks, loaded coalesced into shared memory on
 // an odd row pitch (conflict-free transposed reads), so every global access is unit-stride.
-// Dynamic shared memory 2 o pitch doubles (o <= 64).
-template <bool RANK1>
+// Dynamic shared memory 2 o pitch doubles (o <= 64), + 4 o with the rank-one term, + 2 np with
+// PAIRL: then L holds the folded ladders [L+ | L-], each np x nq (np = o(o+1)/2 pairs i <= j, nq =
+// v(v+1)/2 pairs a <= b, pair index j(j+1)/2 + i), with
+//   L[i,j,a,b] = L+[(i,j),(a,b)] + L-[(i,j),(a,b)] (i <= j, a <= b), L[i,j,b,a] = L+ - L-,
+//   L[j,i,b,a] = L[i,j,a,b], and L- taken as zero for i = j or a = b;
+// block (a <= b) reads column p = blockIdx.x of each.
+template <bool RANK1, bool PAIRL>
 __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(const double *__restrict__ L,
                                                                const double *__restrict__ Z,
                                                                const double *__restrict__ invD, int o, int v,
@@ -303,6 +308,16 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             r1v[k] = w == 0 ? t1[i + (long long)o * a] : w == 1 ? t1[i + (long long)o * b]
                    : w == 2 ? q[a + (long long)v * i] : q[b + (long long)v * i];
         }
+    const int np = o * (o + 1) / 2;
+    double *ls = r1v + (RANK1 ? 4 * o : 0);   // PAIRL: [L+ column | L- column], np each
+    if (PAIRL) {
+        const long long nq = (long long)v * (v + 1) / 2;
+        const double *lp = L + (long long)np * blockIdx.x, *lm = lp + (long long)np * nq;
+        for (int k = threadIdx.x; k < np; k += blockDim.x) {
+            ls[k] = lp[k];
+            ls[np + k] = lm[k];
+        }
+    }
     {
         for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
             const int i = ij % o, j = ij / o;
@@ -315,7 +330,18 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             // Z_ab[i,j] and Z_ba[j,i]; Z_ba[i,j] and Z_ab[j,i]
             const double zab = zs[j + pitch * i], zba_t = zs[o * pitch + i + pitch * j];
             const double inv = invD[ab + ij];   // D is symmetric in (a, b)
-            double x = L[ab + ij] + zab + zba_t;
+            double lab, lba = 0.0;
+            if (PAIRL) {
+                const int i0 = min(i, j), j0 = max(i, j), pij = j0 * (j0 + 1) / 2 + i0;
+                const double lpv = ls[pij];
+                const double lmv = (i == j || a == b) ? 0.0 : (i < j ? ls[np + pij] : -ls[np + pij]);
+                lab = lpv + lmv;
+                lba = lpv - lmv;
+            } else {
+                lab = L[ab + ij];
+            }
+            // Z's two terms first: T[j,i,b,a] sums the same three numbers in the same order
+            double x = lab + (zab + zba_t);
             // C[i,j,a,b] + C[j,i,b,a] = t1[i,a] q[b,j] + t1[j,b] q[a,i]
             if (RANK1) x += r1v[i] * r1v[3 * o + j] + r1v[o + j] * r1v[2 * o + i];
             x *= inv;
@@ -323,7 +349,7 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
             if (a != b) {
                 const double zba = zs[o * pitch + j + pitch * i], zab_t = zs[i + pitch * j];
-                double y = L[ba + ij] + zba + zab_t;
+                double y = (PAIRL ? lba : L[ba + ij]) + (zba + zab_t);
                 if (RANK1) y += r1v[o + i] * r1v[2 * o + j] + r1v[j] * r1v[3 * o + i];
                 y *= inv;
                 Tn[ba + ij] = y;
@@ -335,6 +361,65 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+
+// Folding of a pair-symmetric contraction (the ladders, X, Y).  For an index pair (e, f) of
+// extent d, q = f(f+1)/2 + e (e <= f) numbers the d(d+1)/2 pairs.  Block q writes, for every row
+// r < R,
+//   out+[r + R q] = c (src[ro(r) + e ke + f kf] + src[ro(r) + f ke + e kf])
+//   out-[r + R q] = c (src[ro(r) + e ke + f kf] - src[ro(r) + f ke + e kf])
+// (out- = out+ + R nk, nk = d(d+1)/2), c = scale, halved on the diagonal e = f when diag_half.
+// Rows: with rowpair, r is itself a pair (a <= b) and ro(r) = a rs0 + b rs1; else
+// ro(r) = (r mod rd) rs0 + (r / rd) rs1.
+__global__ void __launch_bounds__(256) pair_fold_kernel(const double *__restrict__ src, long long R, int rowpair,
+                                                        long long rd, long long rs0, long long rs1, long long ke,
+                                                        long long kf, long long nk, double scale, int diag_half,
+                                                        double *__restrict__ out) {
+    int e, f;
+    pair_ab(blockIdx.x, e, f);
+    const long long k1 = e * ke + f * kf, k2 = f * ke + e * kf;
+    const double c = (diag_half && e == f) ? 0.5 * scale : scale;
+    double *op = out + R * (long long)blockIdx.x, *om = op + R * nk;
+    for (long long r = threadIdx.x; r < R; r += blockDim.x) {
+        long long ro;
+        if (rowpair) {
+            int a, b;
+            pair_ab(r, a, b);
+            ro = a * rs0 + b * rs1;
+        } else {
+            long long r1, r0;
+            divmod_ll(r, rd, r1, r0);
+            ro = r0 * rs0 + r1 * rs1;
+        }
+        const double x = src[ro + k1], y = src[ro + k2];
+        op[r] = c * (x + y);
+        om[r] = c * (x - y);
+    }
+}
+
+// The inverse for a pair index (i, j) of extent o (np = o(o+1)/2 pairs): for every i, j < o and
+// column c < C,
+//   out[(i + o j) sij + c sc] = base[same] + P+[p tp + c tc] + sgn P-[p tp + c tc]
+// with p the pair of (min(i,j), max(i,j)), sgn = +1 for i < j, -1 for i > j, and no P- term for
+// i = j (P- = P+ + npc).  ijfast: consecutive threads take consecutive (i, j), else consecutive c.
+__global__ void __launch_bounds__(256) pair_unfold_kernel(const double *__restrict__ P, long long npc,
+                                                          const double *__restrict__ base, int o, long long C,
+                                                          long long sij, long long sc, long long tp, long long tc,
+                                                          int ijfast, double *__restrict__ out) {
+    const long long oo = (long long)o * o, n = oo * C;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+         x += (long long)gridDim.x * blockDim.x) {
+        long long ij, c;
+        if (ijfast) divmod_ll(x, oo, c, ij);
+        else divmod_ll(x, C, ij, c);
+        const int i = (int)(ij % o), j = (int)(ij / o);
+        const int i0 = min(i, j), j0 = max(i, j);
+        const long long pi = (long long)(j0 * (j0 + 1) / 2 + i0) * tp + c * tc;
+        double val = P[pi];
+        if (i != j) val += i < j ? P[npc + pi] : -P[npc + pi];
+        const long long oi = ij * sij + c * sc;
+        out[oi] = (base ? base[oi] : 0.0) + val;
+    }
+}
 
 // T~[i,j,a,b] = 2 T[i,j,a,b] - T[j,i,a,b], one (a,b) block per iteration with its transpose
 // through shared memory (odd row pitch), every global access unit-stride
@@ -890,35 +975,40 @@ void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out) {
     JUES_CHECK_CUDA(cudaGetLastError());
 }
 
+bool t2_finalize_folds(int o, int v) { return o <= 64 && (long long)v * (v + 1) / 2 <= 65536 - 64; }
+
 double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
-                   const double *Told, double *Tn, const double *t1, const double *q) {
+                   const double *Told, double *Tn, const double *t1, const double *q, bool pairl) {
     JUES_REQUIRE(!t1 == !q, "t2_finalize: t1 and q come together");
+    JUES_REQUIRE(!pairl || t2_finalize_folds(o, v), "t2_finalize: folded ladders need nocc <= 64, nvir <= 361");
     long long npair = (long long)v * (v + 1) / 2;
     int nb = (int)(npair < RED_BLOCKS ? npair : RED_BLOCKS);
     {
         Ctx::Scope s(ctx, "t2_finalize");
         // one block per pair; the step norm's partials (one per block) must fit the reduction scratch
-        if (o <= 64 && npair <= 65536 - 64) {
-            const size_t smem = ((size_t)2 * o * (o | 1) + (t1 ? 4 * o : 0)) * sizeof(double);
+        if (t2_finalize_folds(o, v)) {
+            const size_t smem =
+                ((size_t)2 * o * (o | 1) + (t1 ? 4 * o : 0) + (pairl ? (size_t)o * (o + 1) : 0)) * sizeof(double);
             // the rank-one term is a template parameter: without it the kernel fits 32 registers
             // and eight blocks per SM
             static std::atomic<unsigned long long> attr_set{0};
             const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
             if (smem > 48 * 1024 && (!bit || !(attr_set.load() & bit))) {
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 65 * 8));
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (2 * 64 * 65 + 4 * 64) * 8));
+                const int most = (2 * 64 * 65 + 4 * 64 + 64 * 65) * 8;   // o = 64, rank-one term, folded L
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false, false>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true, false>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false, true>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true, true>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, most));
                 attr_set.fetch_or(bit);
             }
             nb = (int)npair;
-            if (t1)
-                t2_finalize_smem_kernel<true><<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn,
-                                                                                   ctx->d_red, t1, q);
-            else
-                t2_finalize_smem_kernel<false><<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn,
-                                                                                    ctx->d_red, nullptr, nullptr);
+            auto kern = t1 ? (pairl ? t2_finalize_smem_kernel<true, true> : t2_finalize_smem_kernel<true, false>)
+                           : (pairl ? t2_finalize_smem_kernel<false, true> : t2_finalize_smem_kernel<false, false>);
+            kern<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red, t1, q);
         } else {
             t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red, t1, q);
         }
@@ -927,6 +1017,25 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
     return Told ? finish_reduce(ctx, nb) : 0.0;
 }
 
+
+void pair_fold(Ctx *ctx, const double *src, long long R, bool rowpair, long long rd, long long rs0, long long rs1,
+               int d, long long ke, long long kf, double scale, bool diag_half, double *out) {
+    const long long nk = (long long)d * (d + 1) / 2;
+    JUES_REQUIRE(d > 0 && R > 0 && nk < (1LL << 31), "pair_fold: bad extents");
+    Ctx::Scope s(ctx, "pair_fold");
+    pair_fold_kernel<<<(unsigned)nk, 256, 0, ctx->stream>>>(src, R, rowpair ? 1 : 0, rd, rs0, rs1, ke, kf, nk, scale,
+                                                            diag_half ? 1 : 0, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
+
+void pair_unfold(Ctx *ctx, const double *P, long long npc, const double *base, int o, long long C, long long sij,
+                 long long sc, long long tp, long long tc, bool ijfast, double *out) {
+    const long long n = (long long)o * o * C;
+    Ctx::Scope s(ctx, "pair_unfold");
+    pair_unfold_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(P, npc, base, o, C, sij, sc, tp, tc, ijfast ? 1 : 0,
+                                                             out);
+    JUES_CHECK_CUDA(cudaGetLastError());
+}
 
 double t1_finalize(Ctx *ctx, double *t1n, const double *eps, int o, int v, const double *t1old) {
     {

@@ -1,0 +1,153 @@
+"""The folded ladders of the split sweeps (csrc/cc.cu pair_x / pair_l / pair_y, csrc/kernels.cu
+pair_fold_kernel / pair_unfold_kernel / t2_finalize_smem_kernel<*, true>), restated in numpy on
+the same flat column-major indices, against the plain contractions (no GPU).
+
+With the pair symmetry T[i,j,a,b] = T[j,i,b,a], the ladders' output L, X and CCSD's Y are
+evaluated over occupied pairs p = (i <= j) and virtual pairs q = (a <= b) in a symmetric (+) and
+an antisymmetric (-) part; the unfolded results must equal oovv + W'^T.T + T.vvvv^T,
+oovv.T^T and ooovQ + T.<am|ef> to rounding, on the S25 system's integrals and amplitudes.
+"""
+import numpy as np
+
+from oracle import ccd, ccsd
+from oracle.mp2 import denominators
+from juesgpu.synthetic import make_named
+
+fl = lambda a: np.asarray(a).reshape(-1, order="F")  # noqa: E731
+
+
+def pair_decode(p):
+    """kernels.cu pair_ab: p = b(b+1)/2 + a, a <= b."""
+    p = np.asarray(p, dtype=np.int64)
+    b = ((np.sqrt(8.0 * p + 1.0) - 1.0) * 0.5).astype(np.int64)
+    b = np.where(b * (b + 1) // 2 > p, b - 1, b)
+    b = np.where((b + 1) * (b + 2) // 2 <= p, b + 1, b)
+    return p - b * (b + 1) // 2, b
+
+
+def pair_fold(src, R, rowpair, rd, rs0, rs1, d, ke, kf, scale, diag_half):
+    """pair_fold_kernel: [out+ | out-], out_s[r + R q] for the K pair q = (e <= f)."""
+    nk = d * (d + 1) // 2
+    e, f = pair_decode(np.arange(nk))
+    r = np.arange(R)
+    if rowpair:
+        a, b = pair_decode(r)
+        ro = a * rs0 + b * rs1
+    else:
+        ro = (r % rd) * rs0 + (r // rd) * rs1
+    i1 = ro[:, None] + (e * ke + f * kf)[None, :]
+    i2 = ro[:, None] + (f * ke + e * kf)[None, :]
+    assert min(i1.min(), i2.min()) >= 0 and max(i1.max(), i2.max()) < src.size
+    c = np.where(diag_half & (e == f), 0.5 * scale, scale)[None, :]
+    x, y = src[i1], src[i2]
+    return np.concatenate([fl(c * (x + y)), fl(c * (x - y))])
+
+
+def pair_unfold(P, npc, base, o, C, sij, sc, tp, tc, size):
+    """pair_unfold_kernel: out[(i + o j) sij + c sc] = base + P+ + sgn P- (no P- for i = j)."""
+    ij = np.arange(o * o)
+    i, j = ij % o, ij // o
+    i0, j0 = np.minimum(i, j), np.maximum(i, j)
+    p = j0 * (j0 + 1) // 2 + i0
+    c = np.arange(C)
+    pi = p[:, None] * tp + c[None, :] * tc
+    assert pi.min() >= 0 and (npc + pi).max() < P.size
+    sgn = np.where(i == j, 0.0, np.where(i < j, 1.0, -1.0))[:, None]
+    oi = ij[:, None] * sij + c[None, :] * sc
+    out = np.zeros(size)
+    out[oi] = (base[oi] if base is not None else 0.0) + P[pi] + sgn * P[npc + pi]
+    return out
+
+
+def unfold_ladder(Lpm, o, v):
+    """t2_finalize_smem_kernel's L[i,j,a,b] from [L+ | L-] (block q = (a <= b), column q)."""
+    np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
+    Lp = Lpm[: np_ * nq].reshape(np_, nq, order="F")
+    Lm = Lpm[np_ * nq:].reshape(np_, nq, order="F")
+    L = np.zeros((o, o, v, v))
+    for q in range(nq):
+        a, b = (int(x) for x in pair_decode(q))
+        for i in range(o):
+            for j in range(o):
+                i0, j0 = min(i, j), max(i, j)
+                pij = j0 * (j0 + 1) // 2 + i0
+                lm = 0.0 if (i == j or a == b) else (Lm[pij, q] if i < j else -Lm[pij, q])
+                L[i, j, a, b] = Lp[pij, q] + lm
+                L[i, j, b, a] = Lp[pij, q] - lm
+    return L
+
+
+def gemm_rows(A, B):
+    """C[m, n] = sum_k A[m, k] B[n, k]: gett_tc_views with A and B as row-major-K packs."""
+    return A @ B.T
+
+
+def folded(T, oovv, vvvv, oooo, Wp_extra=None, ovvv=None, ooovQ=None):
+    """pair_begin + pair_x + pair_l (+ pair_y): W', L and Y through the folded contractions."""
+    o, v = T.shape[0], T.shape[2]
+    oo, vv, ov = o * o, v * v, o * v
+    np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
+    blk = lambda a, k, r, c: a[k * r * c:(k + 1) * r * c].reshape(r, c, order="F")  # noqa: E731
+    Bpm = pair_fold(fl(vvvv), nq, True, 0, 1, v, v, vv, vv * v, 0.5, True)
+    Xw = pair_fold(fl(oovv), oo, False, oo, 1, 0, v, oo, oo * v, 0.5, True)
+    Opm = pair_fold(fl(oovv), np_, True, 0, 1, o, v, oo, oo * v, 0.5, False)
+    Apm = pair_fold(fl(T), np_, True, 0, 1, o, v, oo, oo * v, 1.0, False)
+    Xpm = np.concatenate([fl(gemm_rows(blk(Xw, k, oo, nq), blk(Apm, k, np_, nq))) for k in range(2)])
+    Wp = pair_unfold(Xpm, oo * np_, fl(oooo), o, oo, oo, 1, oo, 1, oo * oo).reshape(o, o, o, o, order="F")
+    if Wp_extra is not None:
+        Wp = Wp + Wp_extra
+    Cpm = pair_fold(fl(Wp), np_, True, 0, oo, oo * o, o, 1, o, 0.5, True)
+    Lpm = []
+    for k in range(2):
+        A, C, B = blk(Apm, k, np_, nq), blk(Cpm, k, np_, np_), blk(Bpm, k, nq, nq)
+        Lpm.append(fl(blk(Opm, k, np_, nq) + gemm_rows(np.hstack([C, A]), np.hstack([A.T, B]))))
+    L = unfold_ladder(np.concatenate(Lpm), o, v)
+    Y = None
+    if ovvv is not None:
+        Yw = pair_fold(fl(ovvv), ov, False, v, o, 1, v, ov * v, ov, 0.5, True)
+        Ypm = np.concatenate([fl(gemm_rows(blk(Apm, k, np_, nq), blk(Yw, k, ov, nq))) for k in range(2)])
+        Y = pair_unfold(Ypm, np_ * ov, fl(ooovQ), o, ov, 1, oo, 1, np_, oo * ov).reshape(o, o, v, o, order="F")
+    return Wp, L, Y
+
+
+def test_pair_decode_order():
+    a, b = pair_decode(np.arange(66))
+    want = [(x, y) for y in range(11) for x in range(y + 1)]
+    assert list(zip(a.tolist(), b.tolist())) == want
+
+
+def test_folded_ladders_equal_plain_ccd():
+    s = make_named("S25")
+    w = s.wfn()
+    oovv, ovov, ovvo, oooo, vvvv = ccd.make_rccd_integrals(w)
+    D = denominators(w.epsa, w.nalpha)
+    T = ccd.jl_cciter(oovv / D, oovv, vvvv, oooo, ovov, ovvo, D)   # pair-symmetric, not a fixed point
+    assert np.abs(T - T.transpose(1, 0, 3, 2)).max() < 1e-14
+    o = T.shape[0]
+    # any pair-symmetric addition to W' (the Fmi terms of wp_fmi are one)
+    rng = np.random.default_rng(3)
+    S = 1e-2 * rng.standard_normal((o, o, o, o))
+    Sx = S + S.transpose(1, 0, 3, 2)
+    Wp, L, _ = folded(T, oovv, vvvv, oooo, Wp_extra=Sx)
+    X = np.einsum("mnef,ijef->mnij", oovv, T)
+    assert np.abs(Wp - (oooo + X + Sx)).max() < 1e-13 * max(1.0, np.abs(Wp).max())
+    Lp = oovv + np.einsum("mnij,mnab->ijab", oooo + X + Sx, T) + np.einsum("ijef,abef->ijab", T, vvvv)
+    assert np.abs(L - Lp).max() < 1e-13 * max(1.0, np.abs(Lp).max())
+
+
+def test_folded_y_equals_plain_ccsd():
+    s = make_named("S25")
+    w = s.wfn()
+    oooo, _, oovv, _, ovvv, vvvv = ccsd.make_rccsd_integrals(w)
+    o, v = oovv.shape[0], oovv.shape[2]
+    rng = np.random.default_rng(5)
+    R = 1e-2 * rng.standard_normal((o, o, v, v))
+    t1 = 1e-2 * rng.standard_normal((o, v))
+    Ttau = R + R.transpose(1, 0, 3, 2) + np.einsum("ia,jb->ijab", t1, t1)   # T2 + tau: pair-symmetric
+    ooovQ = rng.standard_normal((o, o, v, o))
+    _, L, Y = folded(Ttau, oovv, vvvv, oooo, ovvv=ovvv, ooovQ=ooovQ)
+    Yp = ooovQ + np.einsum("ijef,mafe->ijam", Ttau, ovvv)
+    assert np.abs(Y - Yp).max() < 1e-13 * max(1.0, np.abs(Yp).max())
+    X = np.einsum("mnef,ijef->mnij", oovv, Ttau)
+    Lp = oovv + np.einsum("mnij,mnab->ijab", oooo + X, Ttau) + np.einsum("ijef,abef->ijab", Ttau, vvvv)
+    assert np.abs(L - Lp).max() < 1e-13 * max(1.0, np.abs(Lp).max())
