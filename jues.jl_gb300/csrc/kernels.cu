@@ -171,6 +171,15 @@ __device__ __forceinline__ void pair_ab(long long p, int &a, int &b) {
     a = (int)(p - bb * (bb + 1) / 2);
 }
 
+// the same for p < 2^26 in FP32 and 32-bit integers (the FP64 square root is slow on this part)
+__device__ __forceinline__ void pair_ab32(int p, int &a, int &b) {
+    int bb = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+    while (bb * (bb + 1) / 2 > p) --bb;
+    while ((bb + 1) * (bb + 2) / 2 <= p) ++bb;
+    b = bb;
+    a = p - bb * (bb + 1) / 2;
+}
+
 // MP2: each (a<=b) pair block reads K[:,:,a,b] and K[:,:,b,a] once.
 __global__ void mp2_kernel(const double *__restrict__ K, const double *__restrict__ eps, int o, int v,
                            double *part) {
@@ -278,13 +287,8 @@ __global__ void t2_finalize_kernel(const double *__restrict__ L, const double *_
 // pair (a <= b) (one pair per block, so resident blocks overlap their load and compute phases);
 // Z[:,:,a,b] and Z[:,:,b,a] are contiguous o x o blocks, loaded coalesced into shared memory on
 // an odd row pitch (conflict-free transposed reads), so every global access is unit-stride.
-// Dynamic shared memory 2 o pitch doubles (o <= 64), + 4 o with the rank-one term, + 2 np with
-// PAIRL: then L holds the folded ladders [L+ | L-], each np x nq (np = o(o+1)/2 pairs i <= j, nq =
-// v(v+1)/2 pairs a <= b, pair index j(j+1)/2 + i), with
-//   L[i,j,a,b] = L+[(i,j),(a,b)] + L-[(i,j),(a,b)] (i <= j, a <= b), L[i,j,b,a] = L+ - L-,
-//   L[j,i,b,a] = L[i,j,a,b], and L- taken as zero for i = j or a = b;
-// block (a <= b) reads column p = blockIdx.x of each.
-template <bool RANK1, bool PAIRL>
+// Dynamic shared memory 2 o pitch doubles (o <= 64), + 4 o with the rank-one term.
+template <bool RANK1>
 __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(const double *__restrict__ L,
                                                                const double *__restrict__ Z,
                                                                const double *__restrict__ invD, int o, int v,
@@ -299,7 +303,7 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
     const int ooi = o * o;
     double acc = 0.0;
     int a, b;
-    pair_ab(blockIdx.x, a, b);   // one (a <= b) pair per block: resident blocks overlap their phases
+    pair_ab32((int)blockIdx.x, a, b);   // one (a <= b) pair per block: resident blocks overlap their phases
     const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
     double *r1v = zs + 2 * o * pitch;
     if (RANK1)
@@ -308,16 +312,6 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             r1v[k] = w == 0 ? t1[i + (long long)o * a] : w == 1 ? t1[i + (long long)o * b]
                    : w == 2 ? q[a + (long long)v * i] : q[b + (long long)v * i];
         }
-    const int np = o * (o + 1) / 2;
-    double *ls = r1v + (RANK1 ? 4 * o : 0);   // PAIRL: [L+ column | L- column], np each
-    if (PAIRL) {
-        const long long nq = (long long)v * (v + 1) / 2;
-        const double *lp = L + (long long)np * blockIdx.x, *lm = lp + (long long)np * nq;
-        for (int k = threadIdx.x; k < np; k += blockDim.x) {
-            ls[k] = lp[k];
-            ls[np + k] = lm[k];
-        }
-    }
     {
         for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
             const int i = ij % o, j = ij / o;
@@ -330,18 +324,8 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             // Z_ab[i,j] and Z_ba[j,i]; Z_ba[i,j] and Z_ab[j,i]
             const double zab = zs[j + pitch * i], zba_t = zs[o * pitch + i + pitch * j];
             const double inv = invD[ab + ij];   // D is symmetric in (a, b)
-            double lab, lba = 0.0;
-            if (PAIRL) {
-                const int i0 = min(i, j), j0 = max(i, j), pij = j0 * (j0 + 1) / 2 + i0;
-                const double lpv = ls[pij];
-                const double lmv = (i == j || a == b) ? 0.0 : (i < j ? ls[np + pij] : -ls[np + pij]);
-                lab = lpv + lmv;
-                lba = lpv - lmv;
-            } else {
-                lab = L[ab + ij];
-            }
-            // Z's two terms first: T[j,i,b,a] sums the same three numbers in the same order
-            double x = lab + (zab + zba_t);
+            // Z's two terms first, as the folded form sums them
+            double x = L[ab + ij] + (zab + zba_t);
             // C[i,j,a,b] + C[j,i,b,a] = t1[i,a] q[b,j] + t1[j,b] q[a,i]
             if (RANK1) x += r1v[i] * r1v[3 * o + j] + r1v[o + j] * r1v[2 * o + i];
             x *= inv;
@@ -349,7 +333,7 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
             if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
             if (a != b) {
                 const double zba = zs[o * pitch + j + pitch * i], zab_t = zs[i + pitch * j];
-                double y = (PAIRL ? lba : L[ba + ij]) + (zba + zab_t);
+                double y = L[ba + ij] + (zba + zab_t);
                 if (RANK1) y += r1v[o + i] * r1v[2 * o + j] + r1v[j] * r1v[3 * o + i];
                 y *= inv;
                 Tn[ba + ij] = y;
@@ -361,6 +345,80 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+
+// The finalisation from the folded ladders L = [L+ | L-] (np x nq each, np = o(o+1)/2 occupied
+// pairs (i <= j), nq = v(v+1)/2 virtual pairs, pair index j(j+1)/2 + i; column q = the block's
+// pair (a <= b)).  The result is pair-symmetric, Tn[i,j,a,b] = Tn[j,i,b,a], so an occupied pair
+// (i0 <= j0) has two values,
+//   u = (L+ + L-) + (Z_ab[i0,j0] + Z_ba[j0,i0])   -> Tn[i0,j0,a,b] and Tn[j0,i0,b,a]
+//   w = (L+ - L-) + (Z_ab[j0,i0] + Z_ba[i0,j0])   -> Tn[j0,i0,a,b] and Tn[i0,j0,b,a]
+// (L- = 0 for i0 = j0 or a = b; with RANK1 the rank-one pair terms at (i0,j0) and (j0,i0) too).
+// One thread forms both from the four Z elements that it alone reads and writes them back over
+// those elements in shared memory; the block then multiplies by 1/D and stores Tn coalesced.
+template <bool RANK1>
+__global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_fold_kernel(const double *__restrict__ L,
+                                                               const double *__restrict__ Z,
+                                                               const double *__restrict__ invD, int o, int v,
+                                                               const double *__restrict__ Told,
+                                                               double *__restrict__ Tn, double *part,
+                                                               const double *__restrict__ t1,
+                                                               const double *__restrict__ q) {
+    extern __shared__ double zs[];   // Z_ab then Z_ba, element (i, j) at j + pitch i; then 4 o (RANK1)
+    const int pitch = o | 1;
+    const long long oo = (long long)o * o;
+    const int ooi = o * o, np = o * (o + 1) / 2;
+    const long long nq = (long long)v * (v + 1) / 2;
+    double acc = 0.0;
+    int a, b;
+    pair_ab32((int)blockIdx.x, a, b);
+    const long long ab = oo * (a + (long long)v * b), ba = oo * (b + (long long)v * a);
+    double *za = zs, *zb = zs + o * pitch, *r1v = zs + 2 * o * pitch;
+    if (RANK1)
+        for (int k = threadIdx.x; k < 4 * o; k += blockDim.x) {
+            const int w = k / o, i = k % o;
+            r1v[k] = w == 0 ? t1[i + (long long)o * a] : w == 1 ? t1[i + (long long)o * b]
+                   : w == 2 ? q[a + (long long)v * i] : q[b + (long long)v * i];
+        }
+    for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
+        const int i = ij % o, j = ij / o;
+        za[j + pitch * i] = Z[ab + ij];
+        zb[j + pitch * i] = Z[ba + ij];
+    }
+    __syncthreads();
+    const double *lp = L + (long long)np * blockIdx.x, *lm = lp + (long long)np * nq;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+        int i0, j0;
+        pair_ab32(p, i0, j0);
+        const double lpv = lp[p], lmv = (i0 == j0 || a == b) ? 0.0 : lm[p];
+        const int x1 = j0 + pitch * i0, x2 = i0 + pitch * j0;   // (i0, j0) and (j0, i0)
+        double u = (lpv + lmv) + (za[x1] + zb[x2]);
+        double w = (lpv - lmv) + (za[x2] + zb[x1]);
+        if (RANK1) {
+            // C[i,j,a,b] + C[j,i,b,a] = t1[i,a] q[b,j] + t1[j,b] q[a,i]
+            u += r1v[i0] * r1v[3 * o + j0] + r1v[o + j0] * r1v[2 * o + i0];
+            w += r1v[j0] * r1v[3 * o + i0] + r1v[o + i0] * r1v[2 * o + j0];
+        }
+        za[x1] = u;
+        zb[x2] = u;
+        za[x2] = w;
+        zb[x1] = w;
+    }
+    __syncthreads();
+    for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
+        const int i = ij % o, j = ij / o;
+        const double inv = invD[ab + ij];   // D is symmetric in (a, b)
+        const double x = za[j + pitch * i] * inv;
+        Tn[ab + ij] = x;
+        if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
+        if (a != b) {
+            const double y = zb[j + pitch * i] * inv;
+            Tn[ba + ij] = y;
+            if (Told) { const double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
+        }
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
 
 // Folding of a pair-symmetric contraction (the ladders, X, Y).  For an index pair (e, f) of
 // extent d, q = f(f+1)/2 + e (e <= f) numbers the d(d+1)/2 pairs.  Block q writes, for every row
@@ -375,7 +433,7 @@ __global__ void __launch_bounds__(256) pair_fold_kernel(const double *__restrict
                                                         long long kf, long long nk, double scale, int diag_half,
                                                         double *__restrict__ out) {
     int e, f;
-    pair_ab(blockIdx.x, e, f);
+    pair_ab32((int)blockIdx.x, e, f);
     const long long k1 = e * ke + f * kf, k2 = f * ke + e * kf;
     const double c = (diag_half && e == f) ? 0.5 * scale : scale;
     double *op = out + R * (long long)blockIdx.x, *om = op + R * nk;
@@ -383,7 +441,7 @@ __global__ void __launch_bounds__(256) pair_fold_kernel(const double *__restrict
         long long ro;
         if (rowpair) {
             int a, b;
-            pair_ab(r, a, b);
+            pair_ab32((int)r, a, b);
             ro = a * rs0 + b * rs1;
         } else {
             long long r1, r0;
@@ -987,27 +1045,26 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
         Ctx::Scope s(ctx, "t2_finalize");
         // one block per pair; the step norm's partials (one per block) must fit the reduction scratch
         if (t2_finalize_folds(o, v)) {
-            const size_t smem =
-                ((size_t)2 * o * (o | 1) + (t1 ? 4 * o : 0) + (pairl ? (size_t)o * (o + 1) : 0)) * sizeof(double);
+            const size_t smem = ((size_t)2 * o * (o | 1) + (t1 ? 4 * o : 0)) * sizeof(double);
             // the rank-one term is a template parameter: without it the kernel fits 32 registers
             // and eight blocks per SM
             static std::atomic<unsigned long long> attr_set{0};
             const unsigned long long bit = ctx->device >= 0 && ctx->device < 64 ? 1ull << ctx->device : 0ull;
             if (smem > 48 * 1024 && (!bit || !(attr_set.load() & bit))) {
-                const int most = (2 * 64 * 65 + 4 * 64 + 64 * 65) * 8;   // o = 64, rank-one term, folded L
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false, false>,
+                const int most = (2 * 64 * 65 + 4 * 64) * 8;   // o = 64 with the rank-one term
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, most));
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true, false>,
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, most));
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<false, true>,
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_fold_kernel<false>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, most));
-                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_smem_kernel<true, true>,
+                JUES_CHECK_CUDA(cudaFuncSetAttribute(t2_finalize_fold_kernel<true>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, most));
                 attr_set.fetch_or(bit);
             }
             nb = (int)npair;
-            auto kern = t1 ? (pairl ? t2_finalize_smem_kernel<true, true> : t2_finalize_smem_kernel<true, false>)
-                           : (pairl ? t2_finalize_smem_kernel<false, true> : t2_finalize_smem_kernel<false, false>);
+            auto kern = t1 ? (pairl ? t2_finalize_fold_kernel<true> : t2_finalize_smem_kernel<true>)
+                           : (pairl ? t2_finalize_fold_kernel<false> : t2_finalize_smem_kernel<false>);
             kern<<<nb, RED_THREADS, smem, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red, t1, q);
         } else {
             t2_finalize_kernel<<<nb, RED_THREADS, 0, ctx->stream>>>(L, Z, invD, o, v, Told, Tn, ctx->d_red, t1, q);
@@ -1021,7 +1078,7 @@ double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *inv
 void pair_fold(Ctx *ctx, const double *src, long long R, bool rowpair, long long rd, long long rs0, long long rs1,
                int d, long long ke, long long kf, double scale, bool diag_half, double *out) {
     const long long nk = (long long)d * (d + 1) / 2;
-    JUES_REQUIRE(d > 0 && R > 0 && nk < (1LL << 31), "pair_fold: bad extents");
+    JUES_REQUIRE(d > 0 && R > 0 && nk < (1LL << 26) && (!rowpair || R < (1LL << 26)), "pair_fold: bad extents");
     Ctx::Scope s(ctx, "pair_fold");
     pair_fold_kernel<<<(unsigned)nk, 256, 0, ctx->stream>>>(src, R, rowpair ? 1 : 0, rd, rs0, rs1, ke, kf, nk, scale,
                                                             diag_half ? 1 : 0, out);

@@ -151,3 +151,68 @@ def test_folded_y_equals_plain_ccsd():
     X = np.einsum("mnef,ijef->mnij", oovv, Ttau)
     Lp = oovv + np.einsum("mnij,mnab->ijab", oooo + X, Ttau) + np.einsum("ijef,abef->ijab", Ttau, vvvv)
     assert np.abs(L - Lp).max() < 1e-13 * max(1.0, np.abs(Lp).max())
+
+
+def pair_decode32(p):
+    """kernels.cu pair_ab32: the FP32 square root, then the integer correction."""
+    p = np.asarray(p, dtype=np.int64)
+    b = ((np.sqrt(np.float32(8.0) * p.astype(np.float32) + np.float32(1.0)) - np.float32(1.0))
+         * np.float32(0.5)).astype(np.int64)
+    for _ in range(2):
+        b = np.where(b * (b + 1) // 2 > p, b - 1, b)
+        b = np.where((b + 1) * (b + 2) // 2 <= p, b + 1, b)
+    return p - b * (b + 1) // 2, b
+
+
+def test_pair_decode32_exact():
+    p = np.arange(1 << 20)
+    a, b = pair_decode32(p)
+    assert np.all((a >= 0) & (a <= b) & (b * (b + 1) // 2 + a == p))
+    a2, b2 = pair_decode(p)
+    assert np.array_equal(a, a2) and np.array_equal(b, b2)
+
+
+def finalize_fold(Lpm, Z, invD, o, v):
+    """t2_finalize_fold_kernel: per block (a <= b), Z_ab and Z_ba staged, each pair (i0 <= j0)
+    forms u and w over its four Z elements, then Tn = staged * 1/D."""
+    np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
+    Zf, inv = fl(Z), fl(invD)
+    Tn = np.zeros(o * o * v * v)
+    oo = o * o
+    for q in range(nq):
+        a, b = (int(x) for x in pair_decode(q))
+        ab, ba = oo * (a + v * b), oo * (b + v * a)
+        za = Zf[ab:ab + oo].reshape(o, o, order="F").copy()   # za[i, j] = Z[i,j,a,b]
+        zb = Zf[ba:ba + oo].reshape(o, o, order="F").copy()
+        lp, lm = Lpm[np_ * q:np_ * q + np_], Lpm[np_ * nq + np_ * q:np_ * nq + np_ * q + np_]
+        for p in range(np_):
+            i0, j0 = (int(x) for x in pair_decode32(p))
+            lpv, lmv = lp[p], (0.0 if (i0 == j0 or a == b) else lm[p])
+            u = (lpv + lmv) + (za[i0, j0] + zb[j0, i0])
+            w = (lpv - lmv) + (za[j0, i0] + zb[i0, j0])
+            za[i0, j0] = u
+            zb[j0, i0] = u
+            za[j0, i0] = w
+            zb[i0, j0] = w
+        Tn[ab:ab + oo] = fl(za) * inv[ab:ab + oo]
+        if a != b:
+            Tn[ba:ba + oo] = fl(zb) * inv[ab:ab + oo]
+    return Tn.reshape(o, o, v, v, order="F")
+
+
+def test_folded_finalisation_equals_plain():
+    rng = np.random.default_rng(7)
+    o, v = 4, 6
+    R = rng.standard_normal((o, o, v, v))
+    L = R + R.transpose(1, 0, 3, 2)                       # a pair-symmetric ladder output
+    Z = rng.standard_normal((o, o, v, v))                 # any Z
+    e = np.sort(rng.standard_normal(o + v))
+    D = e[:o, None, None, None] + e[None, :o, None, None] - e[None, None, o:, None] - e[None, None, None, o:]
+    invD = 1.0 / D
+    np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
+    # [L+ | L-]: L_s[p, q] = 1/2 (L[i,j,a,b] + s L[i,j,b,a])
+    Lpm = pair_fold(fl(L), np_, True, 0, 1, o, v, o * o, o * o * v, 0.5, False)
+    Tn = finalize_fold(Lpm, Z, invD, o, v)
+    want = (L + Z + Z.transpose(1, 0, 3, 2)) * invD
+    assert np.abs(Tn - want).max() < 1e-13 * np.abs(want).max()
+    assert np.array_equal(Tn, Tn.transpose(1, 0, 3, 2))   # pair-symmetric to the bit
