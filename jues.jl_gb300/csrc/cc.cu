@@ -158,6 +158,8 @@ static void pair_begin(CCState *s) {
     s->Lpm = DBuf<double>(ctx, (size_t)(2 * np * nq));
     s->Cpm = DBuf<double>(ctx, (size_t)(2 * np * np));
     s->Xpm = DBuf<double>(ctx, (size_t)(2 * oo * np));
+    s->invF = DBuf<double>(ctx, (size_t)(np * nq));
+    inv_denominators_folded(ctx, s->eps.p, (int)o, (int)v, s->invF.p);
     for (int k = 0; k < 2; ++k) s->stackPA[k].ensure(ctx, np, kp + kq, 2);
 }
 
@@ -363,12 +365,12 @@ double ccd_sweep(CCState *s, int prec) {
     s->cache_operands = false;
     // with DIIS the step norm comes from its error vector (the same |Tn - T|^2), so the
     // finalisation skips it: two of its five FP64 operations per element
-    const double *Lf = pairl ? s->Lpm.p : s->L.p;
+    const double *Lf = pairl ? s->Lpm.p : s->L.p, *Df = pairl ? s->invF.p : s->invD.p;
     if (s->opts.diis) {
-        t2_finalize(ctx, Lf, Z, s->invD.p, (int)o, (int)v, nullptr, s->Tn.p, nullptr, nullptr, pairl);
+        t2_finalize(ctx, Lf, Z, Df, (int)o, (int)v, nullptr, s->Tn.p, nullptr, nullptr, pairl);
         return -1.0;
     }
-    return t2_finalize(ctx, Lf, Z, s->invD.p, (int)o, (int)v, T, s->Tn.p, nullptr, nullptr, pairl);
+    return t2_finalize(ctx, Lf, Z, Df, (int)o, (int)v, T, s->Tn.p, nullptr, nullptr, pairl);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -997,7 +999,17 @@ double ccsd_sweep(CCState *s, int prec) {
     G(s, prec, "ccsd_t1", o, v, o, -1.0, s->Fmi.p, plain(o), plain(1), t1, plain(1), plain(o),
       1.0, R1, plain(1), plain(o));
     // Fme[m,e] (2 T2[i,m,a,e] - T2[m,i,a,e]), one read of T2
-    t1_fme(ctx, T, s->Fme.p, (int)o, (int)v, R1);
+    if (stacked) {
+        // sum_me (2 T2[i,m,a,e] - T2[m,i,a,e]) Fme[m,e] = [R1 | R23] . [2 Fme ; -Fme] on the ring packs
+        const long long kb = (ov + 127) / 128 * 128;
+        s->stackF.ensure(ctx, 1, 2 * kb, 2);
+        pack_stacked(ctx, s->stackF, 0, s->Fme.p, plain(0), plain(1), 1, ov, 2.0);
+        pack_stacked(ctx, s->stackF, kb, s->Fme.p, plain(0), plain(1), 1, ov, -1.0);
+        gett_tc_views(ctx, s->stackT.view(kb, 2 * kb), s->stackF.view(0, 2 * kb), ov, 1, 1.0, 1.0, R1, plain(1),
+                      plain(ov), nullptr, "ccsd_t1");
+    } else {
+        t1_fme(ctx, T, s->Fme.p, (int)o, (int)v, R1);
+    }
     // t1[m,e] (2 <im|ae> - <ma|ie>) through M1, formed once
     G(s, prec, "ccsd_t1", ov, 1, ov, 1.0, s->M1.p, plain(1), plain(ov), t1, plain(1), plain(0), 1.0, R1, plain(1),
       plain(0), nullptr, true, false);
@@ -1049,8 +1061,8 @@ double ccsd_sweep(CCState *s, int prec) {
     // with DIIS the step norm comes from its error vector over [t1 | T2] (the same squared sum), so
     // the finalisation skips it unless the per-block norms are wanted (AutoRCCSD's rms)
     const bool norms = !s->opts.diis || s->auto_rms;
-    double r2 = t2_finalize(ctx, pairl ? s->Lpm.p : s->L.p, Z, s->invD.p, (int)o, (int)v, norms ? T : nullptr,
-                            s->Tn.p, stacked ? nullptr : t1, stacked ? nullptr : q, pairl);
+    double r2 = t2_finalize(ctx, pairl ? s->Lpm.p : s->L.p, Z, pairl ? s->invF.p : s->invD.p, (int)o, (int)v,
+                            norms ? T : nullptr, s->Tn.p, stacked ? nullptr : t1, stacked ? nullptr : q, pairl);
     // t1n = R1 / D_ia and its step norm
     const double r1 = t1_finalize(ctx, R1, s->eps.p, (int)o, (int)v, norms ? t1 : nullptr);
     if (!norms) return -1.0;

@@ -52,9 +52,12 @@ struct CCState {
     // their contracted pair at 1/2 (1/4 on its diagonal), and O_s = 1/2 oovv folded over (a, b).
     // stackPA[s] = [C_s | A_s] (rows p), stackPB[s] = [A_s^T | B_s] (rows q, B_s packed once),
     // stackPX[s] = Xw_s (rows (m,n)), stackPY[s] = Yw_s (rows (a,m)).
-    bool pairl = false;
     DBuf<double> Apm, Cpm, Lpm, Opm, Xpm, Ypm;
+    DBuf<double> invF;           // the folded 1/D, np x nq (the finalisation of the folded form)
     StackedPack stackPA[2], stackPB[2], stackPX[2], stackPY[2];
+    // CCSD, split precision: [2 Fme | -Fme] (one row, K = the ring blocks R1 and R23 of stackT),
+    // so T1's T2.Fme terms are one GEMM on T2's ring packs
+    StackedPack stackF;
     // DIIS (FP64): amplitude vectors and their errors, ring buffer of diis_size-1 pairs
     std::vector<DBuf<double>> dv, de;
     std::vector<std::vector<double>> gram;   // gram[k][l] = e_k . e_l, k,l in insertion order

@@ -281,6 +281,7 @@ double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t
 // T2 finalisation: Tn[i,j,a,b] = (L + Z[i,j,a,b] + Z[j,i,b,a] + C[i,j,a,b] + C[j,i,b,a]) invD
 // with C[i,j,a,b] = t1[i,a] q[b,j] when t1 and q (v x o) are given; returns ||Tn - Told||^2 if
 // Told != nullptr.  Writes Tn.
+// with pairl, L = [L+ | L-] (the folded ladders) and invD the folded 1/D (inv_denominators_folded)
 double t2_finalize(Ctx *ctx, const double *L, const double *Z, const double *invD, int o, int v,
                    const double *Told, double *Tn, const double *t1 = nullptr, const double *q = nullptr,
                    bool pairl = false);
@@ -295,6 +296,8 @@ void pair_unfold(Ctx *ctx, const double *P, long long npc, const double *base, i
                  long long sc, long long tp, long long tc, bool ijfast, double *out);
 // invD[i,j,a,b] = 1 / (e_i + e_j - e_a - e_b)
 void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out);
+// the same over occupied pairs p = (i <= j) and virtual pairs q = (a <= b): out[p + np q]
+void inv_denominators_folded(Ctx *ctx, const double *eps, int o, int v, double *out);
 // t1n[i,a] /= (e_i - e_a) in place; returns ||t1n - t1old||^2
 double t1_finalize(Ctx *ctx, double *t1n, const double *eps, int o, int v, const double *t1old);
 // X[i,j,a,b] = (L[...]) / D in place variants used for guesses

@@ -244,6 +244,20 @@ __global__ void inv_denominators_kernel(const double *__restrict__ eps, int o, i
     }
 }
 
+// the same over the pairs: out[p + np q] = 1/D[i0,j0,a,b] for p = (i0 <= j0), q = (a <= b), with
+// the sums in inv_denominators_kernel's order (so equal to its entry at (i0,j0,a,b) to the bit)
+__global__ void inv_denominators_folded_kernel(const double *__restrict__ eps, int o, int v, double *__restrict__ out) {
+    const int np = o * (o + 1) / 2;
+    const long long n = (long long)np * v * (v + 1) / 2;
+    for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+         x += (long long)gridDim.x * blockDim.x) {
+        int i, j, a, b;
+        pair_ab32((int)(x % np), i, j);
+        pair_ab32((int)(x / np), a, b);
+        out[x] = 1.0 / (eps[i] + eps[j] - eps[o + a] - eps[o + b]);
+    }
+}
+
 // Tn[i,j,a,b] = (L[i,j,a,b] + Z[i,j,a,b] + Z[j,i,b,a] + C[i,j,a,b] + C[j,i,b,a]) / D with the
 // optional rank-one C[i,j,a,b] = t1[i,a] q[b,j] (t1 o x v, q v x o), and the squared step norm.
 __device__ __forceinline__ double rank1_pair(const double *__restrict__ t1, const double *__restrict__ q, int o,
@@ -353,12 +367,14 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_smem_kernel(co
 //   u = (L+ + L-) + (Z_ab[i0,j0] + Z_ba[j0,i0])   -> Tn[i0,j0,a,b] and Tn[j0,i0,b,a]
 //   w = (L+ - L-) + (Z_ab[j0,i0] + Z_ba[i0,j0])   -> Tn[j0,i0,a,b] and Tn[i0,j0,b,a]
 // (L- = 0 for i0 = j0 or a = b; with RANK1 the rank-one pair terms at (i0,j0) and (j0,i0) too).
-// One thread forms both from the four Z elements that it alone reads and writes them back over
-// those elements in shared memory; the block then multiplies by 1/D and stores Tn coalesced.
+// All four share one denominator, invF[p + np q] = 1/D[i0,j0,a,b] (the folded 1/D).  One thread
+// forms u/D and w/D from the four Z elements that it alone reads and writes them back over those
+// elements in shared memory; the block then stores Tn coalesced.  Two FP64 operations per element
+// of Tn (FP64 issue, at about 0.6e12 operations/s, bounds this kernel with the memory traffic).
 template <bool RANK1>
 __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_fold_kernel(const double *__restrict__ L,
                                                                const double *__restrict__ Z,
-                                                               const double *__restrict__ invD, int o, int v,
+                                                               const double *__restrict__ invF, int o, int v,
                                                                const double *__restrict__ Told,
                                                                double *__restrict__ Tn, double *part,
                                                                const double *__restrict__ t1,
@@ -398,6 +414,9 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_fold_kernel(co
             u += r1v[i0] * r1v[3 * o + j0] + r1v[o + j0] * r1v[2 * o + i0];
             w += r1v[j0] * r1v[3 * o + i0] + r1v[o + i0] * r1v[2 * o + j0];
         }
+        const double inv = invF[p + (long long)np * blockIdx.x];
+        u *= inv;
+        w *= inv;
         za[x1] = u;
         zb[x2] = u;
         za[x2] = w;
@@ -406,12 +425,11 @@ __global__ void __launch_bounds__(256, RANK1 ? 6 : 8) t2_finalize_fold_kernel(co
     __syncthreads();
     for (int ij = threadIdx.x; ij < ooi; ij += blockDim.x) {
         const int i = ij % o, j = ij / o;
-        const double inv = invD[ab + ij];   // D is symmetric in (a, b)
-        const double x = za[j + pitch * i] * inv;
+        const double x = za[j + pitch * i];
         Tn[ab + ij] = x;
         if (Told) { const double d = x - Told[ab + ij]; acc = fma(d, d, acc); }
         if (a != b) {
-            const double y = zb[j + pitch * i] * inv;
+            const double y = zb[j + pitch * i];
             Tn[ba + ij] = y;
             if (Told) { const double d = y - Told[ba + ij]; acc = fma(d, d, acc); }
         }
@@ -449,8 +467,13 @@ __global__ void __launch_bounds__(256) pair_fold_kernel(const double *__restrict
             ro = r0 * rs0 + r1 * rs1;
         }
         const double x = src[ro + k1], y = src[ro + k2];
-        op[r] = c * (x + y);
-        om[r] = c * (x - y);
+        if (c == 1.0) {   // FP64 issue, not memory, paces this kernel: one operation per output
+            op[r] = x + y;
+            om[r] = x - y;
+        } else {
+            op[r] = c * (x + y);
+            om[r] = c * (x - y);
+        }
     }
 }
 
@@ -1024,6 +1047,14 @@ double cc_energy(Ctx *ctx, const double *oovv, const double *T2, const double *t
         JUES_CHECK_CUDA(cudaGetLastError());
     }
     return finish_reduce(ctx, nb);
+}
+
+void inv_denominators_folded(Ctx *ctx, const double *eps, int o, int v, double *out) {
+    const long long n = (long long)o * (o + 1) / 2 * ((long long)v * (v + 1) / 2);
+    JUES_REQUIRE(o * (o + 1) / 2 < (1 << 26) && (long long)v * (v + 1) / 2 < (1LL << 26), "folded 1/D: too large");
+    Ctx::Scope s(ctx, "inv_denominators");
+    inv_denominators_folded_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(eps, o, v, out);
+    JUES_CHECK_CUDA(cudaGetLastError());
 }
 
 void inv_denominators(Ctx *ctx, const double *eps, int o, int v, double *out) {

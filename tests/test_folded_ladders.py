@@ -172,11 +172,20 @@ def test_pair_decode32_exact():
     assert np.array_equal(a, a2) and np.array_equal(b, b2)
 
 
-def finalize_fold(Lpm, Z, invD, o, v):
-    """t2_finalize_fold_kernel: per block (a <= b), Z_ab and Z_ba staged, each pair (i0 <= j0)
-    forms u and w over its four Z elements, then Tn = staged * 1/D."""
+def inv_folded(e, o, v):
+    """inv_denominators_folded_kernel: 1/D[i0,j0,a,b] at p + np q, sums in the same order."""
     np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
-    Zf, inv = fl(Z), fl(invD)
+    x = np.arange(np_ * nq)
+    i, j = pair_decode32(x % np_)
+    a, b = pair_decode32(x // np_)
+    return 1.0 / (e[i] + e[j] - e[o + a] - e[o + b])
+
+
+def finalize_fold(Lpm, Z, invF, o, v):
+    """t2_finalize_fold_kernel: per block (a <= b), Z_ab and Z_ba staged, each pair (i0 <= j0)
+    forms u/D and w/D over its four Z elements, then Tn = the staged values."""
+    np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
+    Zf = fl(Z)
     Tn = np.zeros(o * o * v * v)
     oo = o * o
     for q in range(nq):
@@ -188,15 +197,16 @@ def finalize_fold(Lpm, Z, invD, o, v):
         for p in range(np_):
             i0, j0 = (int(x) for x in pair_decode32(p))
             lpv, lmv = lp[p], (0.0 if (i0 == j0 or a == b) else lm[p])
-            u = (lpv + lmv) + (za[i0, j0] + zb[j0, i0])
-            w = (lpv - lmv) + (za[j0, i0] + zb[i0, j0])
+            inv = invF[p + np_ * q]
+            u = ((lpv + lmv) + (za[i0, j0] + zb[j0, i0])) * inv
+            w = ((lpv - lmv) + (za[j0, i0] + zb[i0, j0])) * inv
             za[i0, j0] = u
             zb[j0, i0] = u
             za[j0, i0] = w
             zb[i0, j0] = w
-        Tn[ab:ab + oo] = fl(za) * inv[ab:ab + oo]
+        Tn[ab:ab + oo] = fl(za)
         if a != b:
-            Tn[ba:ba + oo] = fl(zb) * inv[ab:ab + oo]
+            Tn[ba:ba + oo] = fl(zb)
     return Tn.reshape(o, o, v, v, order="F")
 
 
@@ -209,10 +219,13 @@ def test_folded_finalisation_equals_plain():
     e = np.sort(rng.standard_normal(o + v))
     D = e[:o, None, None, None] + e[None, :o, None, None] - e[None, None, o:, None] - e[None, None, None, o:]
     invD = 1.0 / D
+    invF = inv_folded(e, o, v)
+    i, j = np.triu_indices(o)
+    assert np.array_equal(np.sort(invF[:o * (o + 1) // 2]), np.sort(invD[i, j, 0, 0]))
     np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
     # [L+ | L-]: L_s[p, q] = 1/2 (L[i,j,a,b] + s L[i,j,b,a])
     Lpm = pair_fold(fl(L), np_, True, 0, 1, o, v, o * o, o * o * v, 0.5, False)
-    Tn = finalize_fold(Lpm, Z, invD, o, v)
+    Tn = finalize_fold(Lpm, Z, invF, o, v)
     want = (L + Z + Z.transpose(1, 0, 3, 2)) * invD
     assert np.abs(Tn - want).max() < 1e-13 * np.abs(want).max()
     assert np.array_equal(Tn, Tn.transpose(1, 0, 3, 2))   # pair-symmetric to the bit
