@@ -467,14 +467,29 @@ static void diis_finish(CCState *s, double *x, int slot, size_t len, const std::
     lincomb(ctx, len, m, vecs.data(), c.data(), x);
 }
 
-// x = vector fed into the sweep, xn = sweep output (both length len, device); on return x holds
-// the extrapolated vector and *ee = |xn - x|^2.
-static void diis_step(CCState *s, double *x, const double *xn, size_t len, double *ee = nullptr) {
-    std::vector<const double *> olds;
-    const int slot = diis_begin(s, len, olds);
-    // the new pair and its overlaps with the stored errors, in one pass
+// The sweep's output buffer (CCD: Tn; CCSD: Xn = [t1n | pad | Tn]) and the DIIS slot's amplitude
+// buffer trade places, so that the sweep writes straight into the slot that keeps its output:
+// called once before the sweep and once after it.  CCSD's views are re-pointed and its pad kept
+// zero (it is part of the DIIS vector).
+static void diis_swap_output(CCState *s, int slot) {
+    if (s->method == 0) {
+        std::swap(s->Tn, s->dv[slot]);
+        return;
+    }
+    const size_t ov = (size_t)s->o * s->v, t2n = (size_t)s->o * s->o * s->v * s->v;
+    std::swap(s->Xn, s->dv[slot]);
+    s->t1n = view_of(s->Xn.p, ov);
+    s->Tn = view_of(s->Xn.p + s->xoff, t2n);
+    if (s->xoff > ov) fill(s->ctx, s->Xn.p + ov, s->xoff - ov, 0.0);
+}
+
+// After the sweep wrote its output xn into dv[slot] (diis_swap_output): x = the vector fed into
+// the sweep (length len, device); on return x holds the extrapolated vector and *ee = |xn - x|^2.
+static void diis_step(CCState *s, double *x, int slot, const std::vector<const double *> &olds, size_t len,
+                      double *ee) {
+    // the new error and its overlaps with the stored errors, in one pass
     std::vector<double> dots(olds.size() + 1);
-    diis_error(s->ctx, len, xn, x, s->dv[slot].p, s->de[slot].p, (int)olds.size(), olds.data(), dots.data());
+    diis_error(s->ctx, len, s->dv[slot].p, x, nullptr, s->de[slot].p, (int)olds.size(), olds.data(), dots.data());
     diis_finish(s, x, slot, len, dots, ee);
 }
 
@@ -736,21 +751,24 @@ static void cc_one(CCState *s, int prec) {
     JUES_CHECK_CUDA(cudaEventCreate(&e1));
     JUES_CHECK_CUDA(cudaEventRecord(e0, ctx->stream));
     double r2;
+    // with DIIS the sweep's output goes straight into the slot that keeps it
+    int slot = -1;
+    std::vector<const double *> olds;
+    const size_t dlen = s->method == 0 ? t2n : s->xoff + t2n;
+    if (s->opts.diis) {
+        slot = diis_begin(s, dlen, olds);
+        diis_swap_output(s, slot);
+    }
     if (s->method == 0) {
         r2 = ccd_sweep(s, prec);
     } else {
         r2 = ccsd_sweep(s, prec);
     }
     if (s->opts.diis) {
-        if (s->method == 0) {
-            double ee = 0.0;
-            diis_step(s, s->T.p, s->Tn.p, t2n, &ee);
-            if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
-        } else {
-            double ee = 0.0;
-            diis_step(s, s->X.p, s->Xn.p, s->xoff + t2n, &ee);
-            if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
-        }
+        diis_swap_output(s, slot);
+        double ee = 0.0;
+        diis_step(s, s->method == 0 ? s->T.p : s->X.p, slot, olds, dlen, &ee);
+        if (r2 < 0.0) r2 = ee;   // the sweep left the step norm to DIIS
     } else {
         std::swap(s->T, s->Tn);
         if (s->method == 1) {

@@ -332,7 +332,8 @@ void t1_fme(Ctx *ctx, const double *T, const double *Fme, int o, int v, double *
 // c1[n,e] = sum_m ooov[n,m,m,e], c2[n,e] = sum_m ooov[m,n,m,e], c3[n,e] = sum_m ooov[m,m,n,e] into
 // c12[0..ov), [ov..2ov), [2ov..3ov)
 void ooov_diag_sums(Ctx *ctx, const double *ooov, int o, int v, double *c12);
-// DIIS bookkeeping in one pass: v_out = xn, e_out = xn - x, dots[0] = e.e, dots[1 + k] = olds[k].e
+// DIIS bookkeeping in one pass: v_out = xn (skipped when null), e_out = xn - x, dots[0] = e.e,
+// dots[1 + k] = olds[k].e
 void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
                 const double *const *olds, double *dots);
 // 1 if any element of x is NaN/Inf

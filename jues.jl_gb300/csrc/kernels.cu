@@ -570,37 +570,32 @@ __global__ void lincomb_kernel(size_t n, VecList vl, double *__restrict__ out) {
     }
 }
 
-// DIIS bookkeeping of one sweep, pass 1: v = xn, e = xn - x and e.e (the same grid, products and
-// summation order as dot_kernel, so the sum is identical)
-__global__ void diis_pair_kernel(size_t n, const double *__restrict__ xn, const double *__restrict__ x,
-                                 double *__restrict__ v_out, double *__restrict__ e_out, double *part) {
-    double acc = 0.0;
+// DIIS bookkeeping of one sweep in one pass: e = xn - x (and v = xn when v_out is given), e.e (the
+// same grid, products and summation order as dot_kernel, so the sum is identical) and old_k.e for
+// the NOLD stored errors; row r of the partial sums at part[r gridDim.x + block].  The sweep
+// writes xn into its DIIS slot itself, so v_out is null there.
+template <int NOLD>
+__global__ void diis_pair_dots_kernel(size_t n, const double *__restrict__ xn, const double *__restrict__ x,
+                                      double *__restrict__ v_out, double *__restrict__ e_out, VecList olds,
+                                      double *part) {
+    double acc = 0.0, accs[NOLD > 0 ? NOLD : 1];
+#pragma unroll
+    for (int k = 0; k < NOLD; ++k) accs[k] = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const double xv = xn[i];
         const double e = xv - x[i];
-        v_out[i] = xv;
+        if (v_out) v_out[i] = xv;
         e_out[i] = e;
         acc = fma(e, e, acc);
+#pragma unroll
+        for (int k = 0; k < NOLD; ++k) accs[k] = fma(__ldg(olds.p[k] + i), e, accs[k]);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
-}
-
-// pass 2: old_k . e for the NOLD stored errors, e read once (loads only, no stores)
-template <int NOLD>
-__global__ void multi_dot_kernel(size_t n, VecList olds, const double *__restrict__ e, double *part) {
-    double acc[NOLD];
-#pragma unroll
-    for (int k = 0; k < NOLD; ++k) acc[k] = 0.0;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const double ei = e[i];
-#pragma unroll
-        for (int k = 0; k < NOLD; ++k) acc[k] = fma(__ldg(olds.p[k] + i), ei, acc[k]);
-    }
 #pragma unroll
     for (int k = 0; k < NOLD; ++k) {
-        const double v = block_sum(acc[k]);
-        if (threadIdx.x == 0) part[(size_t)k * gridDim.x + blockIdx.x] = v;
+        const double v = block_sum(accs[k]);
+        if (threadIdx.x == 0) part[(size_t)(1 + k) * gridDim.x + blockIdx.x] = v;
     }
 }
 
@@ -1157,24 +1152,20 @@ void t_tilde(Ctx *ctx, const double *T, int o, int v, double *out) {
 void diis_error(Ctx *ctx, size_t n, const double *xn, const double *x, double *v_out, double *e_out, int nold,
                 const double *const *olds, double *dots) {
     JUES_REQUIRE(nold >= 0 && nold <= 15, "diis_error supports up to 15 stored errors");
-    // partial sums: row 0 = e.e, rows 1..nold = old_k.e
+    // partial sums: row 0 = e.e, rows 1..nold = old_k.e, in one pass
     {
-        Ctx::Scope s(ctx, "diis_error");
-        diis_pair_kernel<<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, xn, x, v_out, e_out, ctx->d_red);
-        JUES_CHECK_CUDA(cudaGetLastError());
-    }
-    if (nold > 0) {
         VecList vl;
         for (int k = 0; k < nold; ++k) { vl.p[k] = olds[k]; vl.c[k] = 0.0; }
         Ctx::Scope s(ctx, "diis_error");
-        double *part = ctx->d_red + RED_BLOCKS;
+        double *part = ctx->d_red;
         switch (nold) {
-#define JUES_MULTI_DOT(K) \
-    case K: multi_dot_kernel<K><<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, vl, e_out, part); break;
-            JUES_MULTI_DOT(1) JUES_MULTI_DOT(2) JUES_MULTI_DOT(3) JUES_MULTI_DOT(4) JUES_MULTI_DOT(5)
-            JUES_MULTI_DOT(6) JUES_MULTI_DOT(7) JUES_MULTI_DOT(8) JUES_MULTI_DOT(9) JUES_MULTI_DOT(10)
-            JUES_MULTI_DOT(11) JUES_MULTI_DOT(12) JUES_MULTI_DOT(13) JUES_MULTI_DOT(14) JUES_MULTI_DOT(15)
-#undef JUES_MULTI_DOT
+#define JUES_DIIS_DOTS(K) \
+    case K: diis_pair_dots_kernel<K><<<RED_BLOCKS, RED_THREADS, 0, ctx->stream>>>(n, xn, x, v_out, e_out, vl, part); break;
+            JUES_DIIS_DOTS(0) JUES_DIIS_DOTS(1) JUES_DIIS_DOTS(2) JUES_DIIS_DOTS(3) JUES_DIIS_DOTS(4)
+            JUES_DIIS_DOTS(5) JUES_DIIS_DOTS(6) JUES_DIIS_DOTS(7) JUES_DIIS_DOTS(8) JUES_DIIS_DOTS(9)
+            JUES_DIIS_DOTS(10) JUES_DIIS_DOTS(11) JUES_DIIS_DOTS(12) JUES_DIIS_DOTS(13) JUES_DIIS_DOTS(14)
+            JUES_DIIS_DOTS(15)
+#undef JUES_DIIS_DOTS
         }
         JUES_CHECK_CUDA(cudaGetLastError());
     }
