@@ -8,6 +8,7 @@ an antisymmetric (-) part; the unfolded results must equal oovv + W'^T.T + T.vvv
 oovv.T^T and ooovQ + T.<am|ef> to rounding, on the S25 system's integrals and amplitudes.
 """
 import numpy as np
+import pytest
 
 from oracle import ccd, ccsd
 from oracle.mp2 import denominators
@@ -229,3 +230,41 @@ def test_folded_finalisation_equals_plain():
     want = (L + Z + Z.transpose(1, 0, 3, 2)) * invD
     assert np.abs(Tn - want).max() < 1e-13 * np.abs(want).max()
     assert np.array_equal(Tn, Tn.transpose(1, 0, 3, 2))   # pair-symmetric to the bit
+
+
+def _symmetric_blocks(o, v, rng, nq=5):
+    """Physicists' <pq|rs> with the full 8-fold symmetry, from a factorised (pr|qs)."""
+    n = o + v
+    B = rng.standard_normal((n, n, nq))
+    B = B + B.transpose(1, 0, 2)
+    phys = np.einsum("prQ,qsQ->pqrs", B, B)   # <pq|rs> = (pr|qs)
+    O, V = slice(0, o), slice(o, n)
+    return (np.asfortranarray(phys[O, O, V, V]), np.asfortranarray(phys[V, V, V, V]),
+            np.asfortranarray(phys[O, O, O, O]), np.asfortranarray(phys[O, V, V, V]))
+
+
+@pytest.mark.parametrize("o,v", [(1, 1), (1, 3), (2, 1), (3, 4), (5, 7), (8, 3)])
+def test_folded_chain_edge_sizes(o, v):
+    rng = np.random.default_rng(100 * o + v)
+    oovv, vvvv, oooo, ovvv = _symmetric_blocks(o, v, rng)
+    R = rng.standard_normal((o, o, v, v))
+    T = R + R.transpose(1, 0, 3, 2)
+    ooovQ = rng.standard_normal((o, o, v, o))
+    Wp, L, Y = folded(T, oovv, vvvv, oooo, ovvv=ovvv, ooovQ=ooovQ)
+    X = np.einsum("mnef,ijef->mnij", oovv, T)
+    Lp = oovv + np.einsum("mnij,mnab->ijab", oooo + X, T) + np.einsum("ijef,abef->ijab", T, vvvv)
+    Yp = ooovQ + np.einsum("ijef,mafe->ijam", T, ovvv)
+    scale = lambda a: max(1.0, np.abs(a).max())  # noqa: E731
+    assert np.abs(Wp - (oooo + X)).max() < 1e-12 * scale(Wp)
+    assert np.abs(L - Lp).max() < 1e-12 * scale(Lp)
+    assert np.abs(Y - Yp).max() < 1e-12 * scale(Yp)
+    # the finalisation from the folded ladders
+    e = np.sort(rng.standard_normal(o + v)) + np.r_[np.full(o, -5.0), np.full(v, 5.0)]
+    D = e[:o, None, None, None] + e[None, :o, None, None] - e[None, None, o:, None] - e[None, None, None, o:]
+    Z = rng.standard_normal((o, o, v, v))
+    np_, nq = o * (o + 1) // 2, v * (v + 1) // 2
+    Lpm = pair_fold(fl(Lp), np_, True, 0, 1, o, v, o * o, o * o * v, 0.5, False)
+    Tn = finalize_fold(Lpm, Z, inv_folded(e, o, v), o, v)
+    want = (Lp + Z + Z.transpose(1, 0, 3, 2)) / D
+    assert np.abs(Tn - want).max() < 1e-12 * scale(want)
+    assert np.array_equal(Tn, Tn.transpose(1, 0, 3, 2))
