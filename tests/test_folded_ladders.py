@@ -268,3 +268,42 @@ def test_folded_chain_edge_sizes(o, v):
     want = (Lp + Z + Z.transpose(1, 0, 3, 2)) / D
     assert np.abs(Tn - want).max() < 1e-12 * scale(want)
     assert np.array_equal(Tn, Tn.transpose(1, 0, 3, 2))
+
+
+BIG = 1 << 60
+
+
+def mode_offsets(mode, n):
+    """common.cuh Mode{d0, d1, s0, s1, s2}: offset (r % d0) s0 + ((r / d0) % d1) s1 + (r / (d0 d1)) s2."""
+    d0, d1, s0, s1, s2 = mode
+    r = np.arange(n, dtype=np.int64)
+    return (r % d0) * s0 + ((r // d0) % d1) * s1 + (r // (d0 * d1 if d0 * d1 < BIG else BIG)) * s2
+
+
+def mode2(d0, s0, s1):
+    return (d0, BIG, s0, s1, 0)
+
+
+def plain(s):
+    return (BIG, 1, s, 0, 0)
+
+
+def test_t1_fme_terms_as_one_gemm_on_the_ring_packs():
+    """ccsd_sweep (split): sum_me (2 T2[i,m,a,e] - T2[m,i,a,e]) Fme[m,e] = [R1 | R23] . [2 Fme ; -Fme]
+    with R1 = T2 packed as rows (i,a) mode2(o,1,oo), K (m,e) mode2(o,o,oov) and R23 as rows
+    mode2(o,o,oo), K mode2(o,1,oov) (ring_stacks_begin), and Fme packed along K with plain(1)."""
+    rng = np.random.default_rng(11)
+    o, v = 3, 5
+    oo, ov, oov = o * o, o * v, o * o * v
+    T = rng.standard_normal((o, o, v, v))
+    T = T + T.transpose(1, 0, 3, 2)
+    Fme = rng.standard_normal((o, v))
+    Tf, Ff = fl(T), fl(Fme)
+    rows1, k1 = mode_offsets(mode2(o, 1, oo), ov), mode_offsets(mode2(o, o, oov), ov)
+    rows2, k2 = mode_offsets(mode2(o, o, oo), ov), mode_offsets(mode2(o, 1, oov), ov)
+    R1 = Tf[rows1[:, None] + k1[None, :]]
+    R23 = Tf[rows2[:, None] + k2[None, :]]
+    B = np.concatenate([2.0 * Ff[mode_offsets(plain(1), ov)], -Ff[mode_offsets(plain(1), ov)]])
+    got = np.hstack([R1, R23]) @ B                      # rows r = i + o a: t1's layout
+    want = np.einsum("imae,me->ia", 2.0 * T - T.transpose(1, 0, 2, 3), Fme)
+    assert np.abs(got - fl(want)).max() < 1e-13
